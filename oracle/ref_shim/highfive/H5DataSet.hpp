@@ -1,0 +1,2 @@
+#pragma once
+#include <highfive/H5File.hpp>
