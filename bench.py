@@ -1,0 +1,281 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the FDTD time-stepping hot path.
+
+Workload: the dispersive-scattering configuration (ffip_gb300.workloads.
+dispersive_spheres(256)): 256^3 Yee cells, 16-cell CPML, 64 Lorentz/Drude
+spheres, an Ex current sheet, a 128x128x32 Ex DFT monitor at 5 frequencies.
+One "step" is one FDTD time step (H and E half steps with CPML, ADE and DFT)
+over the whole grid.  Metric: Yee cell-updates per second (256^3 per step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm (default) times K steps of the fp32-state stepper (fp64 DFT sums) with
+CUDA events on the stepper's stream, inputs resident in HBM; the state (about
+0.9 GB) is far larger than the 129 MB L2, so no flush is needed between steps.
+It also reports the fp64 stepper, the fp32-vs-fp64 DFT error of a full
+4000-step run, an end-to-end figure through the C ABI (config in, DFT arrays
+out, set-up and copies inside the timed region), the roofline of the step
+kernel(s) and a CPU baseline (the oracle's restatement of the reference's
+loops on all host cores, a bounded sample of steps).
+
+--impl reference times that CPU restatement of the reference's own loops
+(oracle/port.py + oracle/step.c) on the host cores, K steps after W warm-up
+steps, on the same workload.
+
+Multi-GPU: the stepper does not shard here (one GPU per box); with torchrun
+each rank runs an independent replica on its own GPU ("replicas only"),
+value = all ranks' cell-updates / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Yee cell-updates/s (fp32 state, fp64 DFT), dispersive 256^3"
+UNIT = "Gcell-updates/s"
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("gloo", rank=rank, world_size=world)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(world, v):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([float(v)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return v
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.rows = []
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+        return self
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for i, n in enumerate(names):
+                if len(r) > 5 + i and r[5 + i].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dft_rel_err(a, b):
+    g = "volume fields dft 0"
+    scale = max(np.abs(b[g]["real"]).max(), np.abs(b[g]["imag"]).max())
+    return float(max(np.abs(a[g]["real"] - b[g]["real"]).max(), np.abs(a[g]["imag"] - b[g]["imag"]).max()) / scale)
+
+
+def cpu_leg(cfg, steps, warmup, threads):
+    """The oracle's restatement of the reference's stepping loops, timed."""
+    from oracle import port
+    t0 = time.perf_counter()
+    sim = port.OracleSim(cfg, {}, threads=threads)
+    setup = time.perf_counter() - t0
+    sim.run_steps(warmup)
+    t0 = time.perf_counter()
+    sim.run_steps(steps)
+    dt = time.perf_counter() - t0
+    return dt, setup
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="cells per axis of the workload")
+    ap.add_argument("--cpu-steps", type=int, default=8, help="steps timed for the CPU baseline sample")
+    ap.add_argument("--skip-full-run", action="store_true", help="skip the full-length fp32/fp64 runs")
+    ap.add_argument("--engine", default="auto")
+    a = ap.parse_args()
+    world, rank, local = dist_init()
+    from ffip_gb300 import workloads
+    warm = max(3, a.warmup)
+    n = a.n
+    cells = float(n) ** 3
+    cfg_meta = {"workload": "dispersive spheres %d^3, 16-cell CPML, 64 Lorentz/Drude spheres, Ex sheet, "
+                            "128x128x32 Ex DFT x5 freqs" % n if n == 256 else "dispersive spheres %d^3" % n,
+                "cells": int(cells), "steps_full_run": workloads.dispersive_spheres(n)["stop condition"]["time"] / 0.5,
+                "l2": "state (~0.9 GB fp32) exceeds the 129 MB L2; no flush needed",
+                "parallelism": "replicas" if world > 1 else "single GPU"}
+
+    if a.impl == "reference":
+        if rank != 0:
+            return 0
+        threads = os.cpu_count() or 1
+        cfg = workloads.dispersive_spheres(n, precision="fp64")
+        dt, setup = cpu_leg(cfg, a.steps, warm, threads)
+        v = cells * a.steps / dt / 1e9
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
+                "warmup": warm, "ms_per_step": dt / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg_meta,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": "%d time steps of the full workload after %d warm-up steps (set-up %.1f s untimed)"
+                                           % (a.steps, warm, setup)},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    from ffip_gb300 import native
+    native.load()
+    dev = local
+    peak, peak_kind = peaks()
+
+    def make(prec):
+        cfg = workloads.dispersive_spheres(n, precision=prec, engine=a.engine)
+        cfg["device"] = dev
+        return cfg
+
+    # ---- device-resident throughput, fp32 and fp64
+    res = {}
+    clocks = None
+    for prec in ("fp32", "fp64"):
+        s = native.NativeSim(make(prec))
+        s.step(warm)
+        st0 = s.stats()
+        barrier(world)
+        if prec == "fp32":
+            with ClockSampler(dev) as cs:
+                ms = s.step_timed(a.steps)
+            clocks = cs.summary()
+        else:
+            ms = s.step_timed(a.steps)
+        barrier(world)
+        st1 = s.stats()
+        ms = allmax(world, ms)
+        res[prec] = {"ms": ms, "launches": st1["kernel_launches"] - st0["kernel_launches"],
+                     "bytes_per_step": st1["bytes_per_step"], "fused": st1["fused"]}
+        s.close()
+    t32 = res["fp32"]["ms"] / a.steps
+    t64 = res["fp64"]["ms"] / a.steps
+    value = world * cells / (t32 * 1e-3) / 1e9
+    v64 = world * cells / (t64 * 1e-3) / 1e9
+    achieved = res["fp32"]["bytes_per_step"] / (t32 * 1e-3) / 1e9
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": warm,
+           "ms_per_step": t32, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded spheres, no dataset)", "config": cfg_meta,
+           "gpu_launches": res["fp32"]["launches"],
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                        "traffic": None, "peak_kind": peak_kind,
+                        "kernel": "k_fused" if res["fp32"]["fused"] else "k_update (H and E launches)",
+                        "algorithmic_bytes_per_step": res["fp32"]["bytes_per_step"],
+                        "timing": "CUDA events on the stepper's stream around the %d timed steps" % a.steps},
+           "fp64": {"value": v64, "unit": UNIT, "ms_per_step": t64, "fp32_speedup": t64 / t32,
+                    "achieved_gbs": res["fp64"]["bytes_per_step"] / (t64 * 1e-3) / 1e9},
+           "clocks": clocks}
+
+    # ---- full runs: fp32-vs-fp64 DFT error and end-to-end through the C ABI
+    if not a.skip_full_run:
+        full = {}
+        e2e = None
+        for prec in ("fp32", "fp64"):
+            barrier(world)
+            t0 = time.perf_counter()
+            s = native.NativeSim(make(prec))
+            s.run()
+            o = s.outputs()
+            dt = time.perf_counter() - t0
+            st = s.stats()
+            s.close()
+            dt = allmax(world, dt)
+            full[prec] = o
+            if prec == "fp32":
+                steps_run = st["time_step"]
+                e2e = {"value": world * cells * steps_run / dt / 1e9, "unit": UNIT,
+                       "h2d_bytes_per_step": st["h2d_bytes"] / steps_run, "d2h_bytes_per_step": st["d2h_bytes"] / steps_run,
+                       "unit_of_work": "one full %d-step run through ffip_create/ffip_run/ffip_output_* "
+                                       "(config JSON in from the host, set-up, stepping, DFT arrays out)" % steps_run,
+                       "seconds": dt}
+        out["e2e"] = e2e
+        out["dft_rel_err_fp32_vs_fp64"] = dft_rel_err(full["fp32"], full["fp64"])
+
+    # ---- CPU baseline sample (rank 0 only)
+    if rank == 0 and world == 1:
+        threads = os.cpu_count() or 1
+        try:
+            dt, setup = cpu_leg(workloads.dispersive_spheres(n, precision="fp64"), a.cpu_steps, 2, threads)
+            out["cpu_baseline"] = {"value": cells * a.cpu_steps / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+                                   "sample": "%d time steps of the full workload after 2 warm-up steps, set-up (%.1f s) untimed"
+                                             % (a.cpu_steps, setup)}
+        except Exception as e:  # the baseline is reported, not required
+            out["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": threads, "kind": "port", "error": str(e)}
+    if rank == 0:
+        print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,77 @@
+"""Builds the native library ffip_gb300/_lib/libffip_gb300.so in-tree:
+CUDA sources with nvcc for sm_103a, host C++ with g++, linked by nvcc.
+Translation units compile in parallel."""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+LIBDIR = os.path.join(HERE, "_lib")
+LIB = os.path.join(LIBDIR, "libffip_gb300.so")
+
+CUDA_SOURCES = ["kernels.cu", "adjoint.cu"]
+CXX_SOURCES = ["plan.cpp", "engine.cpp", "capi.cpp"]
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.sep not in c or os.path.exists(c)):
+            return c
+    return "nvcc"
+
+
+def _deps_mtime() -> float:
+    m = 0.0
+    for d in (CSRC, os.path.join(ROOT, "include")):
+        for f in os.listdir(d):
+            m = max(m, os.path.getmtime(os.path.join(d, f)))
+    return m
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    nvcc = _nvcc()
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
+    jobs = []
+    objs = []
+    for s in CUDA_SOURCES:
+        o = os.path.join(BUILD, s + ".o")
+        objs.append(o)
+        jobs.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+                     "-Xptxas", "-warn-spills", *inc, "-c", os.path.join(CSRC, s), "-o", o])
+    for s in CXX_SOURCES:
+        o = os.path.join(BUILD, s + ".o")
+        objs.append(o)
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", *inc,
+                     "-I", "/usr/local/cuda/include", "-c", os.path.join(CSRC, s), "-o", o])
+    procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)) for j in jobs]
+    failed = []
+    for j, p in procs:
+        out = p.communicate()[0].decode(errors="replace")
+        if p.returncode != 0:
+            failed.append((j, out))
+        elif verbose and out.strip():
+            print(out)
+    if failed:
+        msg = "\n\n".join(" ".join(j) + "\n" + out for j, out in failed)
+        raise RuntimeError("native build failed:\n" + msg)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+    r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("native link failed:\n" + r.stdout.decode(errors="replace"))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

@@ -1,0 +1,87 @@
+// Time-stepping engine: owns the device state of one simulation and drives
+// the kernels in the reference's half-step order (Simulation::step_m /
+// step_e, src/simulation.cpp:748-766).  Memory and launches go through a
+// Backend; the product library links the CUDA backend (kernels.cu).
+#pragma once
+#include <cstdint>
+#include <functional>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "plan.hpp"
+#include "stencil.cuh"
+
+namespace ffipg
+{
+// Fused H+E pass parameters (None boundaries, no magnetic poles): the H
+// update of one z plane and the E update of the same plane in one kernel,
+// ping-ponging field buffers between steps.  See kernels.cu.
+template <typename T>
+struct FusedParams
+{
+    SideParams<T> h, e;   // h.f/e.f = output buffers, h.o/e.o unused
+    const T *ein[3];      // E at step n (input buffers)
+    const T *hin[3];      // H at step n-1/2 (input buffers)
+    T *eout[3], *hout[3]; // outputs
+    const T *psih_in[3][2];
+    T *psih_out[3][2];
+};
+
+struct Backend
+{
+    virtual ~Backend() {}
+    virtual void *alloc(size_t bytes) = 0;  // returns zero-filled memory
+    virtual void release(void *p) = 0;
+    virtual void h2d(void *dst, const void *src, size_t bytes) = 0;
+    virtual void d2h(void *dst, const void *src, size_t bytes) = 0;
+    virtual void zero(void *p, size_t bytes) = 0;
+    virtual void sync() = 0;
+    virtual void update(const SideParams<double> &p, bool is_e) = 0;
+    virtual void update(const SideParams<float> &p, bool is_e) = 0;
+    virtual bool has_fused() const { return false; }
+    virtual void fused(const FusedParams<double> &) {}
+    virtual void fused(const FusedParams<float> &) {}
+    virtual void sources(const SourceParams<double> &p) = 0;
+    virtual void sources(const SourceParams<float> &p) = 0;
+    virtual void ghosts(const GhostParams<double> &p) = 0;
+    virtual void ghosts(const GhostParams<float> &p) = 0;
+    // value of a trilinear probe (up to 8 weighted points) -> out[0]
+    virtual void probe(const double *f, const int64_t *lin, const double *w, int n, double *out) = 0;
+    virtual void probe(const float *f, const int64_t *lin, const double *w, int n, double *out) = 0;
+    // sum over i of re[i]^2 + im[i]^2 -> out[0]
+    virtual void dft_norm(const double *re, const double *im, int64_t n, double *out) = 0;
+    virtual const char *name() const = 0;
+    // device time of f() between events on the backend's stream (ms)
+    virtual double timed(const std::function<void()> &f) = 0;
+    uint64_t h2d_bytes{0}, d2h_bytes{0};
+};
+
+struct OutputGroup
+{
+    std::string group;
+    std::vector<std::string> names;
+    std::vector<std::vector<uint64_t>> shapes;
+    std::vector<std::vector<double>> data;
+};
+
+class EngineBase
+{
+public:
+    virtual ~EngineBase() {}
+    virtual void step(int64_t n) = 0;
+    virtual void run(const Json &stop) = 0;
+    virtual int64_t time_step() const = 0;
+    virtual std::vector<OutputGroup> outputs() = 0;
+    virtual void reset() = 0;
+    virtual void set_density(const std::string &dataset, const double *rho, uint64_t n) = 0;
+    virtual const Plan &plan() const = 0;
+    virtual bool fused() const = 0;
+    virtual int64_t launches() const = 0;  // kernel launches issued so far
+    // algorithmic bytes of one full time step, and the number of Yee cells
+    virtual double bytes_per_step() const = 0;
+};
+
+std::unique_ptr<EngineBase> make_engine(Plan &&plan, Backend *be);
+} // namespace ffipg

@@ -1,0 +1,206 @@
+"""ctypes binding of the C ABI in include/ffip_gb300.h.
+
+``load()`` returns the in-tree native library ffip_gb300/_lib/libffip_gb300.so
+(building it first if needed) and raises if it cannot be built or loaded:
+there is no CPU fallback.  ``NativeSim`` wraps one simulation handle;
+``run_json`` is the one-call form of the reference's run_sim_json
+(app/run_sim_json.cpp): config + datasets in, output datasets out.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+class FfipError(RuntimeError):
+    pass
+
+
+class Dataset(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("data", ctypes.POINTER(ctypes.c_double)), ("n", ctypes.c_uint64)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("time_step", ctypes.c_int64), ("yee_cells", ctypes.c_int64), ("array_cells", ctypes.c_int64),
+                ("dt", ctypes.c_double), ("dx", ctypes.c_double), ("bytes_per_step", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64), ("fused", ctypes.c_int32), ("fp32", ctypes.c_int32),
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+
+
+EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_run", "ffip_output_count", "ffip_output_group", "ffip_output_array",
+           "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync", "ffip_stream", "ffip_destroy",
+           "ffip_last_error", "ffip_transpose", "ffip_sensitivity"]
+
+
+def _declare(lib):
+    P, D, U64, I64 = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_uint64, ctypes.c_int64
+    lib.ffip_create.argtypes = [ctypes.c_char_p, ctypes.POINTER(Dataset), U64, ctypes.POINTER(P)]
+    lib.ffip_step.argtypes = [P, I64]
+    lib.ffip_step_timed.argtypes = [P, I64, ctypes.POINTER(ctypes.c_double)]
+    lib.ffip_run.argtypes = [P, ctypes.c_char_p]
+    lib.ffip_output_count.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
+    lib.ffip_output_group.argtypes = [P, ctypes.c_int, ctypes.c_char_p, U64]
+    lib.ffip_output_array.argtypes = [P, ctypes.c_int, ctypes.c_char_p, D, U64, ctypes.POINTER(U64), ctypes.POINTER(ctypes.c_int)]
+    lib.ffip_set_density.argtypes = [P, ctypes.c_char_p, D, U64]
+    lib.ffip_reset.argtypes = [P]
+    lib.ffip_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
+    lib.ffip_sync.argtypes = [P]
+    lib.ffip_stream.argtypes = [P]
+    lib.ffip_stream.restype = P
+    lib.ffip_destroy.argtypes = [P]
+    lib.ffip_last_error.restype = ctypes.c_char_p
+    lib.ffip_transpose.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
+    lib.ffip_sensitivity.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, U64, D, U64, D, U64,
+                                     D, U64, D]
+    for f in EXPORTS:
+        if f not in ("ffip_stream", "ffip_last_error"):
+            getattr(lib, f).restype = ctypes.c_int
+    return lib
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return os.path.join(_HERE, "_lib", "libffip_gb300.so")
+
+
+def load(path: Optional[str] = None):
+    """Loads (building if stale) the native library; raises FfipError if that fails."""
+    global _lib
+    if path is not None:
+        return _declare(ctypes.CDLL(path))
+    if _lib is None:
+        try:
+            from . import build as _build
+            p = _build.build()
+        except Exception as e:  # no silent fallback: the CUDA library is the product
+            raise FfipError("cannot build the ffip_gb300 CUDA library: %s" % e) from e
+        _lib = _declare(ctypes.CDLL(p))
+    return _lib
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class NativeSim:
+    """One simulation handle (ffip_create ... ffip_destroy)."""
+
+    def __init__(self, config: dict, datasets: Optional[Dict[str, np.ndarray]] = None, lib=None):
+        self.lib = lib if lib is not None else load()
+        self._arrays = []
+        ds = datasets or {}
+        arr = (Dataset * max(1, len(ds)))()
+        for i, (k, v) in enumerate(ds.items()):
+            a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel())
+            self._arrays.append(a)
+            arr[i] = Dataset(k.encode(), _dptr(a), a.size)
+        h = ctypes.c_void_p()
+        self._check(self.lib.ffip_create(json.dumps(config).encode(), arr, len(ds), ctypes.byref(h)))
+        self.h = h
+        self.config = config
+
+    def _check(self, rc):
+        if rc != 0:
+            raise FfipError("ffip error %d: %s" % (rc, self.lib.ffip_last_error().decode(errors="replace")))
+
+    def step(self, n: int):
+        self._check(self.lib.ffip_step(self.h, int(n)))
+
+    def step_timed(self, n: int) -> float:
+        """Runs n steps; returns their device time in ms (CUDA events on the handle's stream)."""
+        ms = ctypes.c_double()
+        self._check(self.lib.ffip_step_timed(self.h, int(n), ctypes.byref(ms)))
+        return ms.value
+
+    def run(self, stop: Optional[dict] = None):
+        self._check(self.lib.ffip_run(self.h, json.dumps(stop).encode() if stop is not None else None))
+
+    def sync(self):
+        self._check(self.lib.ffip_sync(self.h))
+
+    def reset(self):
+        self._check(self.lib.ffip_reset(self.h))
+
+    def set_density(self, dataset: str, rho: np.ndarray):
+        a = np.ascontiguousarray(np.asarray(rho, dtype=np.float64).ravel())
+        self._check(self.lib.ffip_set_density(self.h, dataset.encode(), _dptr(a), a.size))
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.lib.ffip_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def stream(self) -> int:
+        return self.lib.ffip_stream(self.h) or 0
+
+    def outputs(self) -> dict:
+        n = ctypes.c_int()
+        self._check(self.lib.ffip_output_count(self.h, ctypes.byref(n)))
+        out = {}
+        name = ctypes.create_string_buffer(4096)
+        for g in range(n.value):
+            self._check(self.lib.ffip_output_group(self.h, g, name, 4096))
+            grp = {}
+            for arr in ("real", "imag", "x", "y", "z", "f"):
+                dims = (ctypes.c_uint64 * 4)()
+                nd = ctypes.c_int()
+                rc = self.lib.ffip_output_array(self.h, g, arr.encode(), None, 0, dims, ctypes.byref(nd))
+                if rc == -3:
+                    continue
+                self._check(rc)
+                shape = tuple(int(dims[i]) for i in range(nd.value))
+                a = np.zeros(int(np.prod(shape)) if shape else 0, dtype=np.float64)
+                self._check(self.lib.ffip_output_array(self.h, g, arr.encode(), _dptr(a), a.size, dims, ctypes.byref(nd)))
+                grp[arr] = a.reshape(shape)
+            out[name.value.decode()] = grp
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ffip_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def run_json(config: dict, datasets: Optional[Dict[str, np.ndarray]] = None, lib=None) -> dict:
+    """config + datasets -> {group: {array: ndarray}}, like run_sim_json."""
+    with NativeSim(config, datasets, lib=lib) as s:
+        s.run(config["stop condition"])
+        return s.outputs()
+
+
+def transpose(gx, gy, gz, pt, lib=None) -> np.ndarray:
+    """_ffip.transpose (app/ffip.cpp:308-352) on the GPU."""
+    L = lib if lib is not None else load()
+    gx, gy, gz = (np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel()) for v in (gx, gy, gz))
+    pt = np.ascontiguousarray(np.asarray(pt, dtype=np.float64))
+    if gx.size < 1 or gy.size < 1 or gz.size < 1:
+        raise KeyError("some grid size is 0")
+    if pt.ndim != 2:
+        raise KeyError("some dimensions are not right")
+    if pt.shape[1] != 4:
+        raise ValueError("shape(1) of pts is not 4")
+    out = np.zeros((gz.size, gy.size, gx.size), dtype=np.float64)
+    rc = L.ffip_transpose(_dptr(gx), gx.size, _dptr(gy), gy.size, _dptr(gz), gz.size, _dptr(pt), pt.shape[0], _dptr(out))
+    if rc != 0:
+        raise FfipError(L.ffip_last_error().decode())
+    return out

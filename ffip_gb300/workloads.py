@@ -1,0 +1,96 @@
+"""Seeded synthetic workloads in the reference's config schema.
+
+``dispersive_spheres(n=256)`` is the dispersive-scattering workload the
+throughput figures are quoted on: an n^3-cell box, dx = 1, Courant 0.5,
+CPML of n/16 cells (order 3, sigma_max = -(m+1) ln(1e-8) / (2 d)), background
+vacuum, 64 spheres (centres uniform in the non-CPML interior, radii uniform
+4-16 cells scaled by n/256) of which half use one 2-pole Lorentz medium
+(eps_inf 2, delta-eps U(0.5, 3), omega_0 U(0.05, 0.2), gamma U(0.001, 0.02))
+and half one Drude medium (omega_p U(0.3, 1.0), gamma U(0.005, 0.05)); an Ex
+current sheet at z index 3n/32 with a Gaussian1 pulse at f = 0.1; a DFT volume
+monitor of Ex, n/2 x n/2 x n/8 cells, centred, at 5 frequencies in
+[0.06, 0.14]; 4000 steps at n = 256 (scaled by n/256 below that).
+
+Angular rates: omega_0, omega_p and gamma are taken as angular (rad per unit
+time), so the reference's "frequency"/"gamma" parameters (which it multiplies
+by 2 pi, src/medium.cpp:98-108) are omega / (2 pi).  Read as plain frequency
+parameters, Drude plasma frequencies above about 0.45 make the reference's
+own ADE update diverge at Courant 0.5.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+TWO_PI = 2 * math.pi
+
+
+def medium(eps=1.0, mu=1.0, esus=()):
+    return {"epsilon": eps, "mu": mu, "electric conductivity": 0.0, "magnetic conductivity": 0.0,
+            "electric susceptibility": list(esus), "magnetic susceptibility": []}
+
+
+def sigma_max(order: int, thickness: float, R: float = 1e-8) -> float:
+    """sigma_max for a polynomial CPML of given order and reflection R."""
+    return -(order + 1) * math.log(R) / (2 * thickness)
+
+
+def dispersive_spheres(n: int = 256, steps: int | None = None, seed: int = 2024, precision: str = "fp32",
+                       engine: str = "auto") -> dict:
+    rng = np.random.default_rng(seed)
+    scale = n / 256.0
+    pml = max(2, int(round(16 * scale)))
+    half = n / 2.0
+    lor = medium(2.0, esus=[{"type": "Lorentz", "frequency": rng.uniform(0.05, 0.2) / TWO_PI,
+                             "gamma": rng.uniform(0.001, 0.02) / TWO_PI, "amplitude": rng.uniform(0.5, 3.0)}
+                            for _ in range(2)])
+    dru = medium(1.0, esus=[{"type": "Drude", "frequency": rng.uniform(0.3, 1.0) / TWO_PI,
+                             "gamma": rng.uniform(0.005, 0.05) / TWO_PI, "amplitude": 1.0}])
+    geoms = []
+    lo, hi = -half + pml, half - pml
+    for s in range(64):
+        r = rng.uniform(4, 16) * scale
+        c = rng.uniform(lo, hi, size=3)
+        geoms.append({"type": "sphere", "center": [float(v) for v in c], "radius": float(r),
+                      "medium": lor if s % 2 == 0 else dru})
+    z_sheet = -half + 24 * scale
+    cfg = {
+        "courant number": 0.5, "resolution": 1.0, "size": [float(n)] * 3,
+        "input file": "input.h5", "fields output file": "output.h5",
+        "default material": medium(), "progress interval": 1e9,
+        "PML": [{"thickness": float(pml), "k max": 1.0, "sigma max": sigma_max(3, pml), "order": 3}],
+        "geometry": geoms,
+        "sources": [{"type": "volume source", "center": [0.0, 0.0, z_sheet], "size": [n - 2.0 * pml, n - 2.0 * pml, 0.0],
+                     "amplitude": 1.0, "field component": "Ex",
+                     "function": {"type": "Gaussian1", "frequency": 0.1, "cutoff": 4.0, "start time": 0.0}}],
+        "fields output": [{"type": "volume fields dft", "center": [0.0, 0.0, 0.0], "size": [n / 2.0, n / 2.0, n / 8.0],
+                           "frequency": [float(f) for f in np.linspace(0.06, 0.14, 5)], "field component": "Ex",
+                           "output group": "volume fields dft 0"}],
+        "precision": precision, "engine": engine,
+    }
+    nsteps = steps if steps is not None else max(100, int(round(4000 * scale)))
+    cfg["stop condition"] = {"type": "time", "time": nsteps * 0.5}
+    return cfg
+
+
+def vacuum_point(n: int = 64, steps: int = 1000, seed: int = 7, precision: str = "fp64", engine: str = "auto") -> dict:
+    """n^3 vacuum box, 8-cell CPML (order 3, R = 1e-8), one Ez point current at
+    a seeded interior cell (Gaussian1, f = 0.1), DFT Ez plane at z = +n/4 at
+    3 frequencies."""
+    rng = np.random.default_rng(seed)
+    pml = 8
+    half = n / 2
+    c = rng.integers(int(-half + pml + 2), int(half - pml - 2), size=3)
+    return {
+        "courant number": 0.5, "resolution": 1.0, "size": [float(n)] * 3,
+        "input file": "input.h5", "fields output file": "output.h5", "default material": medium(),
+        "PML": [{"thickness": float(pml), "k max": 1.0, "sigma max": sigma_max(3, pml), "order": 3}],
+        "sources": [{"type": "volume source", "center": [float(c[0]), float(c[1]), float(c[2]) + 0.5], "size": [0.0, 0.0, 0.0],
+                     "amplitude": 1.0, "field component": "Ez",
+                     "function": {"type": "Gaussian1", "frequency": 0.1, "cutoff": 4.0, "start time": 0.0}}],
+        "fields output": [{"type": "volume fields dft", "center": [0.0, 0.0, n / 4.0], "size": [float(n), float(n), 0.0],
+                           "frequency": [0.08, 0.1, 0.12], "field component": "Ez", "output group": "volume fields dft 0"}],
+        "stop condition": {"type": "time", "time": steps * 0.5},
+        "precision": precision, "engine": engine,
+    }

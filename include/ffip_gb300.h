@@ -1,0 +1,137 @@
+/*
+ * ffip_gb300 — C ABI of the GB300 (sm_103a) FDTD stepper.
+ *
+ * The reference (ffip) has no C ABI: its hot path is reached through the
+ * run_sim_json CLI (app/run_sim_json.cpp:6-25), which reads config.json and
+ * the HDF5 input file, runs Simulation::init / run / output
+ * (src/simulation.cpp:127-188, 903-958, 967-977) and writes the HDF5 output
+ * file, and through the pybind module _ffip (app/ffip.cpp:390-415).  Each
+ * entry point below names the reference interface it replaces.  The config
+ * JSON is the reference's schema unchanged (what ffip/simulation.py:362-402
+ * emits); input datasets are passed as named float64 arrays instead of an
+ * HDF5 file; outputs are read back as named float64 arrays with the
+ * reference's dataset names and shapes.
+ *
+ * Conventions: every function returns 0 (FFIP_OK) or a negative error code
+ * and never aborts; ffip_last_error() gives the message of the calling
+ * thread's last failure.  Host buffers belong to the caller; device memory
+ * belongs to the handle.  Calls on one handle must be serialised; distinct
+ * handles are independent.  A handle runs on one CUDA device, on its own
+ * stream.
+ */
+#ifndef FFIP_GB300_H
+#define FFIP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FFIP_OK 0
+#define FFIP_ERR_INVALID (-1)   /* bad argument, config or dataset */
+#define FFIP_ERR_CUDA (-2)      /* CUDA runtime failure (no device, out of memory, ...) */
+#define FFIP_ERR_NOT_FOUND (-3) /* unknown output group / array / dataset */
+#define FFIP_ERR_INTERNAL (-4)
+
+typedef struct ffip_sim ffip_sim;
+
+/* One named input dataset (the reference reads these from "input file",
+ * src/simulation.cpp:151-153,301-306,431-496; ffip/geom.py:432-433,528-545;
+ * ffip/source.py:127-129). Arrays are flattened in [z][y][x] order. */
+typedef struct ffip_dataset {
+    const char *name;
+    const double *data;
+    uint64_t n;
+} ffip_dataset;
+
+typedef struct ffip_stats {
+    int64_t time_step;       /* completed time steps */
+    int64_t yee_cells;       /* (size/dx) per axis, multiplied */
+    int64_t array_cells;     /* padded cells per component array */
+    double dt, dx;
+    double bytes_per_step;   /* algorithmic bytes of one time step */
+    int64_t kernel_launches; /* kernel launches issued so far */
+    int32_t fused;           /* 1 = fused H+E pass, 0 = separate H and E passes */
+    int32_t fp32;            /* 1 = fp32 field state, 0 = fp64 */
+    uint64_t h2d_bytes;      /* host->device bytes copied so far */
+    uint64_t d2h_bytes;      /* device->host bytes copied so far */
+} ffip_stats;
+
+/* Simulation::init(config) (src/simulation.cpp:127-188): parses the config
+ * JSON, builds the grid, CPML, media, sources and DFT monitors, and uploads
+ * them to a CUDA device.  Rebuild-only keys: "precision" ("fp64" default,
+ * "fp32" = fp32 field state with fp64 DFT sums), "engine" ("auto", "fused",
+ * "unfused") and "device" (CUDA device index; default: the device current
+ * in the calling thread). */
+int ffip_create(const char *config_json, const ffip_dataset *datasets, uint64_t n_datasets, ffip_sim **out);
+
+/* n iterations of the time loop body of Simulation::run_until_time
+ * (step_m, step_e, ++time_step; src/simulation.cpp:773-779). */
+int ffip_step(ffip_sim *sim, int64_t n_steps);
+
+/* ffip_step with device timing: CUDA events recorded on the handle's stream
+ * before and after the n steps; *ms receives the elapsed device time.
+ * Blocks until the steps have finished. */
+int ffip_step_timed(ffip_sim *sim, int64_t n_steps, double *ms);
+
+/* Simulation::run(stop_cond) (src/simulation.cpp:903-958): "time", "decay"
+ * or DFT steady-state stop conditions.  stop_json == NULL uses the config's
+ * "stop condition".  Like the reference, time_step restarts from 0 only at
+ * creation / ffip_reset. */
+int ffip_run(ffip_sim *sim, const char *stop_json);
+
+/* Output datasets, as Simulation::output writes them (src/simulation.cpp:
+ * 967-977, src/dft.cpp:273-320, geometry info src/simulation.cpp:190-233).
+ * ffip_output_count collects the current values from the device. */
+int ffip_output_count(ffip_sim *sim, int *n_groups);
+int ffip_output_group(ffip_sim *sim, int group, char *name, uint64_t name_cap);
+/* Copies array `array` ("real", "imag", "x", "y", "z", "f") of group `group`
+ * into out[n] (out may be NULL to query the shape); dims/ndim receive the
+ * shape ([nf, nz, ny, nx] for real/imag). */
+int ffip_output_array(ffip_sim *sim, int group, const char *array, double *out, uint64_t n, uint64_t dims[4], int *ndim);
+
+/* Replaces the density of the two-medium / general medium boxes that read
+ * `dataset` (src/simulation.cpp:423-439; Two_Medium_Box, src/geometry.cpp:
+ * 49-76), re-derives the media and resets the fields to time step 0 — one
+ * design iteration without re-parsing the config. */
+int ffip_set_density(ffip_sim *sim, const char *dataset, const double *rho, uint64_t n);
+
+/* Zeroes fields, auxiliary state and DFT sums; time_step = 0. */
+int ffip_reset(ffip_sim *sim);
+
+int ffip_get_stats(ffip_sim *sim, ffip_stats *stats);
+
+/* Blocks until all work of the handle has finished. */
+int ffip_sync(ffip_sim *sim);
+
+/* The handle's cudaStream_t, for callers that order their own work with it. */
+void *ffip_stream(ffip_sim *sim);
+
+int ffip_destroy(ffip_sim *sim);
+
+const char *ffip_last_error(void);
+
+/* _ffip.transpose (app/ffip.cpp:308-352): adjoint of trilinear interpolation
+ * with zero-padded extrapolation (include/utility.hpp:706-749).  Scatter-adds
+ * pt[i][3] at (pt[i][0], pt[i][1], pt[i][2]) onto the grid gx[nx] x gy[ny] x
+ * gz[nz] (uniform spacing from the first two entries); out[nz][ny][nx] is
+ * overwritten.  Host buffers; runs on the current CUDA device. */
+int ffip_transpose(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
+                   const double *pt, uint64_t npts, double *out);
+
+/* Adjoint_Volume.get_sensitivity (ffip/simulation.py:841-869) on the device:
+ * for each of n points, se = Re(2 pi j f * fwd * adj * deps / norm) with
+ * complex fwd, adj and deps (d epsilon / d rho) given as interleaved (re, im)
+ * pairs, then the transpose of trilinear interpolation of se onto the
+ * density grid, as ffip_transpose.
+ * Points are (x, y, z) triples.  out[nz][ny][nx] is overwritten. */
+int ffip_sensitivity(double freq, double norm_re, double norm_im, const double *fwd, const double *adj,
+                     const double *deps, const double *xyz, uint64_t n, const double *gx, uint64_t nx,
+                     const double *gy, uint64_t ny, const double *gz, uint64_t nz, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FFIP_GB300_H */

@@ -525,40 +525,70 @@ class OracleSim:
         objs = [self._build_geometry(g) for g in geoms]
         self.geom_objs = objs
         default = self._abstract(self.bg_medium)
-        # geom_map over all points of the local grid, x fastest
+        want_map = bool(self.cfg.get("geometry info request"))
         L = [self.grid_p2[d] - self.grid_p1[d] + 1 for d in range(3)]
-        self.geom_map = np.full(L[0] * L[1] * L[2], -1, np.int32)
+        # geom_map over all points of the local grid, x fastest (only kept
+        # when a geometry info request needs it)
+        self.geom_map = np.full(L[0] * L[1] * L[2], -1, np.int32) if want_map else None
         groups = {0: {}, 1: {}}
         for ct in E_CTYPES + H_CTYPES:
             side = 0 if is_e_point(ct) else 1
             p1, p2 = component_interior(self.grid_p1, self.grid_p2, ct)
-            X, Y, Z = yee_points(p1, p2)
-            n = X.size
+            lens = [cdiv(p2[d] - p1[d], 2) + 1 for d in range(3)]
+            if min(lens) <= 0:
+                continue
+            axes = [p1[d] + 2 * np.arange(lens[d], dtype=np.int64) for d in range(3)]
             npool = len(self.e_pool) if side == 0 else len(self.m_pool)
-            g_inf = np.full(n, default.epsilon if side == 0 else default.mu)
-            amps = np.tile(default.e_amp if side == 0 else default.m_amp, (n, 1)).reshape(n, npool)
-            owner = np.full(n, -1, np.int64)
+            owner = np.full((lens[2], lens[1], lens[0]), -1, np.int32)
+            owned_idx, owned_g, owned_amp = [], [], []
             for gi, obj in enumerate(objs):
-                free = owner < 0
-                inside = free & obj.inside(X, Y, Z)
-                if not inside.any():
+                blo, bhi = obj.bbox()
+                sl = []
+                for d in range(3):
+                    a = np.searchsorted(axes[d], math.floor(blo[d]) - 1, side="left")
+                    b = np.searchsorted(axes[d], math.ceil(bhi[d]) + 1, side="right")
+                    sl.append(slice(int(a), int(b)))
+                if any(x.start >= x.stop for x in sl):
                     continue
-                owner[inside] = gi
-                eps, mu, ea, ma = obj.medium(X[inside], Y[inside], Z[inside])
-                g_inf[inside] = eps if side == 0 else mu
-                a = ea if side == 0 else ma
-                amps[inside] = a
-            gm_idx = (X - self.grid_p1[0]) + (Y - self.grid_p1[1]) * L[0] + (Z - self.grid_p1[2]) * L[0] * L[1]
-            self.geom_map[gm_idx] = owner
+                sub = owner[sl[2], sl[1], sl[0]]
+                Z, Y, X = np.meshgrid(axes[2][sl[2]], axes[1][sl[1]], axes[0][sl[0]], indexing="ij")
+                new = (sub < 0) & obj.inside(X, Y, Z)
+                if not new.any():
+                    continue
+                sub[new] = gi
+                Xn, Yn, Zn = X[new], Y[new], Z[new]
+                eps, mu, ea, ma = obj.medium(Xn, Yn, Zn)
+                g = np.broadcast_to(np.asarray(eps if side == 0 else mu, dtype=np.float64), Xn.shape)
+                a = np.asarray(ea if side == 0 else ma, dtype=np.float64)
+                if npool == 0:
+                    a = np.zeros((Xn.size, 0))
+                else:
+                    a = np.broadcast_to(a.reshape((-1, npool)) if a.ndim > 1 else a.reshape((1, npool)), (Xn.size, npool))
+                owned_idx.append(self.index(Xn, Yn, Zn)); owned_g.append(np.array(g)); owned_amp.append(np.array(a))
+            if want_map:
+                Z, Y, X = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+                gm_idx = ((X - self.grid_p1[0]) + (Y - self.grid_p1[1]) * L[0]
+                          + (Z - self.grid_p1[2]) * L[0] * L[1]).ravel()
+                self.geom_map[gm_idx] = owner.ravel()
+            # default-medium points
+            Z, Y, X = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+            free = (owner < 0).ravel()
+            didx = self.index(X.ravel()[free], Y.ravel()[free], Z.ravel()[free])
+            dg = np.full(didx.size, default.epsilon if side == 0 else default.mu)
+            damp = np.broadcast_to((default.e_amp if side == 0 else default.m_amp).reshape(1, npool), (didx.size, npool))
+            del X, Y, Z
+            parts = [(didx, dg, damp)] + list(zip(owned_idx, owned_g, owned_amp))
             # group by non-zero pattern, tol 1e-4 (src/structure.cpp:256-264)
-            nz = np.abs(amps) > 1e-4
-            masks = (nz * (1 << np.arange(npool, dtype=np.int64))).sum(axis=1) if npool else np.zeros(n, np.int64)
-            idx = self.index(X, Y, Z)
-            for m in np.unique(masks):
-                sel = masks == m
-                bits = [i for i in range(npool) if (int(m) >> i) & 1]
-                grp = groups[side].setdefault(int(m), {"bits": bits, "idx": [], "g": [], "amp": []})
-                grp["idx"].append(idx[sel]); grp["g"].append(g_inf[sel]); grp["amp"].append(amps[sel][:, bits])
+            for idx, g_inf, amps in parts:
+                if idx.size == 0:
+                    continue
+                nz = np.abs(amps) > 1e-4
+                masks = (nz * (1 << np.arange(npool, dtype=np.int64))).sum(axis=1) if npool else np.zeros(idx.size, np.int64)
+                for m in np.unique(masks):
+                    sel = masks == m
+                    bits = [i for i in range(npool) if (int(m) >> i) & 1]
+                    grp = groups[side].setdefault(int(m), {"bits": bits, "idx": [], "g": [], "amp": []})
+                    grp["idx"].append(idx[sel]); grp["g"].append(g_inf[sel]); grp["amp"].append(amps[sel][:, bits])
         self.medium_groups = {0: [], 1: []}
         for side in (0, 1):
             pool = self.e_ab_pool if side == 0 else self.m_ab_pool
@@ -943,6 +973,9 @@ class _Box:
         return ((X > self.lo[0]) & (X < self.hi[0]) & (Y > self.lo[1]) & (Y < self.hi[1])
                 & (Z > self.lo[2]) & (Z < self.hi[2]))
 
+    def bbox(self):
+        return self.lo, self.hi
+
     def medium(self, X, Y, Z):
         return self.ab.epsilon, self.ab.mu, self.ab.e_amp, self.ab.m_amp
 
@@ -956,6 +989,10 @@ class _Sphere:
     def inside(self, X, Y, Z):
         dx = X - self.c[0]; dy = Y - self.c[1]; dz = Z - self.c[2]
         return dx * dx + dy * dy + dz * dz < self.r2
+
+    def bbox(self):
+        r = math.sqrt(self.r2)
+        return [v - r for v in self.c], [v + r for v in self.c]
 
     def medium(self, X, Y, Z):
         return self.ab.epsilon, self.ab.mu, self.ab.e_amp, self.ab.m_amp

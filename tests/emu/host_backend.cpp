@@ -1,0 +1,113 @@
+// TEST INFRASTRUCTURE — not part of the shipped library.
+//
+// Host emulation backend: runs the per-point update rules of
+// ffip_gb300/csrc/stencil.cuh (the same functions the CUDA kernels call) in
+// plain loops on the CPU, so that the engine's set-up, layout, sequencing and
+// output logic can be checked against the oracle without a GPU.  Built by
+// tests/emu/build_emu.py into tests/_build/libffip_emu.so, which exports the
+// same ffip_* C functions as the product library.  The fused pass is not
+// emulated (it is a CUDA-only tiling of the same rules).
+#include <cstdlib>
+#include <cstring>
+#include <stdexcept>
+
+#include "engine.hpp"
+
+namespace ffipg
+{
+namespace
+{
+class HostBackend : public Backend
+{
+public:
+    void *alloc(size_t bytes) override
+    {
+        void *p = std::calloc(bytes ? bytes : 1, 1);
+        if (!p) throw std::bad_alloc();
+        return p;
+    }
+    void release(void *p) override { std::free(p); }
+    void h2d(void *d, const void *s, size_t b) override
+    {
+        h2d_bytes += b;
+        std::memcpy(d, s, b);
+    }
+    void d2h(void *d, const void *s, size_t b) override
+    {
+        d2h_bytes += b;
+        std::memcpy(d, s, b);
+    }
+    void zero(void *p, size_t b) override { std::memset(p, 0, b); }
+    void sync() override {}
+
+    template <typename T>
+    void update_t(const SideParams<T> &p, bool is_e)
+    {
+        for (int k = 0; k < p.Mz; ++k)
+            for (int j = 0; j < p.My; ++j)
+                for (int i = 0; i < p.Mx; ++i)
+                    for (int c = 0; c < 3; ++c)
+                    {
+                        if (i < p.vlo[c][0] || i > p.vhi[c][0] || j < p.vlo[c][1] || j > p.vhi[c][1] || k < p.vlo[c][2] || k > p.vhi[c][2]) continue;
+                        if (is_e) update_point<T, true>(p, c, i, j, k);
+                        else update_point<T, false>(p, c, i, j, k);
+                    }
+    }
+    void update(const SideParams<double> &p, bool e) override { update_t(p, e); }
+    void update(const SideParams<float> &p, bool e) override { update_t(p, e); }
+
+    template <typename T>
+    void sources_t(const SourceParams<T> &p)
+    {
+        for (int q = 0; q < p.npts; ++q) source_point<T>(p, q);
+    }
+    void sources(const SourceParams<double> &p) override { sources_t(p); }
+    void sources(const SourceParams<float> &p) override { sources_t(p); }
+
+    template <typename T>
+    void ghosts_t(const GhostParams<T> &p)
+    {
+        for (int f = 0; f < p.nfaces; ++f)
+            for (int v = 0; v < p.faces[f].v1; ++v)
+                for (int u = 0; u < p.faces[f].u1; ++u) ghost_point<T>(p, f, u, v);
+    }
+    void ghosts(const GhostParams<double> &p) override { ghosts_t(p); }
+    void ghosts(const GhostParams<float> &p) override { ghosts_t(p); }
+
+    template <typename T>
+    void probe_t(const T *f, const int64_t *lin, const double *w, int n, double *out)
+    {
+        double r = 0;
+        for (int q = 0; q < n; ++q) r += (double)f[lin[q]] * w[q];
+        *out = r;
+    }
+    void probe(const double *f, const int64_t *l, const double *w, int n, double *o) override { probe_t(f, l, w, n, o); }
+    void probe(const float *f, const int64_t *l, const double *w, int n, double *o) override { probe_t(f, l, w, n, o); }
+    void dft_norm(const double *re, const double *im, int64_t n, double *out) override
+    {
+        double s = 0;
+        for (int64_t i = 0; i < n; ++i) s += re[i] * re[i] + im[i] * im[i];
+        *out = s;
+    }
+    const char *name() const override { return "host-emulation"; }
+    double timed(const std::function<void()> &f) override
+    {
+        f();
+        return 0.0;
+    }
+};
+} // namespace
+
+Backend *new_default_backend(int) { return new HostBackend(); }
+void *backend_stream(Backend *) { return nullptr; }
+int adjoint_transpose(const double *, uint64_t, const double *, uint64_t, const double *, uint64_t, const double *, uint64_t,
+                      double *)
+{
+    throw std::runtime_error("not emulated");
+}
+int adjoint_sensitivity(double, double, double, const double *, const double *, const double *, const double *, uint64_t,
+                        const double *, uint64_t, const double *, uint64_t, const double *, uint64_t, double *)
+{
+    throw std::runtime_error("not emulated");
+}
+} // namespace ffipg

@@ -5,7 +5,7 @@ import os
 import numpy as np
 
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-CASES = ["vacuum_pml", "dispersive", "density_boxes", "pmc_periodic_odd", "pec_periodic_magnetic",
+CASES = ["vacuum_pml", "dispersive", "debye_short", "density_boxes", "pmc_periodic_odd", "pec_periodic_magnetic",
          "decay_stop", "dft_stop"]
 
 

@@ -1,0 +1,74 @@
+"""GPU transpose of trilinear interpolation (_ffip.transpose) and the
+sensitivity correlation, against numpy restatements of the reference."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def interpn_transpose_ref(gx, gy, gz, pt):
+    """Sequential restatement of app/ffip.cpp:308-352 / include/utility.hpp:706-749."""
+    nx, ny, nz = len(gx), len(gy), len(gz)
+    dx = gx[1] - gx[0] if nx > 1 else 1.0
+    dy = gy[1] - gy[0] if ny > 1 else 1.0
+    dz = gz[1] - gz[0] if nz > 1 else 1.0
+    out = np.zeros((nz, ny, nx))
+
+    def axis(q, n):
+        if n == 1:
+            return [(0, 1.0)]
+        if q <= 0:
+            return [] if q <= -1 else [(0, 1 + q)]
+        if q >= n - 1:
+            return [] if q >= n else [(n - 1, n - q)]
+        i = int(q)
+        t = q - i
+        return [(i + 1, t), (i, 1 - t)]
+
+    for p in pt:
+        for iz, wz in axis((p[2] - gz[0]) / dz, nz):
+            for iy, wy in axis((p[1] - gy[0]) / dy, ny):
+                for ix, wx in axis((p[0] - gx[0]) / dx, nx):
+                    out[iz, iy, ix] += p[3] * wz * wy * wx
+    return out
+
+
+def test_transpose_matches_reference_restatement():
+    from ffip_gb300 import native
+    rng = np.random.default_rng(3)
+    gx = np.linspace(-2, 3, 11); gy = np.linspace(0, 1, 5); gz = np.array([0.5])
+    pt = np.stack([rng.uniform(-3, 4, 500), rng.uniform(-0.5, 1.5, 500), rng.uniform(0, 1, 500), rng.normal(size=500)], 1)
+    got = native.transpose(gx, gy, gz, pt)
+    ref = interpn_transpose_ref(gx, gy, gz, pt)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-13)
+
+
+def test_transpose_errors():
+    from ffip_gb300 import native
+    with pytest.raises(ValueError):
+        native.transpose([0, 1], [0, 1], [0, 1], np.zeros((3, 3)))
+    with pytest.raises(KeyError):
+        native.transpose([], [0, 1], [0, 1], np.zeros((3, 4)))
+
+
+def test_sensitivity_matches_numpy():
+    import ctypes
+    from ffip_gb300 import native
+    lib = native.load()
+    rng = np.random.default_rng(4)
+    n = 300
+    fwd = rng.normal(size=n) + 1j * rng.normal(size=n)
+    adj = rng.normal(size=n) + 1j * rng.normal(size=n)
+    deps = np.full(n, 11.0 + 0.0j)
+    xyz = np.stack([rng.uniform(0, 2, n), rng.uniform(0, 2, n), rng.uniform(0, 1, n)], 1)
+    f, norm = 0.1, 0.3 - 0.7j
+    gx = np.linspace(0, 2, 9); gy = np.linspace(0, 2, 9); gz = np.linspace(0, 1, 3)
+    se = np.real(2j * np.pi * f * fwd * adj * deps / norm)
+    ref = interpn_transpose_ref(gx, gy, gz, np.concatenate([xyz, se[:, None]], 1))
+    out = np.zeros((3, 9, 9))
+    D = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    keep = [np.ascontiguousarray(np.stack([a.real, a.imag], 1)) for a in (fwd, adj, deps)]
+    rc = lib.ffip_sensitivity(f, norm.real, norm.imag, D(keep[0]), D(keep[1]), D(keep[2]), D(xyz), n,
+                              D(gx), 9, D(gy), 9, D(gz), 3, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    assert rc == 0
+    np.testing.assert_allclose(out, ref, rtol=1e-10, atol=1e-12)

@@ -1,0 +1,157 @@
+"""GPU parity: the CUDA path, called through the C ABI (include/ffip_gb300.h),
+against the reference's golden outputs and against the oracle on seeded
+random configurations.
+
+Tolerances (relative to the largest |DFT| of the monitor group):
+  fp64 state:  1e-10  (the drop-in bar)
+  fp32 state:  1e-4   (fp32 fields, fp64 DFT sums)
+"""
+import copy
+
+import numpy as np
+import pytest
+
+from golden_cases import CASES, flatten, load
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-10
+FP32_TOL = 1e-4
+
+
+def rel_err(out, ref):
+    worst = 0.0
+    for k, r in ref.items():
+        assert k in out, k
+        assert out[k].shape == r.shape, (k, out[k].shape, r.shape)
+        if k.endswith("/real") or k.endswith("/imag"):
+            g = k.rsplit("/", 1)[0]
+            scale = max(np.abs(ref[g + "/real"]).max(), np.abs(ref[g + "/imag"]).max())
+            worst = max(worst, np.abs(out[k] - r).max() / scale)
+        else:
+            assert np.array_equal(out[k], r), k
+    return worst
+
+
+def gpu_run(cfg, ds=None, **over):
+    from ffip_gb300 import native
+    cfg = copy.deepcopy(cfg)
+    cfg.update(over)
+    return flatten(native.run_json(cfg, ds or {}))
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_matches_reference(name):
+    cfg, ds, ref = load(name)
+    assert rel_err(gpu_run(cfg, ds, precision="fp64"), ref) <= FP64_TOL
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp32_within_tolerance(name):
+    cfg, ds, ref = load(name)
+    assert rel_err(gpu_run(cfg, ds, precision="fp32"), ref) <= FP32_TOL
+
+
+@pytest.mark.parametrize("name", ["vacuum_pml", "dispersive", "density_boxes"])
+def test_unfused_and_auto_engines_agree(name):
+    cfg, ds, ref = load(name)
+    a = gpu_run(cfg, ds, engine="unfused")
+    b = gpu_run(cfg, ds, engine="auto")
+    assert rel_err(a, ref) <= FP64_TOL
+    assert rel_err(b, ref) <= FP64_TOL
+
+
+def test_repeat_runs_are_bitwise_identical():
+    cfg, ds, _ = load("dispersive")
+    a = gpu_run(cfg, ds)
+    b = gpu_run(cfg, ds)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def random_config(seed, n=20, steps=150):
+    """Seeded random media/sources/monitors in the reference's schema."""
+    rng = np.random.default_rng(seed)
+    med = lambda eps, esus=(): {"epsilon": eps, "mu": 1.0, "electric conductivity": 0.0, "magnetic conductivity": 0.0,
+                                "electric susceptibility": list(esus), "magnetic susceptibility": []}
+    geoms = []
+    for g in range(6):
+        kind = rng.integers(0, 3)
+        esus = []
+        if kind == 1:
+            esus = [{"type": "Lorentz", "frequency": float(rng.uniform(0.05, 0.2)), "gamma": float(rng.uniform(0.001, 0.02)),
+                     "amplitude": float(rng.uniform(0.5, 3))}]
+        elif kind == 2:
+            esus = [{"type": "Drude", "frequency": float(rng.uniform(0.05, 0.2)), "gamma": float(rng.uniform(0.005, 0.05)),
+                     "amplitude": 1.0}]
+        geoms.append({"type": "sphere", "center": [float(v) for v in rng.uniform(-5, 5, 3)], "radius": float(rng.uniform(1, 4)),
+                      "medium": med(float(rng.uniform(1, 4)), esus)})
+    comps = ["Ex", "Ey", "Ez", "Hx", "Hy", "Hz"]
+    return {
+        "courant number": 0.5, "resolution": 1.0, "size": [n, n, n], "input file": "x", "fields output file": "y",
+        "default material": med(1.0),
+        "PML": [{"thickness": 4.0, "k max": 1.0, "sigma max": 3.45, "order": 3}],
+        "geometry": geoms,
+        "sources": [{"type": "volume source", "center": [float(v) for v in rng.uniform(-3, 3, 3)], "size": [0, 0, 0],
+                     "amplitude": 1.0, "field component": comps[int(rng.integers(0, 6))],
+                     "function": {"type": "Gaussian1", "frequency": 0.1, "cutoff": 4.0, "start time": 0.0}}],
+        "fields output": [{"type": "volume fields dft", "center": [0, 0, 0], "size": [8, 8, 8], "frequency": [0.08, 0.1, 0.12],
+                           "field component": c, "output group": "volume fields dft %d" % i} for i, c in enumerate(comps)],
+        "stop condition": {"type": "time", "time": steps * 0.5},
+    }
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_fp64_matches_oracle_on_random_configs(seed):
+    from oracle import port
+    cfg = random_config(seed)
+    ref = flatten(port.run_json(cfg, {}, threads=4))
+    assert rel_err(gpu_run(cfg, precision="fp64"), ref) <= FP64_TOL
+
+
+def test_workload_downscaled_fp64_matches_oracle():
+    """The benchmark workload (dispersive spheres) at 64^3, 300 steps."""
+    from ffip_gb300 import workloads
+    from oracle import port
+    cfg = workloads.dispersive_spheres(64, steps=300, precision="fp64")
+    ref = flatten(port.run_json(cfg, {}, threads=8))
+    assert rel_err(gpu_run(cfg), ref) <= FP64_TOL
+    cfg32 = workloads.dispersive_spheres(64, steps=300, precision="fp32")
+    assert rel_err(gpu_run(cfg32), ref) <= FP32_TOL
+
+
+def test_empty_and_outside_monitors():
+    """A monitor outside the grid gives zeros of the closure shape, like the
+    reference's unwritten HDF5 hyperslab."""
+    cfg, ds, _ = load("vacuum_pml")
+    cfg = copy.deepcopy(cfg)
+    cfg["fields output"].append({"type": "volume fields dft", "center": [30, 30, 30], "size": [2, 2, 2], "frequency": [0.1],
+                                 "field component": "Ey", "output group": "outside"})
+    out = gpu_run(cfg, ds)
+    assert out["outside/real"].shape == (1, 3, 3, 3)
+    assert not out["outside/real"].any()
+
+
+def test_set_density_matches_fresh_create():
+    from ffip_gb300 import native
+    cfg, ds, _ = load("density_boxes")
+    rho2 = np.random.default_rng(9).uniform(0, 1, size=ds["two medium box 0"].shape)
+    ds2 = dict(ds)
+    ds2["two medium box 0"] = rho2
+    fresh = flatten(native.run_json(cfg, ds2))
+    with native.NativeSim(cfg, ds) as s:
+        s.run(cfg["stop condition"])
+        s.set_density("two medium box 0", rho2)
+        s.run(cfg["stop condition"])
+        again = flatten(s.outputs())
+    for k in fresh:
+        assert np.array_equal(fresh[k], again[k]), k
+
+
+def test_bad_device_index_is_an_error():
+    from ffip_gb300 import native
+    cfg, ds, _ = load("vacuum_pml")
+    cfg = copy.deepcopy(cfg)
+    cfg["device"] = 999
+    with pytest.raises(native.FfipError):
+        native.NativeSim(cfg, ds)
