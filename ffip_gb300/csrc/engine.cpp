@@ -229,7 +229,7 @@ void Engine<T>::init_media()
         D.group = upload(grp, true);
         if (D.poles)
         {
-            D.A = dalloc<T>(D.n, true);
+            if (c >= 3) D.A = dalloc<T>(D.n, true);  // H sources are applied before the H update
             std::vector<T> amp(L.amp.size());
             for (size_t q = 0; q < amp.size(); ++q) amp[q] = (T)L.amp[q];
             D.amp = upload(amp, true);
@@ -529,7 +529,7 @@ void Engine<T>::compute_bytes()
     // Algorithmic (compulsory) bytes of one full time step:
     //  every component point: field read + write;
     //  every (point, transverse axis) with a non-zero CPML c: psi read + write;
-    //  every slot with p poles: accdb read + write and P, P' read + write per pole;
+    //  every slot with p poles: P and P' read + write per pole;
     //  every monitored point: re + im read + write (fp64) per frequency.
     const double s = sizeof(T);
     double b = 0;
@@ -555,7 +555,7 @@ void Engine<T>::compute_bytes()
         for (size_t q = 0; q < L.group.size(); ++q)
         {
             int np = (int)P_.groups[side][L.group[q]].pool.size();
-            if (np) b += s * (2 + 4 * np);
+            if (np) b += s * 4 * np;
         }
     }
     for (auto &U : P_.units) b += 32.0 * (double)U.npoints() * (double)U.freqs.size();

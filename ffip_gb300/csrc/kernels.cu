@@ -8,8 +8,11 @@
 //   k_probe / k_dft_norm   per-step reductions for the stop conditions.
 //   k_fused    (fused.cuh) the H and E half steps of one time step in one
 //              z-marching pass over the grid.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <map>
 #include <stdexcept>
 #include <string>
 
@@ -84,6 +87,41 @@ __global__ void k_dft_norm(const double *re, const double *im, int64_t n, double
     if (threadIdx.x == 0) *out = s[0];
 }
 
+// cuTensorMapEncodeTiled from the driver, without linking libcuda
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn)
+    {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        check(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
+              "cudaGetDriverEntryPoint(cuTensorMapEncodeTiled)");
+        if (q != cudaDriverEntryPointSuccess || !p) throw std::runtime_error("cuTensorMapEncodeTiled not available");
+        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+// 3-D tiled map over one (Mx_pad, My, Mz) field array with a box of
+// (bx, by, 1) elements; out-of-range boxes fill zeros.
+template <typename T>
+CUtensorMap make_map(const T *base, int Mx, int My, int Mz, int bx, int by)
+{
+    CUtensorMap m;
+    cuuint64_t dims[3] = {(cuuint64_t)Mx, (cuuint64_t)My, (cuuint64_t)Mz};
+    cuuint64_t strides[2] = {(cuuint64_t)Mx * sizeof(T), (cuuint64_t)Mx * My * sizeof(T)};
+    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = encode_fn()(&m, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                             const_cast<T *>(base), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                             CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return m;
+}
+
+constexpr int kFusedChunk = 32;  // z planes per CTA
+
 class CudaBackend : public Backend
 {
 public:
@@ -101,6 +139,8 @@ public:
     ~CudaBackend() override
     {
         cudaSetDevice(dev_);
+        cudaStreamSynchronize(stream_);
+        if (err_) cudaFree(err_);
         cudaStreamDestroy(stream_);
     }
     // every entry re-selects the handle's device: calls may come from any thread
@@ -134,7 +174,12 @@ public:
         check(cudaStreamSynchronize(stream_), "d2h sync");
     }
     void zero(void *p, size_t bytes) override { use(); check(cudaMemsetAsync(p, 0, bytes, stream_), "cudaMemsetAsync"); }
-    void sync() override { use(); check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize"); }
+    void sync() override
+    {
+        use();
+        check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        check_err();
+    }
 
     template <typename T>
     void update_t(const SideParams<T> &p, bool is_e)
@@ -149,18 +194,61 @@ public:
     void update(const SideParams<double> &p, bool is_e) override { update_t(p, is_e); }
     void update(const SideParams<float> &p, bool is_e) override { update_t(p, is_e); }
 
-    bool has_fused() const override { return false; }
-    void fused(const FusedParams<double> &p) override
+    bool has_fused() const override { return true; }
+
+    template <typename T>
+    void fused_t(const FusedParams<T> &p)
     {
         use();
-        launch_fused(p, stream_);
+        using SH = FusedShape<T>;
+        using LY = FusedLayout<T>;
+        if (!err_)
+        {
+            check(cudaMalloc(&err_, sizeof(int)), "cudaMalloc");
+            check(cudaMemsetAsync(err_, 0, sizeof(int), stream_), "cudaMemsetAsync");
+        }
+        static bool attr_set = false;
+        if (!attr_set)
+        {
+            check(cudaFuncSetAttribute(k_fused<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM), "cudaFuncSetAttribute");
+            attr_set = true;
+        }
+        FusedLaunch<T> L;
+        for (int c = 0; c < 3; ++c)
+        {
+            L.tm_e[c] = map_for(p.ein[c], p.e.Mx, p.e.My, p.e.Mz, SH::BX, SH::TY + 2);
+            L.tm_h[c] = map_for(p.hin[c], p.e.Mx, p.e.My, p.e.Mz, SH::BX, SH::TY + 1);
+        }
+        L.fp = p;
+        L.kchunk = kFusedChunk;
+        L.err = err_;
+        dim3 block(SH::TX, SH::TY);
+        dim3 grid((p.e.Mx + SH::TX - 1) / SH::TX, (p.e.My + SH::TY - 1) / SH::TY, (p.e.Mz + kFusedChunk - 1) / kFusedChunk);
+        k_fused<T><<<grid, block, LY::SMEM, stream_>>>(L);
         check(cudaGetLastError(), "k_fused launch");
     }
-    void fused(const FusedParams<float> &p) override
+    void fused(const FusedParams<double> &p) override { fused_t(p); }
+    void fused(const FusedParams<float> &p) override { fused_t(p); }
+
+    template <typename T>
+    CUtensorMap map_for(const T *base, int Mx, int My, int Mz, int bx, int by)
     {
-        use();
-        launch_fused(p, stream_);
-        check(cudaGetLastError(), "k_fused launch");
+        auto key = std::make_pair((const void *)base, by);
+        auto it = maps_.find(key);
+        if (it != maps_.end()) return it->second;
+        CUtensorMap m = make_map(base, Mx, My, Mz, bx, by);
+        maps_[key] = m;
+        return m;
+    }
+
+    // raises if a bounded wait inside the fused kernel gave up
+    void check_err()
+    {
+        if (!err_) return;
+        int e = 0;
+        check(cudaMemcpyAsync(&e, err_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "cudaMemcpy err flag");
+        check(cudaStreamSynchronize(stream_), "sync");
+        if (e) throw std::runtime_error("fused kernel: a TMA wait timed out (results of this step are invalid)");
     }
 
     template <typename T>
@@ -225,6 +313,7 @@ public:
             check(cudaEventRecord(b, stream_), "cudaEventRecord");
             check(cudaEventSynchronize(b), "cudaEventSynchronize");
             check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
+            check_err();
         }
         catch (...)
         {
@@ -241,6 +330,8 @@ public:
 private:
     cudaStream_t stream_{nullptr};
     int dev_{0};
+    int *err_{nullptr};
+    std::map<std::pair<const void *, int>, CUtensorMap> maps_;
 };
 } // namespace
 

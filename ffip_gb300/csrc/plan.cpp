@@ -40,6 +40,15 @@ void Susceptibility::coefficients(double dt, double &c1, double &c2, double &c3)
     c3 = (2 * a0 * dt * dt) / c0;
 }
 
+void Susceptibility::increment_coefficients(double dt, double &d1, double &d2, double &c3) const
+{
+    // c1 + c2 - 1 = (4 b2 - 2 b0 dt^2 - 2 b2 + b1 dt - c0) / c0 = -2 b0 dt^2 / c0
+    double c0 = 2 * b2 + b1 * dt;
+    d1 = -2 * b0 * dt * dt / c0;
+    d2 = (2 * b2 - b1 * dt) / c0;
+    c3 = (2 * a0 * dt * dt) / c0;
+}
+
 int64_t Plan::yee_cells() const
 {
     int64_t n = 1;
@@ -809,7 +818,7 @@ void build_plan(const Json &cfg, const std::map<std::string, Dataset> &ds, Plan 
         for (auto &s : p.pool[side])
         {
             std::array<double, 3> c;
-            s.coefficients(p.dt, c[0], c[1], c[2]);
+            s.increment_coefficients(p.dt, c[0], c[1], c[2]);
             p.pool_coef[side].push_back(c);
         }
     }

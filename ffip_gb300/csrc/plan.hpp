@@ -49,6 +49,9 @@ struct Susceptibility  // (a0 + a1 jw) / (b0 + b1 jw - b2 w^2), include/medium.h
     bool operator==(const Susceptibility &o) const { return a0 == o.a0 && a1 == o.a1 && b0 == o.b0 && b1 == o.b1 && b2 == o.b2; }
     // Abstract_Susceptibility, src/medium.cpp:24-31
     void coefficients(double dt, double &c1, double &c2, double &c3) const;
+    // the same recurrence in increment form: d1 = c1 + c2 - 1, d2 = -c2
+    // (derived symbolically so that a Drude pole gets d1 = 0 exactly)
+    void increment_coefficients(double dt, double &d1, double &d2, double &c3) const;
 };
 
 struct Medium
@@ -159,7 +162,7 @@ struct Plan
     PoolMedium default_medium;
     double g_default[2]{1, 1};
     std::vector<Susceptibility> pool[2];
-    std::vector<std::array<double, 3>> pool_coef[2];  // c1,c2,c3 per pool entry
+    std::vector<std::array<double, 3>> pool_coef[2];  // d1,d2,c3 per pool entry (increment form)
     std::vector<PoleGroup> groups[2];
     std::map<std::vector<int>, int> group_index[2];
     std::vector<Geometry> geoms;

@@ -12,10 +12,11 @@
 //   H side uses negated strides (-curl E)            src/fields.cpp:174-177
 //   constitutive    P_n <- c1 P_n + c2 P'_n + amp c3 E_old;
 //                   E = (accdb*dt - sum P_n)/g_inf    src/structure.cpp:56-85
+//                   (carried in an equivalent increment form, material_point)
 //   DFT             re += cos(2 pi f t) v, im += -sin(2 pi f t) v
 //                                                    src/dft.cpp:29-62
-// For a point without poles E = accdb*dt/g_inf is carried as E directly:
-// E += (dt/g_inf) * (curl terms), so no accdb array exists for it.
+// E is carried directly, without the reference's accdb array: for a point
+// without poles E += (dt/g_inf) * (curl terms); with poles see material_point.
 #pragma once
 #include <math.h>
 #include <stdint.h>
@@ -44,9 +45,9 @@ struct SlotView
     const RowRange *rows;    // per (j,k) row
     const T *g, *coef, *inv; // g_inf, dt/g_inf, 1/g_inf per slot
     const uint8_t *group;    // pole group per slot
-    T *A;                    // running curl sum (accdb) per slot; used by slots with poles
+    T *A;                    // pending source sum per slot (H side, slots with poles; else null)
     const T *amp;            // [stride][n]
-    T *P, *P1;               // [stride][n] current and previous polarisation
+    T *P, *P1;               // [stride][n] polarisation P and its last increment J = P - P_prev
     int64_t n;
 };
 
@@ -76,7 +77,7 @@ struct SideParams
     SlotView<T> slot[3];
     const uint8_t *grp_np;     // poles per group
     const uint8_t *grp_pool;   // [group][kMaxPolesDev] pool indices
-    const T *pool_c;           // [pool][3] = c1, c2, c3
+    const T *pool_c;           // [pool][3] = d1, d2, c3 (see material_point)
     int comp_base;             // 0 for E, 3 for H
     int nunits;
     DftView units[kMaxUnitsPerSide];
@@ -106,7 +107,8 @@ FFIP_HD void dft_point(int nunits, const DftView *units, const double (*phase)[2
     }
 }
 
-// CPML-aware curl combination for one point (returns the increment of accdb)
+// CPML-aware curl combination for one point (returns the increment of accdb).
+// psi is read from psi_in and, when psi_out is not null, written to psi_out.
 template <typename T>
 FFIP_HD T curl_term(const SideParams<T> &p, int c, const int ii[3], int64_t idx, T curl1, T curl2, T *psi_in1,
                     T *psi_in2, T *psi_out1, T *psi_out2)
@@ -120,12 +122,12 @@ FFIP_HD T curl_term(const SideParams<T> &p, int c, const int ii[3], int64_t idx,
     if (cv1 != T(0))
     {
         ps1 = p.pb[a1][q1][ii[a1]] * psi_in1[idx] + cv1 * curl1;
-        psi_out1[idx] = ps1;
+        if (psi_out1) psi_out1[idx] = ps1;
     }
     if (cv2 != T(0))
     {
         ps2 = p.pb[a2][q2][ii[a2]] * psi_in2[idx] + cv2 * curl2;
-        psi_out2[idx] = ps2;
+        if (psi_out2) psi_out2[idx] = ps2;
     }
     return ps1 - ps2 + curl1 * p.pik[a1][q1][ii[a1]] - curl2 * p.pik[a2][q2][ii[a2]];
 }
@@ -160,22 +162,41 @@ FFIP_HD T material_point(const SideParams<T> &p, int c, int i, int j, int k, int
         }
         else
         {
-            const T A = S.A[slot] + term;
-            S.A[slot] = A;
-            T sum = T(0);
+            // The reference forms E = (accdb*dt - sum P)/g_inf from the running
+            // sum accdb.  Its difference between consecutive steps gives the
+            // same value without that sum:
+            //   E_new = E_old + (dt*(curl terms + sources) - sum (P_new - P_old)) / g_inf,
+            // which avoids cancelling two large numbers inside metals (it
+            // keeps fp32 state accurate) and needs no accdb array.  H-side
+            // sources arrive before this update and wait in S.A.
+            T pend = T(0);
+            if (S.A)
+            {
+                pend = S.A[slot];
+                if (pend != T(0)) S.A[slot] = T(0);
+            }
+            // Each pole keeps P and its last increment J = P - P_prev.  The
+            // reference's P_new = c1 P + c2 P_prev + amp c3 E_old is the same as
+            //   J_new = d1 P + d2 J + amp c3 E_old,  P_new = P + J_new
+            // with d1 = c1 + c2 - 1 and d2 = -c2 (pool_c holds d1, d2, c3),
+            // whose inputs are well scaled: for a Drude pole d1 is exactly 0,
+            // while c1 ~ 2 and c2 ~ -1 lose the small increment in fp32.
+            T dsum = T(0), psum = T(0);
             for (int q = 0; q < np; ++q)
             {
                 const int pool = p.grp_pool[g * kMaxPolesDev + q];
-                const T c1 = p.pool_c[3 * pool], c2 = p.pool_c[3 * pool + 1], c3 = p.pool_c[3 * pool + 2];
+                const T d1 = p.pool_c[3 * pool], d2 = p.pool_c[3 * pool + 1], c3 = p.pool_c[3 * pool + 2];
                 const int64_t s = q * S.n + slot;
-                const T Pq = S.P[s], P1q = S.P1[s];
-                const T Pn = c1 * Pq + c2 * P1q + S.amp[s] * c3 * old;
-                S.P1[s] = Pq;
+                const T Pq = S.P[s], Jq = S.P1[s];
+                const T Jn = d1 * Pq + d2 * Jq + S.amp[s] * c3 * old;
+                const T Pn = Pq + Jn;
+                S.P1[s] = Jn;
                 S.P[s] = Pn;
-                sum = sum + Pn;
+                dsum = dsum + Jn;
+                psum = psum + Pn;
             }
-            v = (A * p.dt - sum) * S.inv[slot];
-            *vd = A * p.dt;
+            v = old + ((term + pend) * p.dt - dsum) * S.inv[slot];
+            *vd = S.g[slot] * v + psum;  // D = g_inf E + sum P
         }
     }
     *out = v;
@@ -275,11 +296,14 @@ FFIP_HD void source_point(const SourceParams<T> &p, int q)
     T delta, deltad;
     if (slot >= 0 && p.grp_np[S.group[slot]] > 0)
     {
-        // a point with poles keeps the running sum: before its update (H
-        // sources) only the sum changes, the field it is about to read as
-        // "old" must not; after its update (E sources) the field follows.
-        S.A[slot] = S.A[slot] + sv;
-        if (!p.correct) return;
+        // a point with poles: before its update (H sources) the source waits
+        // in S.A, because the polarisation update must still see the old
+        // field; after its update (E sources) the field follows directly.
+        if (!p.correct)
+        {
+            S.A[slot] = S.A[slot] + sv;
+            return;
+        }
         delta = sv * p.dt * S.inv[slot];
         deltad = sv * p.dt;
     }

@@ -43,6 +43,7 @@ public:
     template <typename T>
     void update_t(const SideParams<T> &p, bool is_e)
     {
+#pragma omp parallel for collapse(2) schedule(static)
         for (int k = 0; k < p.Mz; ++k)
             for (int j = 0; j < p.My; ++j)
                 for (int i = 0; i < p.Mx; ++i)
