@@ -159,6 +159,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=8, help="steps timed for the CPU baseline sample")
     ap.add_argument("--skip-full-run", action="store_true", help="skip the full-length fp32/fp64 runs")
     ap.add_argument("--engine", default="auto")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--fp32-only", action="store_true", help="time only the fp32 stepper (profiling runs)")
     a = ap.parse_args()
     world, rank, local = dist_init()
     from ffip_gb300 import workloads
@@ -201,7 +203,7 @@ def main():
     # ---- device-resident throughput, fp32 and fp64
     res = {}
     clocks = None
-    for prec in ("fp32", "fp64"):
+    for prec in (("fp32",) if a.fp32_only else ("fp32", "fp64")):
         s = native.NativeSim(make(prec))
         s.step(warm)
         st0 = s.stats()
@@ -218,6 +220,8 @@ def main():
         res[prec] = {"ms": ms, "launches": st1["kernel_launches"] - st0["kernel_launches"],
                      "bytes_per_step": st1["bytes_per_step"], "fused": st1["fused"]}
         s.close()
+    if a.fp32_only:
+        res["fp64"] = res["fp32"]
     t32 = res["fp32"]["ms"] / a.steps
     t64 = res["fp64"]["ms"] / a.steps
     value = world * cells / (t32 * 1e-3) / 1e9
@@ -263,7 +267,7 @@ def main():
         out["dft_rel_err_fp32_vs_fp64"] = dft_rel_err(full["fp32"], full["fp64"])
 
     # ---- CPU baseline sample (rank 0 only)
-    if rank == 0 and world == 1:
+    if rank == 0 and world == 1 and not a.no_cpu:
         threads = os.cpu_count() or 1
         try:
             dt, setup = cpu_leg(workloads.dispersive_spheres(n, precision="fp64"), a.cpu_steps, 2, threads)
