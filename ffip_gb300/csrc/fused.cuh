@@ -1,29 +1,31 @@
 // Fused H+E time step: one z-marching pass over the grid per time step.
 //
-// Each CTA owns a TX x TY tile in (x, y) and marches a chunk of z planes.
+// Each CTA owns a TX x TY tile in (x, y) and marches a chunk of KCH z planes.
 // For plane k it needs E(k), E(k+1) and H(k) of the previous time level;
 // those planes are staged into shared memory by TMA (cp.async.bulk.tensor,
 // one 3-D tensor map per field array) through an S-stage ring completed by
-// mbarriers, so the loads of later planes are in flight while plane k is
+// mbarriers, so the loads of the next planes are in flight while plane k is
 // computed.  Per plane:
-//   1. H(k) at the new level is computed on the tile plus a one-point halo on
-//      the low x and y sides (the halo points belong to neighbouring CTAs and
-//      are recomputed here, not written) and kept in shared memory;
-//   2. E(k) at the new level is computed on the tile from H(k) and H(k-1)
-//      (the previous plane's result, still in shared memory).
+//   1. H(k) at the new level is computed on the tile, and on the low-x column
+//      and low-y row that the tile's E update needs (those halo points belong
+//      to neighbouring CTAs and are recomputed here, not written), into a
+//      two-plane ring in shared memory;
+//   2. E(k) at the new level is computed on the tile from H(k) and H(k-1).
 // Every field value is read from HBM once and written once per time step.
 // Because neighbouring CTAs read the previous level while this CTA writes the
 // new one, field buffers (and the H-side CPML psi) ping-pong between steps;
 // E-side CPML psi and polarisation state are only touched by their owner and
 // are updated in place.  Each chunk starts by recomputing H of the plane
-// below it (no writes).  Only used with "None" boundaries on every face and no
+// below it (no writes).  Used with "None" boundaries on every face and no
 // magnetic poles (the engine checks this).
 //
-// The per-point arithmetic is the same code the separate H/E kernels use
-// (stencil.cuh: curl_term, material_point, dft_point), so both passes give
-// identical results.  Every mbarrier wait is bounded; on timeout the kernel
-// records an error code, waits (bounded) for its outstanding copies and
-// returns.
+// The per-point arithmetic is the same as the separate H/E kernels
+// (stencil.cuh: pml_combine, material_at, dft_point), so both passes give the
+// same bits.  The CPML tables of the tile's x and y range and of the chunk's
+// z range are staged in shared memory; a tile plane with no CPML takes the
+// plain curl.  Only thread 0 waits on the mbarriers (bounded); on a timeout
+// it records an error word, waits (bounded) for its outstanding copies, and
+// the whole CTA returns.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -38,12 +40,12 @@ struct FusedShape;
 template <>
 struct FusedShape<float>
 {
-    static constexpr int TX = 32, TY = 8, XOFF = 4, BX = 40, S = 4;
+    static constexpr int TX = 32, TY = 8, XOFF = 4, BX = 40, S = 4, KCH = 32;
 };
 template <>
 struct FusedShape<double>
 {
-    static constexpr int TX = 32, TY = 8, XOFF = 2, BX = 36, S = 3;
+    static constexpr int TX = 32, TY = 8, XOFF = 2, BX = 36, S = 3, KCH = 32;
 };
 
 template <typename T>
@@ -58,7 +60,10 @@ struct FusedLayout
     static constexpr int TX_BYTES = 3 * E_BYTES + 3 * H_BYTES;  // bytes one stage receives
     static constexpr int HN_OFF = 128 + SH::S * STAGE;
     static constexpr int HN_PLANE = 3 * (SH::TY + 1) * (SH::TX + 1);  // elements of one H ring plane
-    static constexpr int SMEM = HN_OFF + 2 * HN_PLANE * (int)sizeof(T);
+    static constexpr int NX = SH::TX + 1, NY = SH::TY + 1, NZ = SH::KCH + 2;  // CPML table lengths
+    static constexpr int PML_OFF = HN_OFF + 2 * HN_PLANE * (int)sizeof(T);
+    static constexpr int PML_ELEMS = 6 * (NX + NY + NZ);  // [parity][b,c,ik][n] per axis
+    static constexpr int SMEM = PML_OFF + PML_ELEMS * (int)sizeof(T);
 };
 
 template <typename T>
@@ -67,8 +72,7 @@ struct FusedLaunch
     CUtensorMap tm_e[3];  // E input arrays, box (BX, TY + 2, 1)
     CUtensorMap tm_h[3];  // H input arrays, box (BX, TY + 1, 1)
     FusedParams<T> fp;
-    int kchunk;
-    int *err;             // set to a non-zero code when a wait times out
+    int *err;             // set to 1 when a wait times out
 };
 
 constexpr int kFusedWaitLimit = 1 << 22;
@@ -114,28 +118,164 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
         : "memory");
 }
 
+// Per-CTA context of the fused pass
+template <typename T>
+struct FusedCtx
+{
+    using SH = FusedShape<T>;
+    using LY = FusedLayout<T>;
+    unsigned char *smem;
+    const FusedLaunch<T> *L;
+    int x0, y0, k0;
+    __device__ __forceinline__ const T *e_tile(int st, int c) const
+    {
+        return reinterpret_cast<const T *>(smem + 128 + st * LY::STAGE + c * LY::E_TILE);
+    }
+    __device__ __forceinline__ const T *h_tile(int st, int c) const
+    {
+        return reinterpret_cast<const T *>(smem + 128 + st * LY::STAGE + 3 * LY::E_TILE + c * LY::H_TILE);
+    }
+    __device__ __forceinline__ T &hn_at(int ring, int c, int row, int col) const
+    {
+        return reinterpret_cast<T *>(smem + LY::HN_OFF)[ring * LY::HN_PLANE + (c * (SH::TY + 1) + row) * (SH::TX + 1) + col];
+    }
+    __device__ __forceinline__ T *pml(int axis) const
+    {
+        T *base = reinterpret_cast<T *>(smem + LY::PML_OFF);
+        return axis == 0 ? base : axis == 1 ? base + 6 * LY::NX : base + 6 * (LY::NX + LY::NY);
+    }
+    // table entry v (0 = b, 1 = c, 2 = 1/k) of axis A and parity q at
+    // position pos (an x, y or k index)
+    template <int A>
+    __device__ __forceinline__ T pml_val(int q, int v, int pos) const
+    {
+        constexpr int n = A == 0 ? LY::NX : A == 1 ? LY::NY : LY::NZ;
+        const int o = A == 0 ? pos - (x0 - 1) : A == 1 ? pos - (y0 - 1) : pos - (k0 - 1);
+        return pml(A)[(q * 3 + v) * n + o];
+    }
+};
+
+// accdb increment at one point of component GC from its two curls, CPML
+// coefficients taken from the staged tables
+template <typename T, int GC>
+__device__ __forceinline__ T fused_term(const FusedCtx<T> &X, bool pml_plane, int x, int y, int k, int64_t idx, T curl1,
+                                        T curl2, const T *pin1, const T *pin2, T *pout1, T *pout2)
+{
+    using C = CompT<GC>;
+    if (!pml_plane) return curl1 - curl2;
+    const int p1 = pick<C::a1>(x, y, k), p2 = pick<C::a2>(x, y, k);
+    const T cv1 = X.template pml_val<C::a1>(C::q1, 1, p1), cv2 = X.template pml_val<C::a2>(C::q2, 1, p2);
+    if (cv1 == T(0) && cv2 == T(0)) return curl1 - curl2;
+    return pml_combine(cv1, cv2, X.template pml_val<C::a1>(C::q1, 0, p1), X.template pml_val<C::a2>(C::q2, 0, p2),
+                       X.template pml_val<C::a1>(C::q1, 2, p1), X.template pml_val<C::a2>(C::q2, 2, p2), curl1, curl2, pin1,
+                       pin2, pout1, pout2, idx);
+}
+
+// H at the new level, component GC (3..5), point (x, y) of plane k; stA/stB
+// hold planes k/k+1.  Writes the output, psi and DFT only when `owned`.
+template <typename T, int GC>
+__device__ __forceinline__ T fused_h(const FusedCtx<T> &X, int x, int y, int k, int stA, int stB, bool owned, bool pml_plane)
+{
+    using SH = FusedShape<T>;
+    constexpr int BX = SH::BX, XOFF = SH::XOFF, c = GC - 3;
+    const FusedParams<T> &F = X.L->fp;
+    const SideParams<T> &PH = F.h;
+    if (x < PH.vlo[c][0] || x > PH.vhi[c][0] || y < PH.vlo[c][1] || y > PH.vhi[c][1] || k < PH.vlo[c][2] || k > PH.vhi[c][2])
+        return T(0);
+    const int r = y - (X.y0 - 1), col = x - (X.x0 - XOFF);
+    T curl1, curl2;
+    if (c == 0)  // Hx: -(dEz/dy) + dEy/dz
+    {
+        const T *Ez = X.e_tile(stA, 2), *Ey = X.e_tile(stA, 1);
+        curl1 = (Ez[r * BX + col] - Ez[(r + 1) * BX + col]) * PH.inv_dx;
+        curl2 = (Ey[r * BX + col] - X.e_tile(stB, 1)[r * BX + col]) * PH.inv_dx;
+    }
+    else if (c == 1)  // Hy: -(dEx/dz) + dEz/dx
+    {
+        const T *Ex = X.e_tile(stA, 0), *Ez = X.e_tile(stA, 2);
+        curl1 = (Ex[r * BX + col] - X.e_tile(stB, 0)[r * BX + col]) * PH.inv_dx;
+        curl2 = (Ez[r * BX + col] - Ez[r * BX + col + 1]) * PH.inv_dx;
+    }
+    else  // Hz: -(dEy/dx) + dEx/dy
+    {
+        const T *Ey = X.e_tile(stA, 1), *Ex = X.e_tile(stA, 0);
+        curl1 = (Ey[r * BX + col] - Ey[r * BX + col + 1]) * PH.inv_dx;
+        curl2 = (Ex[r * BX + col] - Ex[(r + 1) * BX + col]) * PH.inv_dx;
+    }
+    const int64_t idx = (int64_t)x + (int64_t)y * PH.sy + (int64_t)k * PH.sz;
+    const T term = fused_term<T, GC>(X, pml_plane, x, y, k, idx, curl1, curl2, F.psih_in[c][0], F.psih_in[c][1],
+                                     owned ? F.psih_out[c][0] : nullptr, owned ? F.psih_out[c][1] : nullptr);
+    const T old = X.h_tile(stA, c)[r * BX + col];
+    const int slot = slot_of(PH.slot[c], PH.My, x, y, k, idx);
+    T vd;
+    const T v = material_at(PH, PH.slot[c], slot, old, term, &vd);
+    if (owned)
+    {
+        F.hout[c][idx] = v;
+        if (PH.nunits) dft_point<T>(PH.nunits, PH.units, PH.phase, GC, x, y, k, (double)v, (double)vd);
+    }
+    return v;
+}
+
+// E at the new level, component GC (0..2), tile point (x, y) of plane k, from
+// the H ring (ring = plane k, ring ^ 1 = plane k-1); stA holds plane k
+template <typename T, int GC>
+__device__ __forceinline__ void fused_e(const FusedCtx<T> &X, int x, int y, int k, int stA, int ring, bool pml_plane)
+{
+    using SH = FusedShape<T>;
+    constexpr int BX = SH::BX, XOFF = SH::XOFF, c = GC;
+    const FusedParams<T> &F = X.L->fp;
+    const SideParams<T> &PE = F.e;
+    if (x < PE.vlo[c][0] || x > PE.vhi[c][0] || y < PE.vlo[c][1] || y > PE.vhi[c][1] || k < PE.vlo[c][2] || k > PE.vhi[c][2])
+        return;
+    const int row = y - (X.y0 - 1), col = x - (X.x0 - 1), prev = ring ^ 1;
+    T curl1, curl2;
+    if (c == 0)  // Ex: dHz/dy - dHy/dz
+    {
+        curl1 = (X.hn_at(ring, 2, row, col) - X.hn_at(ring, 2, row - 1, col)) * PE.inv_dx;
+        curl2 = (X.hn_at(ring, 1, row, col) - X.hn_at(prev, 1, row, col)) * PE.inv_dx;
+    }
+    else if (c == 1)  // Ey: dHx/dz - dHz/dx
+    {
+        curl1 = (X.hn_at(ring, 0, row, col) - X.hn_at(prev, 0, row, col)) * PE.inv_dx;
+        curl2 = (X.hn_at(ring, 2, row, col) - X.hn_at(ring, 2, row, col - 1)) * PE.inv_dx;
+    }
+    else  // Ez: dHy/dx - dHx/dy
+    {
+        curl1 = (X.hn_at(ring, 1, row, col) - X.hn_at(ring, 1, row, col - 1)) * PE.inv_dx;
+        curl2 = (X.hn_at(ring, 0, row, col) - X.hn_at(ring, 0, row - 1, col)) * PE.inv_dx;
+    }
+    const int64_t idx = (int64_t)x + (int64_t)y * PE.sy + (int64_t)k * PE.sz;
+    const T term = fused_term<T, GC>(X, pml_plane, x, y, k, idx, curl1, curl2, PE.psi[c][0], PE.psi[c][1], PE.psi[c][0],
+                                     PE.psi[c][1]);
+    const T old = X.e_tile(stA, c)[(y - (X.y0 - 1)) * BX + (x - (X.x0 - XOFF))];
+    const int slot = slot_of(PE.slot[c], PE.My, x, y, k, idx);
+    T vd;
+    const T v = material_at(PE, PE.slot[c], slot, old, term, &vd);
+    F.eout[c][idx] = v;
+    if (PE.nunits) dft_point<T>(PE.nunits, PE.units, PE.phase, GC, x, y, k, (double)v, (double)vd);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedLaunch<T> L)
 {
     using SH = FusedShape<T>;
     using LY = FusedLayout<T>;
-    constexpr int TX = SH::TX, TY = SH::TY, XOFF = SH::XOFF, BX = SH::BX, S = SH::S;
+    constexpr int TX = SH::TX, TY = SH::TY, XOFF = SH::XOFF, S = SH::S, KCH = SH::KCH;
     extern __shared__ __align__(128) unsigned char smem[];
     const FusedParams<T> &F = L.fp;
-    const SideParams<T> &PH = F.h;
     const SideParams<T> &PE = F.e;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-    const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
-    const int k0 = blockIdx.z * L.kchunk;
-    const int k1 = min(k0 + L.kchunk, PE.Mz);
-    const int NP = k1 - k0 + 2;  // planes k0-1 .. k1
+    FusedCtx<T> X;
+    X.smem = smem;
+    X.L = &L;
+    X.x0 = blockIdx.x * TX;
+    X.y0 = blockIdx.y * TY;
+    X.k0 = blockIdx.z * KCH;
+    const int k1 = min(X.k0 + KCH, PE.Mz);
+    const int NP = k1 - X.k0 + 2;  // planes k0-1 .. k1
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem);
-    T *hn = reinterpret_cast<T *>(smem + LY::HN_OFF);
-    auto e_tile = [&](int st, int c) { return reinterpret_cast<const T *>(smem + 128 + st * LY::STAGE + c * LY::E_TILE); };
-    auto h_tile = [&](int st, int c) {
-        return reinterpret_cast<const T *>(smem + 128 + st * LY::STAGE + 3 * LY::E_TILE + c * LY::H_TILE);
-    };
-    auto hn_at = [&](int ring, int c, int row, int col) -> T & { return hn[ring * LY::HN_PLANE + (c * (TY + 1) + row) * (TX + 1) + col]; };
+    volatile int *flag = reinterpret_cast<volatile int *>(smem + 64);
 
     if (tid == 0)
     {
@@ -143,64 +283,56 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedLaun
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-
     auto issue = [&](int p) {
-        const int st = p % S, z = k0 - 1 + p;
+        const int st = p % S, z = X.k0 - 1 + p;
         mbar_expect_tx(&bar[st], LY::TX_BYTES);
         unsigned char *base = smem + 128 + st * LY::STAGE;
-        for (int c = 0; c < 3; ++c) tma_load_3d(base + c * LY::E_TILE, &L.tm_e[c], x0 - XOFF, y0 - 1, z, &bar[st]);
-        for (int c = 0; c < 3; ++c) tma_load_3d(base + 3 * LY::E_TILE + c * LY::H_TILE, &L.tm_h[c], x0 - XOFF, y0 - 1, z, &bar[st]);
+        for (int c = 0; c < 3; ++c) tma_load_3d(base + c * LY::E_TILE, &L.tm_e[c], X.x0 - XOFF, X.y0 - 1, z, &bar[st]);
+        for (int c = 0; c < 3; ++c)
+            tma_load_3d(base + 3 * LY::E_TILE + c * LY::H_TILE, &L.tm_h[c], X.x0 - XOFF, X.y0 - 1, z, &bar[st]);
     };
     int issued = min(S, NP);
     if (tid == 0)
         for (int p = 0; p < issued; ++p) issue(p);
 
-    const int64_t sy = PE.sy, sz = PE.sz;
+    // stage the CPML tables of this tile / chunk while the first planes load
+    const bool pml_tables = PE.pc[0][0] != nullptr;
+    bool tile_pml = false;
+    if (pml_tables)
+    {
+        for (int a = 0; a < 3; ++a)
+        {
+            const int n = a == 0 ? LY::NX : a == 1 ? LY::NY : LY::NZ;
+            const int first = a == 0 ? X.x0 - 1 : a == 1 ? X.y0 - 1 : X.k0 - 1;
+            const int len = a == 0 ? PE.Mx : a == 1 ? PE.My : PE.Mz;
+            T *tab = X.pml(a);
+            for (int t = tid; t < 2 * n; t += TX * TY)
+            {
+                const int q = t / n, o = t % n, pos = first + o;
+                const bool in = pos >= 0 && pos < len;
+                const T cv = in ? PE.pc[a][q][pos] : T(0);
+                tab[(q * 3 + 0) * n + o] = in ? PE.pb[a][q][pos] : T(0);
+                tab[(q * 3 + 1) * n + o] = cv;
+                tab[(q * 3 + 2) * n + o] = in ? PE.pik[a][q][pos] : T(1);
+                if (a < 2 && cv != T(0)) tile_pml = true;
+            }
+        }
+    }
+    tile_pml = __syncthreads_or(tile_pml);
 
-    // H at the new level for point (x, y) of plane k, own H component c;
-    // stE0 / stE1: stages holding planes k / k+1.  Reads E and H of the old
-    // level from shared memory.
-    auto h_value = [&](int c, int x, int y, int k, int stE0, int stE1, bool owned, T &out_v) -> bool {
-        if (x < PH.vlo[c][0] || x > PH.vhi[c][0] || y < PH.vlo[c][1] || y > PH.vhi[c][1] || k < PH.vlo[c][2] || k > PH.vhi[c][2])
-            return false;
-        const int r = y - (y0 - 1), col = x - (x0 - XOFF);
-        const T *E0x = e_tile(stE0, 0), *E0y = e_tile(stE0, 1), *E0z = e_tile(stE0, 2);
-        T curl1, curl2;
-        if (c == 0)  // Hx: -(dEz/dy) + dEy/dz
-        {
-            curl1 = (E0z[r * BX + col] - E0z[(r + 1) * BX + col]) * PH.inv_dx;
-            curl2 = (E0y[r * BX + col] - e_tile(stE1, 1)[r * BX + col]) * PH.inv_dx;
-        }
-        else if (c == 1)  // Hy: -(dEx/dz) + dEz/dx
-        {
-            curl1 = (E0x[r * BX + col] - e_tile(stE1, 0)[r * BX + col]) * PH.inv_dx;
-            curl2 = (E0z[r * BX + col] - E0z[r * BX + col + 1]) * PH.inv_dx;
-        }
-        else  // Hz: -(dEy/dx) + dEx/dy
-        {
-            curl1 = (E0y[r * BX + col] - E0y[r * BX + col + 1]) * PH.inv_dx;
-            curl2 = (E0x[r * BX + col] - E0x[(r + 1) * BX + col]) * PH.inv_dx;
-        }
-        const int64_t idx = (int64_t)x + y * sy + (int64_t)k * sz;
-        const int ii[3] = {x, y, k};
-        const T term = curl_term(PH, c, ii, idx, curl1, curl2, const_cast<T *>(F.psih_in[c][0]), const_cast<T *>(F.psih_in[c][1]),
-                                 owned ? F.psih_out[c][0] : nullptr, owned ? F.psih_out[c][1] : nullptr);
-        const T old = h_tile(stE0, c)[r * BX + col];
-        T vd;
-        material_point(PH, c, x, y, k, idx, old, term, &out_v, &vd);
-        if (owned)
-        {
-            F.hout[c][idx] = out_v;
-            if (PH.nunits) dft_point<T>(PH.nunits, PH.units, PH.phase, 3 + c, x, y, k, (double)out_v, (double)vd);
-        }
-        return true;
-    };
-
+    const int x = X.x0 + tx, y = X.y0 + ty;
     for (int q = 0; q + 1 < NP; ++q)
     {
         const int stA = q % S, stB = (q + 1) % S;
-        bool ok = mbar_wait_bounded(&bar[stA], (q / S) & 1) && mbar_wait_bounded(&bar[stB], ((q + 1) / S) & 1);
-        if (__syncthreads_or(!ok))
+        if (tid == 0)
+        {
+            bool ok = true;
+            if (q == 0) ok = mbar_wait_bounded(&bar[stA], 0);
+            ok = ok && mbar_wait_bounded(&bar[stB], ((q + 1) / S) & 1);
+            *flag = ok ? 1 : 0;
+        }
+        __syncthreads();
+        if (!*flag)
         {
             if (tid == 0)
             {
@@ -209,76 +341,56 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedLaun
             }
             return;
         }
-        const int k = k0 - 1 + q;
+        // every thread is past plane q-1, so its stage can be refilled
+        if (tid == 0 && q >= 1 && q - 1 + S < NP)
+        {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(q - 1 + S);
+            issued = q + S;
+        }
+        const int k = X.k0 - 1 + q;
         const bool owned = q >= 1;
         const int ring = q & 1;
-        // 1. H(k) on the tile
+        bool pml_plane = false;
+        if (pml_tables)
+            pml_plane = tile_pml || X.template pml_val<2>(0, 1, k) != T(0) || X.template pml_val<2>(1, 1, k) != T(0);
+        // 1. H(k) on the tile ...
+        X.hn_at(ring, 0, ty + 1, tx + 1) = fused_h<T, 3>(X, x, y, k, stA, stB, owned, pml_plane);
+        X.hn_at(ring, 1, ty + 1, tx + 1) = fused_h<T, 4>(X, x, y, k, stA, stB, owned, pml_plane);
+        X.hn_at(ring, 2, ty + 1, tx + 1) = fused_h<T, 5>(X, x, y, k, stA, stB, owned, pml_plane);
+        // ... and the halo the E update reads: Hz and Hx on the low-y row, Hz
+        // and Hy on the low-x column (recomputed, not written)
+        if (tid < 2 * TX + 2 * TY)
         {
-            const int x = x0 + tx, y = y0 + ty;
-            for (int c = 0; c < 3; ++c)
+            if (tid < TX)
             {
-                T v = T(0);
-                if (!h_value(c, x, y, k, stA, stB, owned, v)) v = T(0);
-                hn_at(ring, c, ty + 1, tx + 1) = v;
+                const int hx = X.x0 + tid, hy = X.y0 - 1;
+                X.hn_at(ring, 2, 0, tid + 1) = hy >= 0 ? fused_h<T, 5>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
             }
-        }
-        // ... and on the low-x column and low-y row (recomputed, not written)
-        if (tid < TX + TY)
-        {
-            const int x = tid < TX ? x0 + tid : x0 - 1;
-            const int y = tid < TX ? y0 - 1 : y0 + (tid - TX);
-            const int row = y - (y0 - 1), col = x - (x0 - 1);
-            for (int c = 0; c < 3; ++c)
+            else if (tid < 2 * TX)
             {
-                T v = T(0);
-                if (x < 0 || y < 0 || !h_value(c, x, y, k, stA, stB, false, v)) v = T(0);
-                hn_at(ring, c, row, col) = v;
+                const int hx = X.x0 + tid - TX, hy = X.y0 - 1;
+                X.hn_at(ring, 0, 0, tid - TX + 1) = hy >= 0 ? fused_h<T, 3>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
+            }
+            else if (tid < 2 * TX + TY)
+            {
+                const int hx = X.x0 - 1, hy = X.y0 + tid - 2 * TX;
+                X.hn_at(ring, 2, tid - 2 * TX + 1, 0) = hx >= 0 ? fused_h<T, 5>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
+            }
+            else
+            {
+                const int hx = X.x0 - 1, hy = X.y0 + tid - 2 * TX - TY;
+                X.hn_at(ring, 1, tid - 2 * TX - TY + 1, 0) = hx >= 0 ? fused_h<T, 4>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
             }
         }
         __syncthreads();
         // 2. E(k) on the tile from H(k) and H(k-1)
         if (owned)
         {
-            const int x = x0 + tx, y = y0 + ty;
-            const int row = ty + 1, col = tx + 1, prev = ring ^ 1;
-            const int r = y - (y0 - 1), ecol = x - (x0 - XOFF);
-            for (int c = 0; c < 3; ++c)
-            {
-                if (x < PE.vlo[c][0] || x > PE.vhi[c][0] || y < PE.vlo[c][1] || y > PE.vhi[c][1] || k < PE.vlo[c][2] || k > PE.vhi[c][2])
-                    continue;
-                T curl1, curl2;
-                if (c == 0)  // Ex: dHz/dy - dHy/dz
-                {
-                    curl1 = (hn_at(ring, 2, row, col) - hn_at(ring, 2, row - 1, col)) * PE.inv_dx;
-                    curl2 = (hn_at(ring, 1, row, col) - hn_at(prev, 1, row, col)) * PE.inv_dx;
-                }
-                else if (c == 1)  // Ey: dHx/dz - dHz/dx
-                {
-                    curl1 = (hn_at(ring, 0, row, col) - hn_at(prev, 0, row, col)) * PE.inv_dx;
-                    curl2 = (hn_at(ring, 2, row, col) - hn_at(ring, 2, row, col - 1)) * PE.inv_dx;
-                }
-                else  // Ez: dHy/dx - dHx/dy
-                {
-                    curl1 = (hn_at(ring, 1, row, col) - hn_at(ring, 1, row, col - 1)) * PE.inv_dx;
-                    curl2 = (hn_at(ring, 0, row, col) - hn_at(ring, 0, row - 1, col)) * PE.inv_dx;
-                }
-                const int64_t idx = (int64_t)x + y * sy + (int64_t)k * sz;
-                const int ii[3] = {x, y, k};
-                const T term = curl_term(PE, c, ii, idx, curl1, curl2, PE.psi[c][0], PE.psi[c][1], PE.psi[c][0], PE.psi[c][1]);
-                const T old = e_tile(stA, c)[r * BX + ecol];
-                T vd;
-                const T v = material_point(PE, c, x, y, k, idx, old, term, &F.eout[c][idx], &vd);
-                if (PE.nunits) dft_point<T>(PE.nunits, PE.units, PE.phase, c, x, y, k, (double)v, (double)vd);
-            }
-        }
-        __syncthreads();
-        if (tid == 0 && q + S < NP)
-        {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(q + S);
-            issued = q + S + 1;
+            fused_e<T, 0>(X, x, y, k, stA, ring, pml_plane);
+            fused_e<T, 1>(X, x, y, k, stA, ring, pml_plane);
+            fused_e<T, 2>(X, x, y, k, stA, ring, pml_plane);
         }
     }
 }
-
 } // namespace ffipg

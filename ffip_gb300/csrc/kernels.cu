@@ -38,14 +38,15 @@ __global__ void __launch_bounds__(kUpdTX *kUpdTY) k_update(const __grid_constant
     if (i >= p.Mx || j >= p.My) return;
     const int k0 = blockIdx.z * kUpdKZ;
     const int k1 = min(k0 + kUpdKZ, p.Mz);
+    constexpr int B = IS_E ? 0 : 3;
+    const bool x0ok = i >= p.vlo[0][0] && i <= p.vhi[0][0] && j >= p.vlo[0][1] && j <= p.vhi[0][1];
+    const bool x1ok = i >= p.vlo[1][0] && i <= p.vhi[1][0] && j >= p.vlo[1][1] && j <= p.vhi[1][1];
+    const bool x2ok = i >= p.vlo[2][0] && i <= p.vhi[2][0] && j >= p.vlo[2][1] && j <= p.vhi[2][1];
     for (int k = k0; k < k1; ++k)
     {
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-        {
-            if (i < p.vlo[c][0] || i > p.vhi[c][0] || j < p.vlo[c][1] || j > p.vhi[c][1] || k < p.vlo[c][2] || k > p.vhi[c][2]) continue;
-            update_point<T, IS_E>(p, c, i, j, k);
-        }
+        if (x0ok && k >= p.vlo[0][2] && k <= p.vhi[0][2]) update_point<T, B + 0>(p, i, j, k);
+        if (x1ok && k >= p.vlo[1][2] && k <= p.vhi[1][2]) update_point<T, B + 1>(p, i, j, k);
+        if (x2ok && k >= p.vlo[2][2] && k <= p.vhi[2][2]) update_point<T, B + 2>(p, i, j, k);
     }
 }
 
@@ -119,8 +120,6 @@ CUtensorMap make_map(const T *base, int Mx, int My, int Mz, int bx, int by)
     if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
     return m;
 }
-
-constexpr int kFusedChunk = 32;  // z planes per CTA
 
 class CudaBackend : public Backend
 {
@@ -220,10 +219,9 @@ public:
             L.tm_h[c] = map_for(p.hin[c], p.e.Mx, p.e.My, p.e.Mz, SH::BX, SH::TY + 1);
         }
         L.fp = p;
-        L.kchunk = kFusedChunk;
         L.err = err_;
         dim3 block(SH::TX, SH::TY);
-        dim3 grid((p.e.Mx + SH::TX - 1) / SH::TX, (p.e.My + SH::TY - 1) / SH::TY, (p.e.Mz + kFusedChunk - 1) / kFusedChunk);
+        dim3 grid((p.e.Mx + SH::TX - 1) / SH::TX, (p.e.My + SH::TY - 1) / SH::TY, (p.e.Mz + SH::KCH - 1) / SH::KCH);
         k_fused<T><<<grid, block, LY::SMEM, stream_>>>(L);
         check(cudaGetLastError(), "k_fused launch");
     }

@@ -107,129 +107,161 @@ FFIP_HD void dft_point(int nunits, const DftView *units, const double (*phase)[2
     }
 }
 
-// CPML-aware curl combination for one point (returns the increment of accdb).
-// psi is read from psi_in and, when psi_out is not null, written to psi_out.
-template <typename T>
-FFIP_HD T curl_term(const SideParams<T> &p, int c, const int ii[3], int64_t idx, T curl1, T curl2, T *psi_in1,
-                    T *psi_in2, T *psi_out1, T *psi_out2)
+// Compile-time facts of global component GC (0..5 = Ex Ey Ez Hx Hy Hz): its
+// index within its side (= its direction), its two transverse axes (the curl
+// derivatives, in the reference's x1 = x3+1, x2 = x3+2 order,
+// include/fields.hpp:238-240) and its doubled-grid parities along them.
+template <int GC>
+struct CompT
 {
-    const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-    if (p.pc[a1][0] == nullptr) return curl1 - curl2;
-    const int q1 = p.par[c][a1], q2 = p.par[c][a2];
-    const T cv1 = p.pc[a1][q1][ii[a1]], cv2 = p.pc[a2][q2][ii[a2]];
-    if (cv1 == T(0) && cv2 == T(0)) return curl1 - curl2;
+    static constexpr int c = GC % 3;
+    static constexpr int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+    static constexpr int ct = GC == 0 ? 1 : GC == 1 ? 2 : GC == 2 ? 4 : GC == 3 ? 6 : GC == 4 ? 5 : 3;
+    static constexpr int q1 = (ct >> a1) & 1, q2 = (ct >> a2) & 1;
+};
+
+template <int A>
+FFIP_HD int pick(int i, int j, int k)
+{
+    return A == 0 ? i : (A == 1 ? j : k);
+}
+
+// CPML combination at a point where c1 or c2 is non-zero (PML_Stepping::step,
+// src/fields.cpp:98-107).  psi is read from pin and, when pout is not null,
+// written to pout.
+template <typename T>
+FFIP_HD T pml_combine(T cv1, T cv2, T b1, T b2, T ik1, T ik2, T curl1, T curl2, const T *pin1, const T *pin2, T *pout1,
+                      T *pout2, int64_t idx)
+{
     T ps1 = T(0), ps2 = T(0);
     if (cv1 != T(0))
     {
-        ps1 = p.pb[a1][q1][ii[a1]] * psi_in1[idx] + cv1 * curl1;
-        if (psi_out1) psi_out1[idx] = ps1;
+        ps1 = b1 * pin1[idx] + cv1 * curl1;
+        if (pout1) pout1[idx] = ps1;
     }
     if (cv2 != T(0))
     {
-        ps2 = p.pb[a2][q2][ii[a2]] * psi_in2[idx] + cv2 * curl2;
-        if (psi_out2) psi_out2[idx] = ps2;
+        ps2 = b2 * pin2[idx] + cv2 * curl2;
+        if (pout2) pout2[idx] = ps2;
     }
-    return ps1 - ps2 + curl1 * p.pik[a1][q1][ii[a1]] - curl2 * p.pik[a2][q2][ii[a2]];
+    return ps1 - ps2 + curl1 * ik1 - curl2 * ik2;
 }
 
-// Constitutive update of one point given its curl increment; `old` is the
-// point's field before this half step.  Writes the new field to *out and
-// returns it; *vd receives the D/B value for D/B monitors.
-template <typename T>
-FFIP_HD T material_point(const SideParams<T> &p, int c, int i, int j, int k, int64_t idx, T old, T term, T *out, T *vd)
+// curl increment of accdb at a point, CPML tables read from global memory
+template <typename T, int GC>
+FFIP_HD T curl_term_global(const SideParams<T> &p, int i, int j, int k, int64_t idx, T curl1, T curl2, const T *pin1,
+                           const T *pin2, T *pout1, T *pout2)
 {
-    const SlotView<T> &S = p.slot[c];
-    int slot = -1;
-    if (S.map)
-    {
-        RowRange r = S.rows[j + (int64_t)k * p.My];
-        if (i >= r.lo && i <= r.hi) slot = S.map[idx];
-    }
+    using C = CompT<GC>;
+    if (p.pc[0][0] == nullptr) return curl1 - curl2;
+    const int i1 = pick<C::a1>(i, j, k), i2 = pick<C::a2>(i, j, k);
+    const T cv1 = p.pc[C::a1][C::q1][i1], cv2 = p.pc[C::a2][C::q2][i2];
+    if (cv1 == T(0) && cv2 == T(0)) return curl1 - curl2;
+    return pml_combine(cv1, cv2, p.pb[C::a1][C::q1][i1], p.pb[C::a2][C::q2][i2], p.pik[C::a1][C::q1][i1],
+                       p.pik[C::a2][C::q2][i2], curl1, curl2, pin1, pin2, pout1, pout2, idx);
+}
+
+// slot index of a point (-1: default medium)
+template <typename T>
+FFIP_HD int slot_of(const SlotView<T> &S, int My, int i, int j, int k, int64_t idx)
+{
+    if (!S.map) return -1;
+    const RowRange r = S.rows[j + (int64_t)k * My];
+    return (i >= r.lo && i <= r.hi) ? S.map[idx] : -1;
+}
+
+// Constitutive update of one point given its accdb increment `term`; `old`
+// is the point's field before this half step.  Returns the new field; *vd
+// receives the D/B value for D/B monitors.
+template <typename T>
+FFIP_HD T material_at(const SideParams<T> &p, const SlotView<T> &S, int slot, T old, T term, T *vd)
+{
     T v;
     if (slot < 0)
     {
         v = old + p.coef_def * term;
         *vd = p.g_def * v;
+        return v;
     }
-    else
+    const int g = S.group[slot];
+    const int np = p.grp_np[g];
+    if (np == 0)
     {
-        const int g = S.group[slot];
-        const int np = p.grp_np[g];
-        if (np == 0)
-        {
-            v = old + S.coef[slot] * term;
-            *vd = S.g[slot] * v;
-        }
-        else
-        {
-            // The reference forms E = (accdb*dt - sum P)/g_inf from the running
-            // sum accdb.  Its difference between consecutive steps gives the
-            // same value without that sum:
-            //   E_new = E_old + (dt*(curl terms + sources) - sum (P_new - P_old)) / g_inf,
-            // which avoids cancelling two large numbers inside metals (it
-            // keeps fp32 state accurate) and needs no accdb array.  H-side
-            // sources arrive before this update and wait in S.A.
-            T pend = T(0);
-            if (S.A)
-            {
-                pend = S.A[slot];
-                if (pend != T(0)) S.A[slot] = T(0);
-            }
-            // Each pole keeps P and its last increment J = P - P_prev.  The
-            // reference's P_new = c1 P + c2 P_prev + amp c3 E_old is the same as
-            //   J_new = d1 P + d2 J + amp c3 E_old,  P_new = P + J_new
-            // with d1 = c1 + c2 - 1 and d2 = -c2 (pool_c holds d1, d2, c3),
-            // whose inputs are well scaled: for a Drude pole d1 is exactly 0,
-            // while c1 ~ 2 and c2 ~ -1 lose the small increment in fp32.
-            T dsum = T(0), psum = T(0);
-            for (int q = 0; q < np; ++q)
-            {
-                const int pool = p.grp_pool[g * kMaxPolesDev + q];
-                const T d1 = p.pool_c[3 * pool], d2 = p.pool_c[3 * pool + 1], c3 = p.pool_c[3 * pool + 2];
-                const int64_t s = q * S.n + slot;
-                const T Pq = S.P[s], Jq = S.P1[s];
-                const T Jn = d1 * Pq + d2 * Jq + S.amp[s] * c3 * old;
-                const T Pn = Pq + Jn;
-                S.P1[s] = Jn;
-                S.P[s] = Pn;
-                dsum = dsum + Jn;
-                psum = psum + Pn;
-            }
-            v = old + ((term + pend) * p.dt - dsum) * S.inv[slot];
-            *vd = S.g[slot] * v + psum;  // D = g_inf E + sum P
-        }
+        v = old + S.coef[slot] * term;
+        *vd = S.g[slot] * v;
+        return v;
     }
-    *out = v;
+    // The reference forms E = (accdb*dt - sum P)/g_inf from the running sum
+    // accdb.  Its difference between consecutive steps gives the same value
+    // without that sum:
+    //   E_new = E_old + (dt*(curl terms + sources) - sum (P_new - P_old)) / g_inf,
+    // which avoids cancelling two large numbers inside metals (it keeps fp32
+    // state accurate) and needs no accdb array.  H-side sources arrive before
+    // this update and wait in S.A.
+    T pend = T(0);
+    if (S.A)
+    {
+        pend = S.A[slot];
+        if (pend != T(0)) S.A[slot] = T(0);
+    }
+    // Each pole keeps P and its last increment J = P - P_prev.  The
+    // reference's P_new = c1 P + c2 P_prev + amp c3 E_old is the same as
+    //   J_new = d1 P + d2 J + amp c3 E_old,  P_new = P + J_new
+    // with d1 = c1 + c2 - 1 and d2 = -c2 (pool_c holds d1, d2, c3), whose
+    // inputs are well scaled: for a Drude pole d1 is exactly 0, while c1 ~ 2
+    // and c2 ~ -1 lose the small increment in fp32.
+    T dsum = T(0), psum = T(0);
+    for (int q = 0; q < np; ++q)
+    {
+        const int pool = p.grp_pool[g * kMaxPolesDev + q];
+        const T d1 = p.pool_c[3 * pool], d2 = p.pool_c[3 * pool + 1], c3 = p.pool_c[3 * pool + 2];
+        const int64_t s = q * S.n + slot;
+        const T Pq = S.P[s], Jq = S.P1[s];
+        const T Jn = d1 * Pq + d2 * Jq + S.amp[s] * c3 * old;
+        const T Pn = Pq + Jn;
+        S.P1[s] = Jn;
+        S.P[s] = Pn;
+        dsum = dsum + Jn;
+        psum = psum + Pn;
+    }
+    v = old + ((term + pend) * p.dt - dsum) * S.inv[slot];
+    *vd = S.g[slot] * v + psum;  // D = g_inf E + sum P
     return v;
 }
 
-// Full update of one point of own component c on side E (IS_E) or H, in
-// place, reading the other side's fields from p.o.
-template <typename T, bool IS_E>
-FFIP_HD void update_point(const SideParams<T> &p, int c, int i, int j, int k)
+// Full update of one point of global component GC (E side: GC < 3), in place,
+// reading the other side's fields from p.o.  E reads its odd neighbours at
+// index i-1 and i, H (the reference's negated strides, src/fields.cpp:174-177)
+// its even neighbours at i and i+1.
+template <typename T, int GC>
+FFIP_HD void update_point(const SideParams<T> &p, int i, int j, int k)
 {
+    using C = CompT<GC>;
+    constexpr bool IS_E = GC < 3;
     const int64_t idx = (int64_t)i + (int64_t)j * p.sy + (int64_t)k * p.sz;
-    const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-    const int64_t st[3] = {1, p.sy, p.sz};
-    const T *O1 = p.o[a2];  // derivative along a1 of the other-side component pointing along a2
-    const T *O2 = p.o[a1];
+    const int64_t s1 = C::a1 == 0 ? 1 : (C::a1 == 1 ? p.sy : p.sz);
+    const int64_t s2 = C::a2 == 0 ? 1 : (C::a2 == 1 ? p.sy : p.sz);
+    const T *O1 = p.o[C::a2];  // derivative along a1 of the other-side component pointing along a2
+    const T *O2 = p.o[C::a1];
     T curl1, curl2;
     if (IS_E)
     {
-        curl1 = (O1[idx] - O1[idx - st[a1]]) * p.inv_dx;
-        curl2 = (O2[idx] - O2[idx - st[a2]]) * p.inv_dx;
+        curl1 = (O1[idx] - O1[idx - s1]) * p.inv_dx;
+        curl2 = (O2[idx] - O2[idx - s2]) * p.inv_dx;
     }
     else
     {
-        curl1 = (O1[idx] - O1[idx + st[a1]]) * p.inv_dx;
-        curl2 = (O2[idx] - O2[idx + st[a2]]) * p.inv_dx;
+        curl1 = (O1[idx] - O1[idx + s1]) * p.inv_dx;
+        curl2 = (O2[idx] - O2[idx + s2]) * p.inv_dx;
     }
-    const int ii[3] = {i, j, k};
-    T term = curl_term(p, c, ii, idx, curl1, curl2, p.psi[c][0], p.psi[c][1], p.psi[c][0], p.psi[c][1]);
+    constexpr int c = C::c;
+    const T term = curl_term_global<T, GC>(p, i, j, k, idx, curl1, curl2, p.psi[c][0], p.psi[c][1], p.psi[c][0], p.psi[c][1]);
+    const int slot = slot_of(p.slot[c], p.My, i, j, k, idx);
     T vd;
     T *F = p.f[c];
-    T v = material_point(p, c, i, j, k, idx, F[idx], term, &F[idx], &vd);
-    if (p.nunits) dft_point<T>(p.nunits, p.units, p.phase, p.comp_base + c, i, j, k, (double)v, (double)vd);
+    const T v = material_at(p, p.slot[c], slot, F[idx], term, &vd);
+    F[idx] = v;
+    if (p.nunits) dft_point<T>(p.nunits, p.units, p.phase, GC, i, j, k, (double)v, (double)vd);
 }
 
 // ---------------------------------------------------------------------------

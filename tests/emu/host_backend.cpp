@@ -50,8 +50,18 @@ public:
                     for (int c = 0; c < 3; ++c)
                     {
                         if (i < p.vlo[c][0] || i > p.vhi[c][0] || j < p.vlo[c][1] || j > p.vhi[c][1] || k < p.vlo[c][2] || k > p.vhi[c][2]) continue;
-                        if (is_e) update_point<T, true>(p, c, i, j, k);
-                        else update_point<T, false>(p, c, i, j, k);
+                        if (is_e)
+                        {
+                            if (c == 0) update_point<T, 0>(p, i, j, k);
+                            else if (c == 1) update_point<T, 1>(p, i, j, k);
+                            else update_point<T, 2>(p, i, j, k);
+                        }
+                        else
+                        {
+                            if (c == 0) update_point<T, 3>(p, i, j, k);
+                            else if (c == 1) update_point<T, 4>(p, i, j, k);
+                            else update_point<T, 5>(p, i, j, k);
+                        }
                     }
     }
     void update(const SideParams<double> &p, bool e) override { update_t(p, e); }
