@@ -40,12 +40,12 @@ struct FusedShape;
 template <>
 struct FusedShape<float>
 {
-    static constexpr int TX = 32, TY = 8, XOFF = 4, BX = 40, S = 4, KCH = 32;
+    static constexpr int TX = 32, TY = 8, XOFF = 4, BX = 40, S = 4, KCH = 32, MINB = 4;  // CTAs per SM (smem-bound)
 };
 template <>
 struct FusedShape<double>
 {
-    static constexpr int TX = 32, TY = 8, XOFF = 2, BX = 36, S = 3, KCH = 32;
+    static constexpr int TX = 32, TY = 8, XOFF = 2, BX = 36, S = 3, KCH = 32, MINB = 3;
 };
 
 template <typename T>
@@ -173,14 +173,16 @@ __device__ __forceinline__ T fused_term(const FusedCtx<T> &X, bool pml_plane, in
 
 // H at the new level, component GC (3..5), point (x, y) of plane k; stA/stB
 // hold planes k/k+1.  Writes the output, psi and DFT only when `owned`.
-template <typename T, int GC>
-__device__ __forceinline__ T fused_h(const FusedCtx<T> &X, int x, int y, int k, int stA, int stB, bool owned, bool pml_plane)
+template <typename T, int GC, bool CHECK>
+__device__ __forceinline__ T fused_h(const FusedCtx<T> &X, int x, int y, int k, int stA, int stB, bool owned, bool pml_plane,
+                                     bool slots, bool dft)
 {
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX, XOFF = SH::XOFF, c = GC - 3;
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PH = F.h;
-    if (x < PH.vlo[c][0] || x > PH.vhi[c][0] || y < PH.vlo[c][1] || y > PH.vhi[c][1] || k < PH.vlo[c][2] || k > PH.vhi[c][2])
+    if (CHECK && (x < PH.vlo[c][0] || x > PH.vhi[c][0] || y < PH.vlo[c][1] || y > PH.vhi[c][1] || k < PH.vlo[c][2] ||
+                  k > PH.vhi[c][2]))
         return T(0);
     const int r = y - (X.y0 - 1), col = x - (X.x0 - XOFF);
     T curl1, curl2;
@@ -202,31 +204,38 @@ __device__ __forceinline__ T fused_h(const FusedCtx<T> &X, int x, int y, int k, 
         curl1 = (Ey[r * BX + col] - Ey[r * BX + col + 1]) * PH.inv_dx;
         curl2 = (Ex[r * BX + col] - Ex[(r + 1) * BX + col]) * PH.inv_dx;
     }
-    const int64_t idx = (int64_t)x + (int64_t)y * PH.sy + (int64_t)k * PH.sz;
+    const int idx = x + y * (int)PH.sy + k * (int)PH.sz;
     const T term = fused_term<T, GC>(X, pml_plane, x, y, k, idx, curl1, curl2, F.psih_in[c][0], F.psih_in[c][1],
                                      owned ? F.psih_out[c][0] : nullptr, owned ? F.psih_out[c][1] : nullptr);
     const T old = X.h_tile(stA, c)[r * BX + col];
-    const int slot = slot_of(PH.slot[c], PH.My, x, y, k, idx);
-    T vd;
-    const T v = material_at(PH, PH.slot[c], slot, old, term, &vd);
+    T v, vd;
+    if (!slots)
+    {
+        v = old + PH.coef_def * term;
+        vd = PH.g_def * v;
+    }
+    else
+        v = material_at(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
     if (owned)
     {
         F.hout[c][idx] = v;
-        if (PH.nunits) dft_point<T>(PH.nunits, PH.units, PH.phase, GC, x, y, k, (double)v, (double)vd);
+        if (dft) dft_point<T>(PH.nunits, PH.units, PH.phase, GC, x, y, k, (double)v, (double)vd);
     }
     return v;
 }
 
 // E at the new level, component GC (0..2), tile point (x, y) of plane k, from
 // the H ring (ring = plane k, ring ^ 1 = plane k-1); stA holds plane k
-template <typename T, int GC>
-__device__ __forceinline__ void fused_e(const FusedCtx<T> &X, int x, int y, int k, int stA, int ring, bool pml_plane)
+template <typename T, int GC, bool CHECK>
+__device__ __forceinline__ void fused_e(const FusedCtx<T> &X, int x, int y, int k, int stA, int ring, bool pml_plane,
+                                        bool slots, bool dft)
 {
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX, XOFF = SH::XOFF, c = GC;
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PE = F.e;
-    if (x < PE.vlo[c][0] || x > PE.vhi[c][0] || y < PE.vlo[c][1] || y > PE.vhi[c][1] || k < PE.vlo[c][2] || k > PE.vhi[c][2])
+    if (CHECK && (x < PE.vlo[c][0] || x > PE.vhi[c][0] || y < PE.vlo[c][1] || y > PE.vhi[c][1] || k < PE.vlo[c][2] ||
+                  k > PE.vhi[c][2]))
         return;
     const int row = y - (X.y0 - 1), col = x - (X.x0 - 1), prev = ring ^ 1;
     T curl1, curl2;
@@ -245,19 +254,24 @@ __device__ __forceinline__ void fused_e(const FusedCtx<T> &X, int x, int y, int 
         curl1 = (X.hn_at(ring, 1, row, col) - X.hn_at(ring, 1, row, col - 1)) * PE.inv_dx;
         curl2 = (X.hn_at(ring, 0, row, col) - X.hn_at(ring, 0, row - 1, col)) * PE.inv_dx;
     }
-    const int64_t idx = (int64_t)x + (int64_t)y * PE.sy + (int64_t)k * PE.sz;
+    const int idx = x + y * (int)PE.sy + k * (int)PE.sz;
     const T term = fused_term<T, GC>(X, pml_plane, x, y, k, idx, curl1, curl2, PE.psi[c][0], PE.psi[c][1], PE.psi[c][0],
                                      PE.psi[c][1]);
     const T old = X.e_tile(stA, c)[(y - (X.y0 - 1)) * BX + (x - (X.x0 - XOFF))];
-    const int slot = slot_of(PE.slot[c], PE.My, x, y, k, idx);
-    T vd;
-    const T v = material_at(PE, PE.slot[c], slot, old, term, &vd);
+    T v, vd;
+    if (!slots)
+    {
+        v = old + PE.coef_def * term;
+        vd = PE.g_def * v;
+    }
+    else
+        v = material_at(PE, PE.slot[c], slot_of(PE.slot[c], PE.My, x, y, k, idx), old, term, &vd);
     F.eout[c][idx] = v;
-    if (PE.nunits) dft_point<T>(PE.nunits, PE.units, PE.phase, GC, x, y, k, (double)v, (double)vd);
+    if (dft) dft_point<T>(PE.nunits, PE.units, PE.phase, GC, x, y, k, (double)v, (double)vd);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedLaunch<T> L)
+__global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid_constant__ FusedLaunch<T> L)
 {
     using SH = FusedShape<T>;
     using LY = FusedLayout<T>;
@@ -319,6 +333,22 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedLaun
         }
     }
     tile_pml = __syncthreads_or(tile_pml);
+    // the tile and its low-side halo lie inside every component's valid x/y
+    // range; kin_lo..kin_hi: planes where every component is valid
+    bool tile_inside = true;
+    int kin_lo = 0, kin_hi = PE.Mz;
+    for (int sd = 0; sd < 2; ++sd)
+    {
+        const SideParams<T> &P = sd == 0 ? PE : F.h;
+        for (int c = 0; c < 3; ++c)
+        {
+            tile_inside = tile_inside && P.vlo[c][0] <= X.x0 - 1 && X.x0 + TX - 1 <= P.vhi[c][0] && P.vlo[c][1] <= X.y0 - 1 &&
+                          X.y0 + TY - 1 <= P.vhi[c][1];
+            kin_lo = max(kin_lo, P.vlo[c][2]);
+            kin_hi = min(kin_hi, P.vhi[c][2]);
+        }
+    }
+    const bool h_slots = F.h.slot[0].map || F.h.slot[1].map || F.h.slot[2].map;
 
     const int x = X.x0 + tx, y = X.y0 + ty;
     for (int q = 0; q + 1 < NP; ++q)
@@ -354,10 +384,36 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedLaun
         bool pml_plane = false;
         if (pml_tables)
             pml_plane = tile_pml || X.template pml_val<2>(0, 1, k) != T(0) || X.template pml_val<2>(1, 1, k) != T(0);
+        // CTA-uniform: every point of the tile (and its halo) valid in every
+        // component at this plane?
+        const bool inside = tile_inside && k >= kin_lo && k <= kin_hi;
+        // DFT units touching this tile plane (E and H sides)
+        bool dft_e = false, dft_h = false;
+        for (int u = 0; u < PE.nunits; ++u)
+        {
+            const DftView &U = PE.units[u];
+            dft_e = dft_e || (k >= U.i0[2] && k < U.i0[2] + U.ld[2] && U.i0[1] < X.y0 + TY && U.i0[1] + U.ld[1] > X.y0 &&
+                              U.i0[0] < X.x0 + TX && U.i0[0] + U.ld[0] > X.x0);
+        }
+        for (int u = 0; u < F.h.nunits; ++u)
+        {
+            const DftView &U = F.h.units[u];
+            dft_h = dft_h || (k >= U.i0[2] && k < U.i0[2] + U.ld[2] && U.i0[1] < X.y0 + TY && U.i0[1] + U.ld[1] > X.y0 &&
+                              U.i0[0] < X.x0 + TX && U.i0[0] + U.ld[0] > X.x0);
+        }
         // 1. H(k) on the tile ...
-        X.hn_at(ring, 0, ty + 1, tx + 1) = fused_h<T, 3>(X, x, y, k, stA, stB, owned, pml_plane);
-        X.hn_at(ring, 1, ty + 1, tx + 1) = fused_h<T, 4>(X, x, y, k, stA, stB, owned, pml_plane);
-        X.hn_at(ring, 2, ty + 1, tx + 1) = fused_h<T, 5>(X, x, y, k, stA, stB, owned, pml_plane);
+        if (inside)
+        {
+            X.hn_at(ring, 0, ty + 1, tx + 1) = fused_h<T, 3, false>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
+            X.hn_at(ring, 1, ty + 1, tx + 1) = fused_h<T, 4, false>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
+            X.hn_at(ring, 2, ty + 1, tx + 1) = fused_h<T, 5, false>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
+        }
+        else
+        {
+            X.hn_at(ring, 0, ty + 1, tx + 1) = fused_h<T, 3, true>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
+            X.hn_at(ring, 1, ty + 1, tx + 1) = fused_h<T, 4, true>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
+            X.hn_at(ring, 2, ty + 1, tx + 1) = fused_h<T, 5, true>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
+        }
         // ... and the halo the E update reads: Hz and Hx on the low-y row, Hz
         // and Hy on the low-x column (recomputed, not written)
         if (tid < 2 * TX + 2 * TY)
@@ -365,31 +421,48 @@ __global__ void __launch_bounds__(256) k_fused(const __grid_constant__ FusedLaun
             if (tid < TX)
             {
                 const int hx = X.x0 + tid, hy = X.y0 - 1;
-                X.hn_at(ring, 2, 0, tid + 1) = hy >= 0 ? fused_h<T, 5>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
+                X.hn_at(ring, 2, 0, tid + 1) = hy >= 0 ? fused_h<T, 5, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
             }
             else if (tid < 2 * TX)
             {
                 const int hx = X.x0 + tid - TX, hy = X.y0 - 1;
-                X.hn_at(ring, 0, 0, tid - TX + 1) = hy >= 0 ? fused_h<T, 3>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
+                X.hn_at(ring, 0, 0, tid - TX + 1) = hy >= 0 ? fused_h<T, 3, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
             }
             else if (tid < 2 * TX + TY)
             {
                 const int hx = X.x0 - 1, hy = X.y0 + tid - 2 * TX;
-                X.hn_at(ring, 2, tid - 2 * TX + 1, 0) = hx >= 0 ? fused_h<T, 5>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
+                X.hn_at(ring, 2, tid - 2 * TX + 1, 0) = hx >= 0 ? fused_h<T, 5, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
             }
             else
             {
                 const int hx = X.x0 - 1, hy = X.y0 + tid - 2 * TX - TY;
-                X.hn_at(ring, 1, tid - 2 * TX - TY + 1, 0) = hx >= 0 ? fused_h<T, 4>(X, hx, hy, k, stA, stB, false, pml_plane) : T(0);
+                X.hn_at(ring, 1, tid - 2 * TX - TY + 1, 0) = hx >= 0 ? fused_h<T, 4, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
             }
         }
+        // material slots of the E components in this warp's row (warp-uniform)
+        bool e_slots = false;
+        if (owned && tx < 3 && y < PE.My && PE.slot[tx].map)
+        {
+            const RowRange r = PE.slot[tx].rows[y + (int64_t)k * PE.My];
+            e_slots = r.lo <= r.hi && r.lo < X.x0 + TX && r.hi >= X.x0;
+        }
+        e_slots = __any_sync(0xffffffffu, e_slots);
         __syncthreads();
         // 2. E(k) on the tile from H(k) and H(k-1)
         if (owned)
         {
-            fused_e<T, 0>(X, x, y, k, stA, ring, pml_plane);
-            fused_e<T, 1>(X, x, y, k, stA, ring, pml_plane);
-            fused_e<T, 2>(X, x, y, k, stA, ring, pml_plane);
+            if (inside)
+            {
+                fused_e<T, 0, false>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
+                fused_e<T, 1, false>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
+                fused_e<T, 2, false>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
+            }
+            else
+            {
+                fused_e<T, 0, true>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
+                fused_e<T, 1, true>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
+                fused_e<T, 2, true>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
+            }
         }
     }
 }
