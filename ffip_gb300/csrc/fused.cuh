@@ -351,6 +351,13 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
     const bool h_slots = F.h.slot[0].map || F.h.slot[1].map || F.h.slot[2].map;
 
     const int x = X.x0 + tx, y = X.y0 + ty;
+    // per-thread constants of the vacuum path
+    constexpr int BX = SH::BX;
+    const int offE = (ty + 1) * BX + tx + XOFF;  // own point in an E or H stage tile
+    const int offN = (ty + 1) * (TX + 1) + tx + 1;  // own point in an H ring plane
+    const int sz = (int)PE.sz;
+    const int own0 = x + y * (int)PE.sy;
+    const T coefH = F.h.coef_def, coefE = PE.coef_def, idh = F.h.inv_dx, ide = PE.inv_dx;
     for (int q = 0; q + 1 < NP; ++q)
     {
         const int stA = q % S, stB = (q + 1) % S;
@@ -401,42 +408,74 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
             dft_h = dft_h || (k >= U.i0[2] && k < U.i0[2] + U.ld[2] && U.i0[1] < X.y0 + TY && U.i0[1] + U.ld[1] > X.y0 &&
                               U.i0[0] < X.x0 + TX && U.i0[0] + U.ld[0] > X.x0);
         }
-        // 1. H(k) on the tile ...
-        if (inside)
+        const bool h_fast = inside && !pml_plane && !h_slots && !dft_h;
+        if (h_fast)
         {
-            X.hn_at(ring, 0, ty + 1, tx + 1) = fused_h<T, 3, false>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
-            X.hn_at(ring, 1, ty + 1, tx + 1) = fused_h<T, 4, false>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
-            X.hn_at(ring, 2, ty + 1, tx + 1) = fused_h<T, 5, false>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
+            // 1a. vacuum tile plane: H(k) from 12 staged values, no branches
+            const T *eA0 = X.e_tile(stA, 0), *eA1 = X.e_tile(stA, 1), *eA2 = X.e_tile(stA, 2);
+            const T *eB0 = X.e_tile(stB, 0), *eB1 = X.e_tile(stB, 1);
+            const T *hA0 = X.h_tile(stA, 0), *hA1 = X.h_tile(stA, 1), *hA2 = X.h_tile(stA, 2);
+            const T exa = eA0[offE], exy = eA0[offE + BX], exb = eB0[offE];
+            const T eya = eA1[offE], eyx = eA1[offE + 1], eyb = eB1[offE];
+            const T eza = eA2[offE], ezy = eA2[offE + BX], ezx = eA2[offE + 1];
+            const T hx0 = hA0[offE], hy0 = hA1[offE], hz0 = hA2[offE];
+            const T hx = hx0 + coefH * ((eza - ezy) * idh - (eya - eyb) * idh);
+            const T hy = hy0 + coefH * ((exa - exb) * idh - (eza - ezx) * idh);
+            const T hz = hz0 + coefH * ((eya - eyx) * idh - (exa - exy) * idh);
+            X.hn_at(ring, 0, ty + 1, tx + 1) = hx;
+            X.hn_at(ring, 1, ty + 1, tx + 1) = hy;
+            X.hn_at(ring, 2, ty + 1, tx + 1) = hz;
+            if (owned)
+            {
+                const int idx = own0 + k * sz;
+                F.hout[0][idx] = hx;
+                F.hout[1][idx] = hy;
+                F.hout[2][idx] = hz;
+            }
+            // halo: Hz, Hx on the low-y row (row 0), Hz, Hy on the low-x column
+            if (tid < 2 * TX + 2 * TY)
+            {
+                if (tid < 2 * TX)
+                {
+                    const int u = tid < TX ? tid : tid - TX, o = u + XOFF;  // row 0 of the tiles
+                    if (tid < TX)
+                        X.hn_at(ring, 2, 0, u + 1) = hA2[o] + coefH * ((eA1[o] - eA1[o + 1]) * idh - (eA0[o] - eA0[o + BX]) * idh);
+                    else
+                        X.hn_at(ring, 0, 0, u + 1) = hA0[o] + coefH * ((eA2[o] - eA2[o + BX]) * idh - (eA1[o] - eB1[o]) * idh);
+                }
+                else
+                {
+                    const int v = tid < 2 * TX + TY ? tid - 2 * TX : tid - 2 * TX - TY;
+                    const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
+                    if (tid < 2 * TX + TY)
+                        X.hn_at(ring, 2, v + 1, 0) = hA2[o] + coefH * ((eA1[o] - eA1[o + 1]) * idh - (eA0[o] - eA0[o + BX]) * idh);
+                    else
+                        X.hn_at(ring, 1, v + 1, 0) = hA1[o] + coefH * ((eA0[o] - eB0[o]) * idh - (eA2[o] - eA2[o + 1]) * idh);
+                }
+            }
         }
         else
         {
+            // 1b. general tile plane: H(k) on the tile ...
             X.hn_at(ring, 0, ty + 1, tx + 1) = fused_h<T, 3, true>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
             X.hn_at(ring, 1, ty + 1, tx + 1) = fused_h<T, 4, true>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
             X.hn_at(ring, 2, ty + 1, tx + 1) = fused_h<T, 5, true>(X, x, y, k, stA, stB, owned, pml_plane, h_slots, dft_h);
-        }
-        // ... and the halo the E update reads: Hz and Hx on the low-y row, Hz
-        // and Hy on the low-x column (recomputed, not written)
-        if (tid < 2 * TX + 2 * TY)
-        {
-            if (tid < TX)
+            // ... and the halo the E update reads (recomputed, not written)
+            if (tid < 2 * TX + 2 * TY)
             {
-                const int hx = X.x0 + tid, hy = X.y0 - 1;
-                X.hn_at(ring, 2, 0, tid + 1) = hy >= 0 ? fused_h<T, 5, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
-            }
-            else if (tid < 2 * TX)
-            {
-                const int hx = X.x0 + tid - TX, hy = X.y0 - 1;
-                X.hn_at(ring, 0, 0, tid - TX + 1) = hy >= 0 ? fused_h<T, 3, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
-            }
-            else if (tid < 2 * TX + TY)
-            {
-                const int hx = X.x0 - 1, hy = X.y0 + tid - 2 * TX;
-                X.hn_at(ring, 2, tid - 2 * TX + 1, 0) = hx >= 0 ? fused_h<T, 5, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
-            }
-            else
-            {
-                const int hx = X.x0 - 1, hy = X.y0 + tid - 2 * TX - TY;
-                X.hn_at(ring, 1, tid - 2 * TX - TY + 1, 0) = hx >= 0 ? fused_h<T, 4, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false) : T(0);
+                int hx, hy, comp, row, col;
+                if (tid < TX) { hx = X.x0 + tid; hy = X.y0 - 1; comp = 2; row = 0; col = tid + 1; }
+                else if (tid < 2 * TX) { hx = X.x0 + tid - TX; hy = X.y0 - 1; comp = 0; row = 0; col = tid - TX + 1; }
+                else if (tid < 2 * TX + TY) { hx = X.x0 - 1; hy = X.y0 + tid - 2 * TX; comp = 2; row = tid - 2 * TX + 1; col = 0; }
+                else { hx = X.x0 - 1; hy = X.y0 + tid - 2 * TX - TY; comp = 1; row = tid - 2 * TX - TY + 1; col = 0; }
+                T v = T(0);
+                if (hx >= 0 && hy >= 0)
+                {
+                    if (comp == 0) v = fused_h<T, 3, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false);
+                    else if (comp == 1) v = fused_h<T, 4, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false);
+                    else v = fused_h<T, 5, true>(X, hx, hy, k, stA, stB, false, pml_plane, h_slots, false);
+                }
+                X.hn_at(ring, comp, row, col) = v;
             }
         }
         // material slots of the E components in this warp's row (warp-uniform)
@@ -451,11 +490,23 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
         // 2. E(k) on the tile from H(k) and H(k-1)
         if (owned)
         {
-            if (inside)
+            if (inside && !pml_plane && !e_slots && !dft_e)
             {
-                fused_e<T, 0, false>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
-                fused_e<T, 1, false>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
-                fused_e<T, 2, false>(X, x, y, k, stA, ring, pml_plane, e_slots, dft_e);
+                const int prev = ring ^ 1;
+                const T *eA0 = X.e_tile(stA, 0), *eA1 = X.e_tile(stA, 1), *eA2 = X.e_tile(stA, 2);
+                const T *n0 = &X.hn_at(ring, 0, 0, 0), *n1 = &X.hn_at(ring, 1, 0, 0), *n2 = &X.hn_at(ring, 2, 0, 0);
+                const T *p0 = &X.hn_at(prev, 0, 0, 0), *p1 = &X.hn_at(prev, 1, 0, 0);
+                const T hzr = n2[offN], hzy = n2[offN - (TX + 1)], hzx = n2[offN - 1];
+                const T hyr = n1[offN], hyp = p1[offN], hyx = n1[offN - 1];
+                const T hxr = n0[offN], hxp = p0[offN], hxy = n0[offN - (TX + 1)];
+                const T ex0 = eA0[offE], ey0 = eA1[offE], ez0 = eA2[offE];
+                const T ex = ex0 + coefE * ((hzr - hzy) * ide - (hyr - hyp) * ide);
+                const T ey = ey0 + coefE * ((hxr - hxp) * ide - (hzr - hzx) * ide);
+                const T ez = ez0 + coefE * ((hyr - hyx) * ide - (hxr - hxy) * ide);
+                const int idx = own0 + k * sz;
+                F.eout[0][idx] = ex;
+                F.eout[1][idx] = ey;
+                F.eout[2][idx] = ez;
             }
             else
             {
