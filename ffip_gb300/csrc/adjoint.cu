@@ -73,20 +73,18 @@ __global__ void k_transpose(Grid3 g, const double *pt, long long n, double *out)
     scatter(g, pt[4 * i], pt[4 * i + 1], pt[4 * i + 2], pt[4 * i + 3], out);
 }
 
-__global__ void k_sensitivity(Grid3 g, double freq, double nr, double ni, const double *fwd, const double *adj,
+__global__ void k_sensitivity(Grid3 g, double wr, double wi, double nr, double ni, const double *fwd, const double *adj,
                               const double *deps, const double *xyz, long long n, double *out)
 {
     long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    // ((((2j pi) f) fwd) adj) deps / norm, in numpy's left-to-right order
-    const double two_pi = 2 * 3.141592653589793;
-    double ar = 0.0 * freq, ai = two_pi * freq;                       // 2j*pi*f
+    // (((w fwd) adj) deps) / norm, left to right as numpy evaluates it
     double br = fwd[2 * i], bi = fwd[2 * i + 1];
-    double tr = ar * br - ai * bi, ti = ar * bi + ai * br;           // * fwd
+    double tr = wr * br - wi * bi, ti = wr * bi + wi * br;            // w * fwd
     br = adj[2 * i]; bi = adj[2 * i + 1];
-    double ur = tr * br - ti * bi, ui = tr * bi + ti * br;           // * adj
+    double ur = tr * br - ti * bi, ui = tr * bi + ti * br;            // * adj
     br = deps[2 * i]; bi = deps[2 * i + 1];
-    tr = ur * br - ui * bi; ti = ur * bi + ui * br;                  // * deps
+    tr = ur * br - ui * bi; ti = ur * bi + ui * br;                   // * deps
     // real part of (tr + j ti) / (nr + j ni)
     const double den = nr * nr + ni * ni;
     const double se = (tr * nr + ti * ni) / den;
@@ -157,7 +155,7 @@ int adjoint_transpose(const double *gx, uint64_t nx, const double *gy, uint64_t 
     return 0;
 }
 
-int adjoint_sensitivity(double freq, double norm_re, double norm_im, const double *fwd, const double *adj,
+int adjoint_sensitivity(double w_re, double w_im, double norm_re, double norm_im, const double *fwd, const double *adj,
                         const double *deps, const double *xyz, uint64_t n, const double *gx, uint64_t nx,
                         const double *gy, uint64_t ny, const double *gz, uint64_t nz, double *out)
 {
@@ -168,7 +166,7 @@ int adjoint_sensitivity(double freq, double norm_re, double norm_im, const doubl
         double *df = to_device(fwd, 2 * n, keep), *da = to_device(adj, 2 * n, keep), *de = to_device(deps, 2 * n, keep);
         double *dx = to_device(xyz, 3 * n, keep);
         run_scatter(nx * ny * nz, out, [&](double *dout) {
-            if (n) k_sensitivity<<<(unsigned)((n + 255) / 256), 256>>>(g, freq, norm_re, norm_im, df, da, de, dx, (long long)n, dout);
+            if (n) k_sensitivity<<<(unsigned)((n + 255) / 256), 256>>>(g, w_re, w_im, norm_re, norm_im, df, da, de, dx, (long long)n, dout);
         });
     }
     catch (...)

@@ -14,7 +14,7 @@ Backend *new_default_backend(int device);  // the CUDA backend (kernels.cu); -1 
 void *backend_stream(Backend *be);
 int adjoint_transpose(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
                       const double *pt, uint64_t npts, double *out);
-int adjoint_sensitivity(double freq, double norm_re, double norm_im, const double *fwd, const double *adj,
+int adjoint_sensitivity(double w_re, double w_im, double norm_re, double norm_im, const double *fwd, const double *adj,
                         const double *deps, const double *xyz, uint64_t n, const double *gx, uint64_t nx,
                         const double *gy, uint64_t ny, const double *gz, uint64_t nz, double *out);
 } // namespace ffipg
@@ -244,14 +244,14 @@ int ffip_transpose(const double *gx, uint64_t nx, const double *gy, uint64_t ny,
     });
 }
 
-int ffip_sensitivity(double freq, double norm_re, double norm_im, const double *fwd, const double *adj, const double *deps,
+int ffip_sensitivity(double w_re, double w_im, double norm_re, double norm_im, const double *fwd, const double *adj, const double *deps,
                      const double *xyz, uint64_t n, const double *gx, uint64_t nx, const double *gy, uint64_t ny,
                      const double *gz, uint64_t nz, double *out)
 {
     return guard([&]() -> int {
         if (!gx || !gy || !gz || !out || (n && (!fwd || !adj || !deps || !xyz))) return fail(FFIP_ERR_INVALID, "null argument");
         if (nx < 1 || ny < 1 || nz < 1) return fail(FFIP_ERR_INVALID, "some grid size is 0");
-        return ffipg::adjoint_sensitivity(freq, norm_re, norm_im, fwd, adj, deps, xyz, n, gx, nx, gy, ny, gz, nz, out);
+        return ffipg::adjoint_sensitivity(w_re, w_im, norm_re, norm_im, fwd, adj, deps, xyz, n, gx, nx, gy, ny, gz, nz, out);
     });
 }
 

@@ -63,7 +63,8 @@ struct FusedLayout
     static constexpr int NX = SH::TX + 1, NY = SH::TY + 1, NZ = SH::KCH + 2;  // CPML table lengths
     static constexpr int PML_OFF = HN_OFF + 2 * HN_PLANE * (int)sizeof(T);
     static constexpr int PML_ELEMS = 6 * (NX + NY + NZ);  // [parity][b,c,ik][n] per axis
-    static constexpr int SMEM = PML_OFF + PML_ELEMS * (int)sizeof(T);
+    static constexpr int MASK_OFF = PML_OFF + PML_ELEMS * (int)sizeof(T);
+    static constexpr int SMEM = MASK_OFF + NZ * 4;  // per plane: bit r = row y0+r has E slots in the tile
 };
 
 template <typename T>
@@ -332,6 +333,19 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
             }
         }
     }
+    // per plane of the chunk, which tile rows contain E-side material slots in
+    // the tile's x range (one batch of loads, while the first planes arrive)
+    unsigned *slot_mask = reinterpret_cast<unsigned *>(smem + LY::MASK_OFF);
+    for (int t = tid; t < LY::NZ; t += TX * TY) slot_mask[t] = 0u;
+    __syncthreads();
+    for (int t = tid; t < LY::NZ * TY * 3; t += TX * TY)
+    {
+        const int c = t % 3, r = (t / 3) % TY, o = t / (3 * TY);
+        const int kk = X.k0 - 1 + o, yy = X.y0 + r;
+        if (!PE.slot[c].map || kk < 0 || kk >= PE.Mz || yy >= PE.My) continue;
+        const RowRange rr = PE.slot[c].rows[yy + (int64_t)kk * PE.My];
+        if (rr.lo <= rr.hi && rr.lo < X.x0 + TX && rr.hi >= X.x0) atomicOr(&slot_mask[o], 1u << r);
+    }
     tile_pml = __syncthreads_or(tile_pml);
     // the tile and its low-side halo lie inside every component's valid x/y
     // range; kin_lo..kin_hi: planes where every component is valid
@@ -479,13 +493,7 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
             }
         }
         // material slots of the E components in this warp's row (warp-uniform)
-        bool e_slots = false;
-        if (owned && tx < 3 && y < PE.My && PE.slot[tx].map)
-        {
-            const RowRange r = PE.slot[tx].rows[y + (int64_t)k * PE.My];
-            e_slots = r.lo <= r.hi && r.lo < X.x0 + TX && r.hi >= X.x0;
-        }
-        e_slots = __any_sync(0xffffffffu, e_slots);
+        const bool e_slots = (slot_mask[q] >> ty) & 1u;
         __syncthreads();
         // 2. E(k) on the tile from H(k) and H(k-1)
         if (owned)

@@ -56,8 +56,8 @@ def _declare(lib):
     lib.ffip_destroy.argtypes = [P]
     lib.ffip_last_error.restype = ctypes.c_char_p
     lib.ffip_transpose.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
-    lib.ffip_sensitivity.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, U64, D, U64, D, U64,
-                                     D, U64, D]
+    lib.ffip_sensitivity.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, U64,
+                                     D, U64, D, U64, D, U64, D]
     for f in EXPORTS:
         if f not in ("ffip_stream", "ffip_last_error"):
             getattr(lib, f).restype = ctypes.c_int

@@ -537,8 +537,18 @@ def _dptr(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
 
 
-def sensitivity_scatter(frequency, norm, fwd, adj, deps, x, y, z, gx, gy, gz):
-    """Re(2 pi j f fwd adj deps / norm) at points (x, y, z), scattered onto the
+def frequency_factor(frequency, dt=None):
+    """The factor that turns E_fwd E_adj / norm into d F / d epsilon.  The
+    reference uses the continuous 2 pi j f (ffip/simulation.py:858); the
+    leap-frog E update, (E^{n+1} - E^n)/dt with the pulse sampled at half
+    steps, makes it 2 j sin(pi f dt) / dt exactly (dt given)."""
+    if dt is None:
+        return 2j * pi * frequency
+    return 2j * np.sin(pi * frequency * dt) / dt
+
+
+def sensitivity_scatter(factor, norm, fwd, adj, deps, x, y, z, gx, gy, gz):
+    """Re(factor fwd adj deps / norm) at points (x, y, z), scattered onto the
     grid gx x gy x gz with the transpose of trilinear interpolation; on the GPU
     (ffip_sensitivity)."""
     lib = native.load()
@@ -548,8 +558,8 @@ def sensitivity_scatter(frequency, norm, fwd, adj, deps, x, y, z, gx, gy, gz):
     xyz = np.ascontiguousarray(np.stack([np.ravel(x), np.ravel(y), np.ravel(z)], axis=-1), dtype=np.float64)
     gx, gy, gz = (np.ascontiguousarray(np.asarray(v, dtype=np.float64)) for v in (gx, gy, gz))
     out = np.zeros((gz.size, gy.size, gx.size))
-    norm = complex(norm)
-    rc = lib.ffip_sensitivity(float(frequency), norm.real, norm.imag, _dptr(f), _dptr(a), _dptr(d), _dptr(xyz), n,
+    norm, factor = complex(norm), complex(factor)
+    rc = lib.ffip_sensitivity(factor.real, factor.imag, norm.real, norm.imag, _dptr(f), _dptr(a), _dptr(d), _dptr(xyz), n,
                               _dptr(gx), gx.size, _dptr(gy), gy.size, _dptr(gz), gz.size, _dptr(out))
     if rc != 0:
         raise native.FfipError(lib.ffip_last_error().decode())
@@ -615,11 +625,14 @@ class Adjoint_Volume:
         Z, Y, X = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
         return X.ravel(), Y.ravel(), Z.ravel()
 
-    def get_sensitivity(self):
+    def get_sensitivity(self, exact=False):
         """dF/drho on the density grid: Re(2 pi j f E_fwd E_adj deps/drho / norm)
         at every E point of the design box, transposed through the trilinear
-        density interpolation (simulation.py:841-869), on the GPU."""
+        density interpolation (simulation.py:841-869), on the GPU.  exact=True
+        uses the leap-frog factor 2 j sin(pi f dt)/dt instead of 2 pi j f."""
         rho_interp = RegularGridInterpolator((self.z, self.y, self.x), self.density, bounds_error=True)
+        dt = self.forward_simulation.dx * self.forward_simulation.courant
+        factor = frequency_factor(self.frequency, dt if exact else None)
         res = 0
         for i in range(3):
             x, y, z = self.design_points(i)
@@ -627,7 +640,7 @@ class Adjoint_Volume:
             fwd = self.forward_dfts[i].get_interpolant(method="linear", bounds_error=True)(pts)
             adj = self.adjoint_dfts[i].get_interpolant(method="linear", bounds_error=True)(pts)
             deps = self.epsilon_der(rho_interp(np.stack((z, y, x), axis=-1)))
-            res = res + sensitivity_scatter(self.frequency, self.norm, fwd, adj, np.asarray(deps, dtype=complex), x, y, z,
+            res = res + sensitivity_scatter(factor, self.norm, fwd, adj, np.asarray(deps, dtype=complex), x, y, z,
                                             self.x, self.y, self.z)
         return np.reshape(res, self.shape)
 

@@ -122,12 +122,13 @@ int ffip_transpose(const double *gx, uint64_t nx, const double *gy, uint64_t ny,
                    const double *pt, uint64_t npts, double *out);
 
 /* Adjoint_Volume.get_sensitivity (ffip/simulation.py:841-869) on the device:
- * for each of n points, se = Re(2 pi j f * fwd * adj * deps / norm) with
- * complex fwd, adj and deps (d epsilon / d rho) given as interleaved (re, im)
- * pairs, then the transpose of trilinear interpolation of se onto the
- * density grid, as ffip_transpose.
+ * for each of n points, se = Re(w * fwd * adj * deps / norm) with complex fwd,
+ * adj and deps (d epsilon / d rho) given as interleaved (re, im) pairs, then
+ * the transpose of trilinear interpolation of se onto the density grid, as
+ * ffip_transpose.  w = 2 pi j f reproduces the reference's formula;
+ * w = 2 j sin(pi f dt) / dt is the exact factor of the leap-frog E update.
  * Points are (x, y, z) triples.  out[nz][ny][nx] is overwritten. */
-int ffip_sensitivity(double freq, double norm_re, double norm_im, const double *fwd, const double *adj,
+int ffip_sensitivity(double w_re, double w_im, double norm_re, double norm_im, const double *fwd, const double *adj,
                      const double *deps, const double *xyz, uint64_t n, const double *gx, uint64_t nx,
                      const double *gy, uint64_t ny, const double *gz, uint64_t nz, double *out);
 

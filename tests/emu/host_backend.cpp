@@ -116,7 +116,7 @@ int adjoint_transpose(const double *, uint64_t, const double *, uint64_t, const 
 {
     throw std::runtime_error("not emulated");
 }
-int adjoint_sensitivity(double, double, double, const double *, const double *, const double *, const double *, uint64_t,
+int adjoint_sensitivity(double, double, double, double, const double *, const double *, const double *, const double *, uint64_t,
                         const double *, uint64_t, const double *, uint64_t, const double *, uint64_t, double *)
 {
     throw std::runtime_error("not emulated");

@@ -68,7 +68,7 @@ def test_sensitivity_matches_numpy():
     out = np.zeros((3, 9, 9))
     D = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(ctypes.POINTER(ctypes.c_double))
     keep = [np.ascontiguousarray(np.stack([a.real, a.imag], 1)) for a in (fwd, adj, deps)]
-    rc = lib.ffip_sensitivity(f, norm.real, norm.imag, D(keep[0]), D(keep[1]), D(keep[2]), D(xyz), n,
+    rc = lib.ffip_sensitivity(0.0, 2 * np.pi * f, norm.real, norm.imag, D(keep[0]), D(keep[1]), D(keep[2]), D(xyz), n,
                               D(gx), 9, D(gy), 9, D(gz), 3, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     assert rc == 0
     np.testing.assert_allclose(out, ref, rtol=1e-10, atol=1e-12)
