@@ -130,6 +130,19 @@ def peaks():
     return 6800.0, "fallback"
 
 
+def profiled_traffic(n):
+    """DRAM bytes per k_fused launch from the committed ncu summary of the
+    n^3 workload (dram__bytes_read.sum + dram__bytes_write.sum), or None."""
+    p = os.path.join(ROOT, "profiles", "k_fused_fp32_dispersive%d.md" % n)
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for line in f:
+            if line.startswith("| DRAM traffic per launch |"):
+                return float(line.split("|")[2].split()[0]) * 1e6
+    return None
+
+
 def dft_rel_err(a, b):
     g = "volume fields dft 0"
     scale = max(np.abs(b[g]["real"]).max(), np.abs(b[g]["imag"]).max())
@@ -233,7 +246,9 @@ def main():
            "data": "synthetic (seeded spheres, no dataset)", "config": cfg_meta,
            "gpu_launches": res["fp32"]["launches"],
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                        "traffic": None, "peak_kind": peak_kind,
+                        "traffic": profiled_traffic(a.n) if res["fp32"]["fused"] else None,
+                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one k_fused launch, "
+                                          "profiles/k_fused_fp32_dispersive%d.md" % a.n, "peak_kind": peak_kind,
                         "kernel": "k_fused" if res["fp32"]["fused"] else "k_update (H and E launches)",
                         "algorithmic_bytes_per_step": res["fp32"]["bytes_per_step"],
                         "timing": "CUDA events on the stepper's stream around the %d timed steps" % a.steps},
