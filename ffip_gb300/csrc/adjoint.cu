@@ -177,4 +177,54 @@ int adjoint_sensitivity(double w_re, double w_im, double norm_re, double norm_im
     for (double *p : keep) cudaFree(p);
     return 0;
 }
+
+// ffip_transpose_noalloc: the same k_transpose over a fixed, file-scope
+// device buffer instead of per-call cudaMalloc/cudaFree.  Layout inside the
+// buffer: the 4 * npts point doubles, then the nx * ny * nz output doubles
+// (the output region is zeroed on every call; the point region is fully
+// overwritten by the copy).  One buffer per device and per process: calls
+// that overlap on the same device race on it.
+namespace
+{
+constexpr uint64_t kTransposeScratchDoubles = uint64_t(1) << 20; // 8 MiB
+__device__ __align__(256) double g_transpose_scratch[kTransposeScratchDoubles];
+
+// address of g_transpose_scratch on each device, looked up once per device
+double *scratch_address(int device)
+{
+    constexpr int kMaxDevices = 64;
+    static double *addr[kMaxDevices] = {};
+    if (device < 0 || device >= kMaxDevices) throw std::runtime_error("device ordinal out of range");
+    if (!addr[device])
+    {
+        void *p = nullptr;
+        check(cudaGetSymbolAddress(&p, g_transpose_scratch), "cudaGetSymbolAddress");
+        addr[device] = static_cast<double *>(p);
+    }
+    return addr[device];
+}
+} // namespace
+
+uint64_t adjoint_transpose_noalloc_capacity() { return kTransposeScratchDoubles; }
+
+int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
+                              const double *pt, uint64_t npts, double *out)
+{
+    const uint64_t nout = nx * ny * nz;
+    if (npts > kTransposeScratchDoubles / 4 || nout > kTransposeScratchDoubles - 4 * npts)
+        throw std::length_error("ffip_transpose_noalloc: 4 * npts + nx * ny * nz = " + std::to_string(4 * npts + nout) +
+                                " doubles exceeds the fixed scratch of " + std::to_string(kTransposeScratchDoubles) +
+                                " doubles; use ffip_transpose");
+    int device = 0;
+    check(cudaGetDevice(&device), "cudaGetDevice");
+    double *base = scratch_address(device);
+    double *dpt = base, *dout = base + 4 * npts;
+    Grid3 g = make_grid(gx, nx, gy, ny, gz, nz);
+    if (npts) check(cudaMemcpy(dpt, pt, 4 * npts * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+    check(cudaMemset(dout, 0, nout * sizeof(double)), "cudaMemset");
+    if (npts) k_transpose<<<(unsigned)((npts + 255) / 256), 256>>>(g, dpt, (long long)npts, dout);
+    check(cudaGetLastError(), "adjoint kernel launch");
+    check(cudaMemcpy(out, dout, nout * sizeof(double), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    return 0;
+}
 } // namespace ffipg

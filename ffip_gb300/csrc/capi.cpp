@@ -17,6 +17,9 @@ int adjoint_transpose(const double *gx, uint64_t nx, const double *gy, uint64_t 
 int adjoint_sensitivity(double w_re, double w_im, double norm_re, double norm_im, const double *fwd, const double *adj,
                         const double *deps, const double *xyz, uint64_t n, const double *gx, uint64_t nx,
                         const double *gy, uint64_t ny, const double *gz, uint64_t nz, double *out);
+int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
+                              const double *pt, uint64_t npts, double *out);
+uint64_t adjoint_transpose_noalloc_capacity();
 } // namespace ffipg
 
 struct ffip_sim
@@ -252,6 +255,21 @@ int ffip_sensitivity(double w_re, double w_im, double norm_re, double norm_im, c
         if (!gx || !gy || !gz || !out || (n && (!fwd || !adj || !deps || !xyz))) return fail(FFIP_ERR_INVALID, "null argument");
         if (nx < 1 || ny < 1 || nz < 1) return fail(FFIP_ERR_INVALID, "some grid size is 0");
         return ffipg::adjoint_sensitivity(w_re, w_im, norm_re, norm_im, fwd, adj, deps, xyz, n, gx, nx, gy, ny, gz, nz, out);
+    });
+}
+
+int ffip_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
+                           const double *pt, uint64_t npts, double *out)
+{
+    return guard([&]() -> int {
+        if (!gx || !gy || !gz || !out || (!pt && npts)) return fail(FFIP_ERR_INVALID, "null argument");
+        if (nx < 1 || ny < 1 || nz < 1) return fail(FFIP_ERR_INVALID, "some grid size is 0");
+        const uint64_t cap = ffipg::adjoint_transpose_noalloc_capacity();
+        if (nx > cap || ny > cap || nz > cap || nx * ny > cap || nx * ny * nz > cap)
+            return fail(FFIP_ERR_INVALID, "ffip_transpose_noalloc: grid of " + std::to_string(nx) + " x " + std::to_string(ny) +
+                                              " x " + std::to_string(nz) + " exceeds the fixed scratch of " +
+                                              std::to_string(cap) + " doubles; use ffip_transpose");
+        return ffipg::adjoint_transpose_noalloc(gx, nx, gy, ny, gz, nz, pt, npts, out);
     });
 }
 

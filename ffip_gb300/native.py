@@ -35,7 +35,7 @@ class Stats(ctypes.Structure):
 
 EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_run", "ffip_output_count", "ffip_output_group", "ffip_output_array",
            "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync", "ffip_stream", "ffip_destroy",
-           "ffip_last_error", "ffip_transpose", "ffip_sensitivity"]
+           "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc"]
 
 
 def _declare(lib):
@@ -56,6 +56,7 @@ def _declare(lib):
     lib.ffip_destroy.argtypes = [P]
     lib.ffip_last_error.restype = ctypes.c_char_p
     lib.ffip_transpose.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
+    lib.ffip_transpose_noalloc.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
     lib.ffip_sensitivity.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, U64,
                                      D, U64, D, U64, D, U64, D]
     for f in EXPORTS:
@@ -201,6 +202,23 @@ def transpose(gx, gy, gz, pt, lib=None) -> np.ndarray:
         raise ValueError("shape(1) of pts is not 4")
     out = np.zeros((gz.size, gy.size, gx.size), dtype=np.float64)
     rc = L.ffip_transpose(_dptr(gx), gx.size, _dptr(gy), gy.size, _dptr(gz), gz.size, _dptr(pt), pt.shape[0], _dptr(out))
+    if rc != 0:
+        raise FfipError(L.ffip_last_error().decode())
+    return out
+
+
+def transpose_noalloc(gx, gy, gz, pt, lib=None) -> np.ndarray:
+    """transpose() through ffip_transpose_noalloc: no device allocation, at
+    most 4 * npts + nx * ny * nz = 2**20 doubles, calls on one device must
+    not overlap."""
+    L = lib if lib is not None else load()
+    gx, gy, gz = (np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel()) for v in (gx, gy, gz))
+    pt = np.ascontiguousarray(np.asarray(pt, dtype=np.float64))
+    if pt.ndim != 2 or pt.shape[1] != 4:
+        raise ValueError("pts must have shape (n, 4)")
+    out = np.zeros((gz.size, gy.size, gx.size), dtype=np.float64)
+    rc = L.ffip_transpose_noalloc(_dptr(gx), gx.size, _dptr(gy), gy.size, _dptr(gz), gz.size, _dptr(pt), pt.shape[0],
+                                  _dptr(out))
     if rc != 0:
         raise FfipError(L.ffip_last_error().decode())
     return out

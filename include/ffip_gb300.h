@@ -132,6 +132,25 @@ int ffip_sensitivity(double w_re, double w_im, double norm_re, double norm_im, c
                      const double *deps, const double *xyz, uint64_t n, const double *gx, uint64_t nx,
                      const double *gy, uint64_t ny, const double *gz, uint64_t nz, double *out);
 
+/* ffip_transpose without any device allocation.  No counterpart in the
+ * reference (its transpose runs on the host).  Same arguments, result and
+ * errors as ffip_transpose, but the points and the output grid are staged in
+ * one fixed 8 MiB device buffer compiled into the library (a file-scope
+ * __device__ array) instead of cudaMalloc/cudaFree per call.  For callers
+ * that must not allocate: a process whose HBM is fully committed to field
+ * arrays, where a per-call cudaMalloc fails, and a density-update loop that
+ * runs beside a stepping simulation, where cudaMalloc/cudaFree would
+ * synchronise the device.
+ * Limit: 4 * npts + nx * ny * nz <= 1048576 doubles; larger inputs return
+ * FFIP_ERR_INVALID with a message, use ffip_transpose for them.
+ * The output part of the buffer is zeroed by every call.  The buffer is
+ * shared by all calls on a device: calls that overlap on one device (from
+ * several threads) race and must be serialised by the caller.  The first
+ * call on each device looks the buffer's address up with
+ * cudaGetSymbolAddress; make that first call outside any stream capture. */
+int ffip_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
+                           const double *pt, uint64_t npts, double *out);
+
 #ifdef __cplusplus
 }
 #endif

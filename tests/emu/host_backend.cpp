@@ -121,4 +121,10 @@ int adjoint_sensitivity(double, double, double, double, const double *, const do
 {
     throw std::runtime_error("not emulated");
 }
+int adjoint_transpose_noalloc(const double *, uint64_t, const double *, uint64_t, const double *, uint64_t, const double *,
+                              uint64_t, double *)
+{
+    throw std::runtime_error("not emulated");
+}
+uint64_t adjoint_transpose_noalloc_capacity() { return uint64_t(1) << 20; }
 } // namespace ffipg
