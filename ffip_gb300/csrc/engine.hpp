@@ -41,8 +41,9 @@ struct Backend
     virtual void update(const SideParams<double> &p, bool is_e) = 0;
     virtual void update(const SideParams<float> &p, bool is_e) = 0;
     virtual bool has_fused() const { return false; }
-    virtual void fused(const FusedParams<double> &) {}
-    virtual void fused(const FusedParams<float> &) {}
+    // one fused time step; returns the number of kernels it launched
+    virtual int fused(const FusedParams<double> &) { return 0; }
+    virtual int fused(const FusedParams<float> &) { return 0; }
     virtual void sources(const SourceParams<double> &p) = 0;
     virtual void sources(const SourceParams<float> &p) = 0;
     virtual void ghosts(const GhostParams<double> &p) = 0;
@@ -76,6 +77,8 @@ public:
     virtual std::vector<OutputGroup> outputs() = 0;
     virtual void reset() = 0;
     virtual void set_density(const std::string &dataset, const double *rho, uint64_t n) = 0;
+    // new amplitude/phase datasets of inhomogeneous sources; zeroes the state
+    virtual void set_source_data(const std::map<std::string, std::vector<double>> &data) = 0;
     virtual const Plan &plan() const = 0;
     virtual bool fused() const = 0;
     virtual int64_t launches() const = 0;  // kernel launches issued so far

@@ -12,6 +12,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -196,7 +197,7 @@ public:
     bool has_fused() const override { return true; }
 
     template <typename T>
-    void fused_t(const FusedParams<T> &p)
+    int fused_t(const FusedParams<T> &p)
     {
         use();
         using SH = FusedShape<T>;
@@ -210,6 +211,9 @@ public:
         if (!attr_set)
         {
             check(cudaFuncSetAttribute(k_fused<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM), "cudaFuncSetAttribute");
+            // shared memory before L1: several CTAs of the pass per SM
+            check(cudaFuncSetAttribute(k_fused<T>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared),
+                  "cudaFuncSetAttribute");
             attr_set = true;
         }
         FusedLaunch<T> L;
@@ -220,13 +224,50 @@ public:
         }
         L.fp = p;
         L.err = err_;
+        // valid extents over all six components
+        int xend = 0, yend = 0, kbeg = p.e.Mz, kend = 0;
+        for (int sd = 0; sd < 2; ++sd)
+        {
+            const SideParams<T> &P = sd == 0 ? p.e : p.h;
+            for (int c = 0; c < 3; ++c)
+            {
+                xend = std::max(xend, P.vhi[c][0] + 1);
+                yend = std::max(yend, P.vhi[c][1] + 1);
+                kbeg = std::min(kbeg, P.vlo[c][2]);
+                kend = std::max(kend, P.vhi[c][2] + 1);
+            }
+        }
+        // tiles start at index 1; one or two layers beyond a whole number of
+        // tiles go to k_face
+        const int nxp = xend - 1, nyp = yend - 1;
+        const int rx = nxp % SH::TX, ry = nyp % SH::TY;
+        const int nbx = (nxp >= SH::TX && rx <= 2) ? nxp / SH::TX : (nxp + SH::TX - 1) / SH::TX;
+        const int nby = (nyp >= SH::TY && ry <= 2) ? nyp / SH::TY : (nyp + SH::TY - 1) / SH::TY;
+        L.xlim = std::min(xend, 1 + nbx * SH::TX);
+        L.ylim = std::min(yend, 1 + nby * SH::TY);
+        L.xend = xend;
+        L.yend = yend;
+        L.kbeg = kbeg;
+        L.kend = std::max(kend, kbeg + 1);
         dim3 block(SH::TX, SH::TY);
-        dim3 grid((p.e.Mx + SH::TX - 1) / SH::TX, (p.e.My + SH::TY - 1) / SH::TY, (p.e.Mz + SH::KCH - 1) / SH::KCH);
+        dim3 grid(std::max(nbx, 1), std::max(nby, 1), (L.kend - L.kbeg + SH::KCH - 1) / SH::KCH);
         k_fused<T><<<grid, block, LY::SMEM, stream_>>>(L);
         check(cudaGetLastError(), "k_fused launch");
+        int n = 1;
+        const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
+        if (nface > 0)
+        {
+            const unsigned blocks = (unsigned)((nface + 255) / 256);
+            k_face<T, false><<<blocks, 256, 0, stream_>>>(L);
+            check(cudaGetLastError(), "k_face launch");
+            k_face<T, true><<<blocks, 256, 0, stream_>>>(L);
+            check(cudaGetLastError(), "k_face launch");
+            n += 2;
+        }
+        return n;
     }
-    void fused(const FusedParams<double> &p) override { fused_t(p); }
-    void fused(const FusedParams<float> &p) override { fused_t(p); }
+    int fused(const FusedParams<double> &p) override { return fused_t(p); }
+    int fused(const FusedParams<float> &p) override { return fused_t(p); }
 
     template <typename T>
     CUtensorMap map_for(const T *base, int Mx, int My, int Mz, int bx, int by)

@@ -127,24 +127,30 @@ FFIP_HD int pick(int i, int j, int k)
 }
 
 // CPML combination at a point where c1 or c2 is non-zero (PML_Stepping::step,
-// src/fields.cpp:98-107).  psi is read from pin and, when pout is not null,
-// written to pout.
+// src/fields.cpp:98-107), from psi values already loaded (psi1/psi2 are not
+// used where the matching c is 0).  *ps1/*ps2 receive the new psi.
+template <typename T>
+FFIP_HD T pml_term(T cv1, T cv2, T b1, T b2, T ik1, T ik2, T curl1, T curl2, T psi1, T psi2, T *ps1, T *ps2)
+{
+    const T p1 = cv1 != T(0) ? b1 * psi1 + cv1 * curl1 : T(0);
+    const T p2 = cv2 != T(0) ? b2 * psi2 + cv2 * curl2 : T(0);
+    *ps1 = p1;
+    *ps2 = p2;
+    return p1 - p2 + curl1 * ik1 - curl2 * ik2;
+}
+
+// The same with psi read from pin and, when pout is not null, written to pout.
 template <typename T>
 FFIP_HD T pml_combine(T cv1, T cv2, T b1, T b2, T ik1, T ik2, T curl1, T curl2, const T *pin1, const T *pin2, T *pout1,
                       T *pout2, int64_t idx)
 {
-    T ps1 = T(0), ps2 = T(0);
-    if (cv1 != T(0))
-    {
-        ps1 = b1 * pin1[idx] + cv1 * curl1;
-        if (pout1) pout1[idx] = ps1;
-    }
-    if (cv2 != T(0))
-    {
-        ps2 = b2 * pin2[idx] + cv2 * curl2;
-        if (pout2) pout2[idx] = ps2;
-    }
-    return ps1 - ps2 + curl1 * ik1 - curl2 * ik2;
+    const T psi1 = cv1 != T(0) ? pin1[idx] : T(0);
+    const T psi2 = cv2 != T(0) ? pin2[idx] : T(0);
+    T ps1, ps2;
+    const T t = pml_term(cv1, cv2, b1, b2, ik1, ik2, curl1, curl2, psi1, psi2, &ps1, &ps2);
+    if (cv1 != T(0) && pout1) pout1[idx] = ps1;
+    if (cv2 != T(0) && pout2) pout2[idx] = ps2;
+    return t;
 }
 
 // curl increment of accdb at a point, CPML tables read from global memory
