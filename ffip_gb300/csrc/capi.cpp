@@ -2,6 +2,7 @@
 #include "../../include/ffip_gb300.h"
 
 #include <cstring>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -180,6 +181,21 @@ int ffip_set_density(ffip_sim *sim, const char *dataset, const double *rho, uint
     return guard([&]() -> int {
         if (!sim || !dataset || (!rho && n)) return fail(FFIP_ERR_INVALID, "null argument");
         sim->eng->set_density(dataset, rho, n);
+        return FFIP_OK;
+    });
+}
+
+int ffip_set_source_data(ffip_sim *sim, const ffip_dataset *datasets, uint64_t n)
+{
+    return guard([&]() -> int {
+        if (!sim || (!datasets && n)) return fail(FFIP_ERR_INVALID, "null argument");
+        std::map<std::string, std::vector<double>> data;
+        for (uint64_t i = 0; i < n; ++i)
+        {
+            if (!datasets[i].name || (!datasets[i].data && datasets[i].n)) return fail(FFIP_ERR_INVALID, "null dataset");
+            data[datasets[i].name].assign(datasets[i].data, datasets[i].data + datasets[i].n);
+        }
+        sim->eng->set_source_data(data);
         return FFIP_OK;
     });
 }

@@ -58,6 +58,7 @@ public:
     std::vector<OutputGroup> outputs() override;
     void reset() override;
     void set_density(const std::string &dataset, const double *rho, uint64_t n) override;
+    void set_source_data(const std::map<std::string, std::vector<double>> &data) override;
     double bytes_per_step() const override { return bytes_per_step_; }
 
 private:
@@ -65,6 +66,7 @@ private:
     Backend *be_;
     std::vector<void *> allocs_;       // freed with the engine
     std::vector<void *> slot_allocs_;  // freed when the media change
+    std::vector<void *> src_allocs_;   // freed when the sources change
     T *buf_[2][6]{};                   // field buffers; [1] only with the fused pass
     int cur_{0};
     T *psi_[6][2]{};
@@ -86,26 +88,31 @@ private:
     int64_t scratch_n_{0};
     double bytes_per_step_{0};
 
+    // allocation lifetimes: with the engine, until the media change, until
+    // the sources change
+    enum Life { kEngine = 0, kMedia = 1, kSources = 2 };
     template <typename U>
-    U *dalloc(size_t n, bool slot = false)
+    U *dalloc(size_t n, int life = kEngine)
     {
         if (n == 0) return nullptr;
         void *p = be_->alloc(n * sizeof(U));
-        (slot ? slot_allocs_ : allocs_).push_back(p);
+        (life == kMedia ? slot_allocs_ : life == kSources ? src_allocs_ : allocs_).push_back(p);
         return (U *)p;
     }
     template <typename U>
-    U *upload(const std::vector<U> &v, bool slot = false)
+    U *upload(const std::vector<U> &v, int life = kEngine)
     {
-        U *p = dalloc<U>(v.size(), slot);
+        U *p = dalloc<U>(v.size(), life);
         if (p) be_->h2d(p, v.data(), v.size() * sizeof(U));
         return p;
     }
     void free_all()
     {
         for (void *p : slot_allocs_) be_->release(p);
+        for (void *p : src_allocs_) be_->release(p);
         for (void *p : allocs_) be_->release(p);
         slot_allocs_.clear();
+        src_allocs_.clear();
         allocs_.clear();
     }
 
@@ -221,20 +228,20 @@ void Engine<T>::init_media()
             if (L.group[s] > 255) throw std::runtime_error("more than 256 distinct pole patterns");
             grp[s] = (uint8_t)L.group[s];
         }
-        D.map = upload(map, true);
-        D.rows = upload(rows, true);
-        D.g = upload(g, true);
-        D.coef = upload(coef, true);
-        D.inv = upload(inv, true);
-        D.group = upload(grp, true);
+        D.map = upload(map, kMedia);
+        D.rows = upload(rows, kMedia);
+        D.g = upload(g, kMedia);
+        D.coef = upload(coef, kMedia);
+        D.inv = upload(inv, kMedia);
+        D.group = upload(grp, kMedia);
         if (D.poles)
         {
-            if (c >= 3) D.A = dalloc<T>(D.n, true);  // H sources are applied before the H update
+            if (c >= 3) D.A = dalloc<T>(D.n, kMedia);  // H sources are applied before the H update
             std::vector<T> amp(L.amp.size());
             for (size_t q = 0; q < amp.size(); ++q) amp[q] = (T)L.amp[q];
-            D.amp = upload(amp, true);
-            D.P = dalloc<T>(amp.size(), true);
-            D.P1 = dalloc<T>(amp.size(), true);
+            D.amp = upload(amp, kMedia);
+            D.P = dalloc<T>(amp.size(), kMedia);
+            D.P1 = dalloc<T>(amp.size(), kMedia);
         }
     }
     for (int side = 0; side < 2; ++side)
@@ -250,12 +257,12 @@ void Engine<T>::init_media()
                 pool[g * kMaxPolesDev + q] = (uint8_t)G[g].pool[q];
             }
         }
-        grp_np_[side] = upload(np, true);
-        grp_pool_[side] = upload(pool, true);
+        grp_np_[side] = upload(np, kMedia);
+        grp_pool_[side] = upload(pool, kMedia);
         std::vector<T> pc(std::max<size_t>(P_.pool_coef[side].size(), 1) * 3, T(0));
         for (size_t q = 0; q < P_.pool_coef[side].size(); ++q)
             for (int t = 0; t < 3; ++t) pc[3 * q + t] = (T)P_.pool_coef[side][q][t];
-        pool_c_[side] = upload(pc, true);
+        pool_c_[side] = upload(pc, kMedia);
     }
 }
 
@@ -335,14 +342,14 @@ void Engine<T>::init_sources()
             }
             off.push_back((int)amp.size());
         }
-        S.comp = upload(c8);
-        S.lin = upload(lin);
-        S.off = upload(off);
-        S.amp = upload(amp);
-        S.start = upload(st);
-        S.end = upload(en);
-        S.width = upload(wd);
-        S.kind = upload(kind);
+        S.comp = upload(c8, kSources);
+        S.lin = upload(lin, kSources);
+        S.off = upload(off, kSources);
+        S.amp = upload(amp, kSources);
+        S.start = upload(st, kSources);
+        S.end = upload(en, kSources);
+        S.width = upload(wd, kSources);
+        S.kind = upload(kind, kSources);
         // DFT memberships of each source point (applied with the E sources,
         // which are added after the fused/unfused E update)
         std::vector<int> moff(1, 0), munit;
@@ -362,9 +369,9 @@ void Engine<T>::init_sources()
             }
             moff.push_back((int)munit.size());
         }
-        S.moff = upload(moff);
-        S.munit = upload(munit);
-        S.mlin = upload(mlin);
+        S.moff = upload(moff, kSources);
+        S.munit = upload(munit, kSources);
+        S.mlin = upload(mlin, kSources);
     }
 }
 
@@ -614,8 +621,7 @@ void Engine<T>::one_step()
                 fp.psih_out[c][s] = even ? b : a;
             }
         }
-        be_->fused(fp);
-        ++nlaunch_;
+        nlaunch_ += be_->fused(fp);
         cur_ = nx;
         for (int c = 0; c < 3; ++c)
         {
@@ -909,6 +915,26 @@ void Engine<T>::set_density(const std::string &dataset, const double *rho, uint6
     init_media();
     reset();
     compute_bytes();
+}
+template <typename T>
+void Engine<T>::set_source_data(const std::map<std::string, std::vector<double>> &data)
+{
+    for (auto &kv : data)
+    {
+        auto it = P_.source_data.find(kv.first);
+        if (it == P_.source_data.end())
+            throw std::runtime_error("no inhomogeneous source uses dataset '" + kv.first + "'");
+        if (kv.second.size() != it->second.size())
+            throw std::runtime_error("dataset '" + kv.first + "' has " + std::to_string(kv.second.size()) +
+                                     " values, the source uses " + std::to_string(it->second.size()));
+    }
+    for (auto &kv : data) P_.source_data[kv.first] = kv.second;
+    be_->sync();
+    rebuild_sources(P_);
+    for (void *p : src_allocs_) be_->release(p);
+    src_allocs_.clear();
+    init_sources();
+    reset();
 }
 } // namespace
 

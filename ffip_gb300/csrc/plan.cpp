@@ -855,22 +855,41 @@ void build_plan(const Json &cfg, const std::map<std::string, Dataset> &ds, Plan 
             p.geom_info.push_back(gi);
         }
     // sources, src/simulation.cpp:338-357
-    p.dipoles[0].clear();
-    p.dipoles[1].clear();
-    p.turnoff_time = 0;
-    if (cfg.has("sources"))
-        for (auto &s : cfg.at("sources").items())
-        {
-            const std::string &t = s.at("type").str();
-            if (t == "volume source") set_volume_source(p, s);
-            else if (t == "inhomogeneous source") set_inhom_source(p, s, ds);
-            else throw std::runtime_error("unknown source type '" + t + "'");
-        }
+    p.has_sources = cfg.has("sources");
+    p.source_data.clear();
+    if (p.has_sources)
+    {
+        p.sources_cfg = cfg.at("sources");
+        for (auto &s : p.sources_cfg.items())
+            if (s.at("type").str() == "inhomogeneous source")
+                for (const char *key : {"amplitude dataset", "phase dataset"})
+                {
+                    const std::string &name = s.at(key).str();
+                    p.source_data[name] = get_dataset(ds, name);
+                }
+    }
+    rebuild_sources(p);
     if (cfg.has("fields output")) set_fields_output(p, cfg.at("fields output"));
     if (cfg.has("stop condition"))
     {
         p.stop = cfg.at("stop condition");
         p.has_stop = true;
+    }
+}
+void rebuild_sources(Plan &p)
+{
+    p.dipoles[0].clear();
+    p.dipoles[1].clear();
+    p.turnoff_time = 0;
+    if (!p.has_sources) return;
+    std::map<std::string, Dataset> ds;
+    for (auto &kv : p.source_data) ds[kv.first] = Dataset{kv.second.data(), kv.second.size()};
+    for (auto &s : p.sources_cfg.items())
+    {
+        const std::string &t = s.at("type").str();
+        if (t == "volume source") set_volume_source(p, s);
+        else if (t == "inhomogeneous source") set_inhom_source(p, s, ds);
+        else throw std::runtime_error("unknown source type '" + t + "'");
     }
 }
 } // namespace ffipg

@@ -170,6 +170,9 @@ struct Plan
     // sources, in the reference's insertion order, split by side
     std::vector<Dipole> dipoles[2];
     double turnoff_time{0};
+    Json sources_cfg;  // the config's "sources" array (replayed by rebuild_sources)
+    bool has_sources{false};
+    std::map<std::string, std::vector<double>> source_data;  // datasets the inhomogeneous sources read
     // DFT
     std::vector<DftUnit> units;
     std::vector<DftRequest> requests;
@@ -202,6 +205,10 @@ void build_plan(const Json &cfg, const std::map<std::string, Dataset> &datasets,
 
 // Rebuilds the material slots (after a density dataset changed).
 void rasterize_media(Plan &plan);
+
+// Rebuilds the dipole lists from sources_cfg and source_data (after an
+// inhomogeneous source's amplitude/phase datasets changed).
+void rebuild_sources(Plan &plan);
 
 // Component closure of a box (include/utility.hpp:546-552)
 void component_closure(const double p1[3], const double p2[3], int ctype, int c1[3], int c2[3]);

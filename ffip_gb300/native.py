@@ -35,7 +35,8 @@ class Stats(ctypes.Structure):
 
 EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_run", "ffip_output_count", "ffip_output_group", "ffip_output_array",
            "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync", "ffip_stream", "ffip_destroy",
-           "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc"]
+           "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc",
+           "ffip_set_source_data"]
 
 
 def _declare(lib):
@@ -48,6 +49,7 @@ def _declare(lib):
     lib.ffip_output_group.argtypes = [P, ctypes.c_int, ctypes.c_char_p, U64]
     lib.ffip_output_array.argtypes = [P, ctypes.c_int, ctypes.c_char_p, D, U64, ctypes.POINTER(U64), ctypes.POINTER(ctypes.c_int)]
     lib.ffip_set_density.argtypes = [P, ctypes.c_char_p, D, U64]
+    lib.ffip_set_source_data.argtypes = [P, ctypes.POINTER(Dataset), U64]
     lib.ffip_reset.argtypes = [P]
     lib.ffip_get_stats.argtypes = [P, ctypes.POINTER(Stats)]
     lib.ffip_sync.argtypes = [P]
@@ -133,6 +135,16 @@ class NativeSim:
     def set_density(self, dataset: str, rho: np.ndarray):
         a = np.ascontiguousarray(np.asarray(rho, dtype=np.float64).ravel())
         self._check(self.lib.ffip_set_density(self.h, dataset.encode(), _dptr(a), a.size))
+
+    def set_source_data(self, datasets: Dict[str, np.ndarray]):
+        """New amplitude/phase datasets of inhomogeneous sources; resets the fields."""
+        keep = []
+        arr = (Dataset * max(1, len(datasets)))()
+        for i, (k, v) in enumerate(datasets.items()):
+            a = np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel())
+            keep.append(a)
+            arr[i] = Dataset(k.encode(), _dptr(a), a.size)
+        self._check(self.lib.ffip_set_source_data(self.h, arr, len(datasets)))
 
     def stats(self) -> dict:
         s = Stats()

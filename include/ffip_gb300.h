@@ -98,6 +98,16 @@ int ffip_output_array(ffip_sim *sim, int group, const char *array, double *out, 
  * design iteration without re-parsing the config. */
 int ffip_set_density(ffip_sim *sim, const char *dataset, const double *rho, uint64_t n);
 
+/* Replaces amplitude / phase datasets of the inhomogeneous sources that read
+ * them (Simulation::set_inhom_source, src/simulation.cpp:284-336; written by
+ * Inhom_Source.dump, ffip/source.py:126-129 — the adjoint sources of
+ * Adjoint_Source.eval_functionals_and_set_sources, ffip/simulation.py:
+ * 728-753), rebuilds the dipoles and resets the fields to time step 0 — the
+ * adjoint run of a design iteration without re-parsing the config.  Each
+ * dataset must keep its size; a name no inhomogeneous source reads is an
+ * error (FFIP_ERR_INVALID). */
+int ffip_set_source_data(ffip_sim *sim, const ffip_dataset *datasets, uint64_t n);
+
 /* Zeroes fields, auxiliary state and DFT sums; time_step = 0. */
 int ffip_reset(ffip_sim *sim);
 

@@ -67,3 +67,27 @@ def test_set_density_equals_fresh_run(lib):
         again = flatten(s.outputs())
     for k in fresh:
         assert np.array_equal(fresh[k], again[k]), k
+
+
+def test_set_source_data_equals_fresh_run(lib):
+    from ffip_gb300 import native
+    cfg, ds, _ = load("density_boxes")
+    rng = np.random.default_rng(9)
+    amp = rng.uniform(0.5, 2.0, size=ds["inhom source amplitude 0"].shape)
+    phase = rng.uniform(-np.pi, np.pi, size=ds["inhom source phase 0"].shape)
+    ds2 = dict(ds)
+    ds2["inhom source amplitude 0"] = amp
+    ds2["inhom source phase 0"] = phase
+    fresh = flatten(native.run_json(cfg, ds2, lib=lib))
+    with native.NativeSim(cfg, ds, lib=lib) as s:
+        s.run(cfg["stop condition"])
+        s.set_source_data({"inhom source amplitude 0": amp, "inhom source phase 0": phase})
+        assert s.stats()["time_step"] == 0
+        s.run(cfg["stop condition"])
+        again = flatten(s.outputs())
+        with pytest.raises(native.FfipError, match="no inhomogeneous source"):
+            s.set_source_data({"two medium box 0": amp})
+        with pytest.raises(native.FfipError, match="values"):
+            s.set_source_data({"inhom source amplitude 0": amp[:-1]})
+    for k in fresh:
+        assert np.array_equal(fresh[k], again[k]), k
