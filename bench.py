@@ -162,6 +162,43 @@ def cpu_leg(cfg, steps, warmup, threads):
     return dt, setup
 
 
+def design_leg(iters, dev, world):
+    """Seconds per design iteration on the adjoint workload: 192 x 192 x 160
+    cells, 16-cell CPML, 96 x 96 x 24 design box (97 x 97 x 25 density nodes,
+    seeded filtered noise, eps = 1 + 11 rho), Ex sheet below, |Ex|^2 at 4
+    probe cells above at 3 frequencies; fp32 state; one forward run and three
+    adjoint runs of 5000 steps per iteration, then the gradient on the
+    density nodes.  The first iteration (which also builds the four device
+    simulations) is reported apart; each timed iteration takes a small
+    gradient step, so densities and adjoint sources change every time."""
+    from ffip_gb300 import workloads
+    prob, rho = workloads.adjoint_design(precision="fp32")
+    for sim in [prob.forward_simulation] + [t.adjoint_simulation for t in prob.terms]:
+        sim.device = dev
+    barrier(world)
+    t0 = time.perf_counter()
+    F, g = prob.value_and_gradient(rho)
+    first = time.perf_counter() - t0
+    times, values = [], [F]
+    for _ in range(iters):
+        step = 0.05 / max(np.abs(g).max(), 1e-30)
+        rho = np.clip(rho - step * g, 0.0, 1.0)
+        barrier(world)
+        t0 = time.perf_counter()
+        F, g = prob.value_and_gradient(rho)
+        times.append(allmax(world, time.perf_counter() - t0))
+        values.append(F)
+    prob.release()
+    steps = int(round(prob.stop.time / 0.5))
+    cells = 192 * 192 * 160
+    return {"value": statistics.median(times), "unit": "s/design iter", "first_iter_s": first,
+            "iters_timed": iters, "runs_per_iter": 1 + len(prob.terms), "steps_per_run": steps,
+            "gcell_updates_per_s": (1 + len(prob.terms)) * steps * cells / statistics.median(times) / 1e9,
+            "objective": values, "dtype": "f32 state, f64 DFT and gradient",
+            "workload": "adjoint design 192x192x160, 16-cell CPML, 96x96x24 design box, Ex sheet, "
+                        "|Ex|^2 at 4 probes x 3 freqs, 5000 steps per run"}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -174,6 +211,8 @@ def main():
     ap.add_argument("--engine", default="auto")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--fp32-only", action="store_true", help="time only the fp32 stepper (profiling runs)")
+    ap.add_argument("--design-iters", type=int, default=2,
+                    help="timed design iterations of the adjoint workload (0: skip that leg)")
     a = ap.parse_args()
     world, rank, local = dist_init()
     from ffip_gb300 import workloads
@@ -280,6 +319,11 @@ def main():
                        "seconds": dt}
         out["e2e"] = e2e
         out["dft_rel_err_fp32_vs_fp64"] = dft_rel_err(full["fp32"], full["fp64"])
+
+    # ---- design iterations of the adjoint workload (forward + one adjoint
+    #      run per frequency + gradient), simulations kept between iterations
+    if a.design_iters > 0 and not a.fp32_only:
+        out["design_iter"] = design_leg(a.design_iters, dev, world)
 
     # ---- CPU baseline sample (rank 0 only)
     if rank == 0 and world == 1 and not a.no_cpu:

@@ -362,21 +362,70 @@ class Simulation:
             cfg["device"] = int(self.device)
         return cfg
 
-    def run(self, stop_condition, decomposition=None, np=1, skip=False, pop=False, write_config=None, **kwargs):
+    def run(self, stop_condition, decomposition=None, np=1, skip=False, pop=False, write_config=None, keep=False,
+            **kwargs):
         """Runs to the stop condition and reads the outputs back.  `decomposition`
         and `np` (MPI ranks of the reference) are accepted and ignored: one GPU
         runs the whole domain.  write_config: optional path to also write the
-        config JSON (what the reference's run_sim_json would read)."""
+        config JSON (what the reference's run_sim_json would read).
+
+        keep=True keeps the device simulation between runs: when the config is
+        unchanged and only two-medium-box densities or inhomogeneous-source
+        amplitude/phase datasets differ, the next run updates them in place
+        (ffip_set_density / ffip_set_source_data) instead of building the
+        simulation again, which is what a design loop repeats."""
         cfg = self.config(stop_condition)
         if write_config:
             with open(write_config, "w") as f:
                 json.dump(self.get_json(stop_condition, decomposition), f, indent=4)
         if not skip:
-            self.outputs = native.run_json(cfg, self.dump())
+            datasets = self.dump()
+            if keep:
+                self.outputs = self._run_kept(cfg, datasets)
+            else:
+                self.release()
+                self.outputs = native.run_json(cfg, datasets)
         for item in self.dft_fields:
             item.read(self.outputs)
         for item in self.geom_info_requests:
             item.read(self.outputs)
+
+    def _run_kept(self, cfg, datasets):
+        kept = getattr(self, "_kept", None)
+        if kept is not None and kept["cfg"] == cfg and kept["names"] == set(datasets):
+            density = {g.dataset_name for g in self.geometry if isinstance(g, Two_Medium_Box)}
+            source = set()
+            for src in self.sources:
+                if isinstance(src, Inhom_Source):
+                    source |= {src.amplitude_dataset_name, src.phase_dataset_name}
+            changed = [k for k, v in datasets.items() if not np.array_equal(kept["data"][k], v)]
+            if all(k in density or k in source for k in changed):
+                sim = kept["sim"]
+                for k in changed:
+                    if k in density:
+                        sim.set_density(k, datasets[k])
+                src_changed = {k: datasets[k] for k in changed if k in source}
+                if src_changed:
+                    sim.set_source_data(src_changed)
+                if not changed:
+                    sim.reset()
+                for k in changed:
+                    kept["data"][k] = np.array(datasets[k], copy=True)
+                sim.run(cfg["stop condition"])
+                return sim.outputs()
+        self.release()
+        sim = native.NativeSim(cfg, datasets)
+        self._kept = {"cfg": cfg, "names": set(datasets), "sim": sim,
+                      "data": {k: np.array(v, copy=True) for k, v in datasets.items()}}
+        sim.run(cfg["stop condition"])
+        return sim.outputs()
+
+    def release(self):
+        """Frees a simulation kept on the device by run(keep=True)."""
+        kept = getattr(self, "_kept", None)
+        if kept is not None:
+            kept["sim"].close()
+            self._kept = None
 
     def add_geometry(self, geom):
         self.geometry.insert(0, geom)
@@ -570,7 +619,11 @@ class Adjoint_Volume:
     """Design region and its sensitivity (simulation.py:759-915)."""
 
     def __init__(self, adjoint_simulation, forward_simulation, frequency=1.0, center=None, size=None, dim=None, density=None,
-                 medium1=None, medium2=None, epsilon_fun=None, epsilon_der=None, e_sus=(), norm=1):
+                 medium1=None, medium2=None, epsilon_fun=None, epsilon_der=None, e_sus=(), norm=1, geometry=None):
+        """geometry (rebuild-only): the design box of another Adjoint_Volume
+        of the same forward simulation (another frequency); it is then added
+        to the adjoint simulation only, so that the forward simulation holds
+        the design box once."""
         self.adjoint_simulation, self.forward_simulation = adjoint_simulation, forward_simulation
         self.frequency = float(frequency)
         self.center = (center if center is not None else Vector3()).copy()
@@ -585,14 +638,19 @@ class Adjoint_Volume:
             self.epsilon_fun = lambda rho: e1 * rho + (1 - rho) * e2
             self.epsilon_der = lambda rho: e1 - e2
             self.medium1, self.medium2 = deepcopy(medium1), deepcopy(medium2)
-            self.geom = Two_Medium_Box(size=self.size, center=self.center, dim=dim, density=density, medium1=medium1,
-                                       medium2=medium2, suffix="adjoint")
+            if geometry is None:
+                geometry = Two_Medium_Box(size=self.size, center=self.center, dim=dim, density=density, medium1=medium1,
+                                          medium2=medium2, suffix="adjoint")
         else:
             self.epsilon_der, self.epsilon_fun = epsilon_der, epsilon_fun
-            self.geom = General_Medium_Box(size=self.size, center=self.center, dim=dim, frequency=frequency, density=density,
-                                           epsilon_fun=epsilon_fun, e_sus=e_sus, suffix="adjoint")
+            if geometry is None:
+                geometry = General_Medium_Box(size=self.size, center=self.center, dim=dim, frequency=frequency,
+                                              density=density, epsilon_fun=epsilon_fun, e_sus=e_sus, suffix="adjoint")
+        shared = geometry is not None and any(g is geometry for g in forward_simulation.geometry)
+        self.geom = geometry
         adjoint_simulation.add_geometry(self.geom)
-        forward_simulation.add_geometry(self.geom)
+        if not shared:
+            forward_simulation.add_geometry(self.geom)
         comps = ["Ex", "Ey", "Ez"]
         self.forward_dfts = [forward_simulation.add_dft_fields(center=self.center, size=self.size, frequency=[frequency],
                                                                field_component=c) for c in comps]

@@ -94,3 +94,59 @@ def vacuum_point(n: int = 64, steps: int = 1000, seed: int = 7, precision: str =
         "stop condition": {"type": "time", "time": steps * 0.5},
         "precision": precision, "engine": engine,
     }
+
+
+def filtered_noise(shape, sigma, seed):
+    """Seeded uniform noise, Gaussian-filtered (sigma in nodes), min-max
+    rescaled to [0, 1]: the design-density recipe of the adjoint workload."""
+    from scipy.ndimage import gaussian_filter
+    rng = np.random.default_rng(seed)
+    r = gaussian_filter(rng.uniform(0, 1, size=shape), sigma=sigma, mode="reflect")
+    return (r - r.min()) / (r.max() - r.min())
+
+
+def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0.11), steps=5000, nprobe=4,
+                   seed=2024, precision="fp32", exact=True):
+    """The adjoint-gradient workload: a size[0] x size[0] x size[1] cell box
+    (dx = 1, Courant 0.5) with a `pml`-cell CPML; a design box of
+    design[0] x design[0] x design[1] cells centred at the origin whose
+    density (nodes at every cell corner: (design + 1) per axis) is seeded
+    filtered noise (sigma = 3 nodes), eps = 1 + 11 rho (medium1 eps 12,
+    medium2 vacuum); an Ex current sheet (Gaussian1, f = 0.1) half-way
+    between the lower CPML and the design box; objective F = sum over
+    `nprobe` seeded probe cells above the design box and over `freqs` of
+    |Ex|^2.  One forward run and one adjoint run per frequency, `steps` time
+    steps each.  Returns (AdjointProblem, rho0)."""
+    from . import design as D
+    from .geom import Medium, Vector3
+    from .simulation import Adjoint_Source, Adjoint_Volume, Simulation, field_match_objective, run_until_time
+    from .source import Gaussian1, Source
+    from .simulation import PML
+    n, nz = size
+    dn, dz = design
+    rng = np.random.default_rng(seed)
+    V = Vector3
+    pmls = [PML(thickness=pml, sigma_max=sigma_max(3, pml))]
+    z_lo = -nz / 2 + pml
+    z_sheet = float(np.round((z_lo + (-dz / 2)) / 2))
+    fwd_func = Gaussian1(0.1, cutoff=4, start_time=0.0)
+    fwd = Simulation(size=V(n, n, nz), resolution=1, pmls=pmls, precision=precision,
+                     sources=[Source(function=fwd_func, center=V(0, 0, z_sheet), size=V(n - 2 * pml, n - 2 * pml, 0),
+                                     field_component="Ex")])
+    probes = [(float(rng.integers(-dn // 3, dn // 3)) + 0.5, float(rng.integers(-dn // 3, dn // 3)),
+               float(rng.integers(dz // 2 + 8, nz / 2 - pml - 8))) for _ in range(nprobe)]
+    rho0 = filtered_noise((dz + 1, dn + 1, dn + 1), 3.0, seed)
+    dt = 0.5
+    t = np.arange(fwd_func.start_time, fwd_func.end_time, dt)
+    terms, geom = [], None
+    for f in freqs:
+        adj = Simulation(size=V(n, n, nz), resolution=1, pmls=pmls, precision=precision)
+        adj_func = Gaussian1(0.1, cutoff=4, start_time=0.5 / f)
+        srcs = [Adjoint_Source(adj, fwd, function=adj_func, frequency=f, center=V(*p), size=V(0, 0, 0), dim=V(1, 1, 1),
+                               udfs=[field_match_objective(np.zeros((1, 1, 1)), "Ex", weight=1.0)]) for p in probes]
+        norm = np.sum(np.exp(-2j * np.pi * f * t) * fwd_func(t))
+        vol = Adjoint_Volume(adj, fwd, frequency=f, center=V(0, 0, 0), size=V(dn, dn, dz), dim=V(dn + 1, dn + 1, dz + 1),
+                             density=rho0, medium1=Medium(epsilon=12), medium2=Medium(), norm=norm, geometry=geom)
+        geom = vol.geom
+        terms.append(D.AdjointTerm(adj, srcs, vol))
+    return D.AdjointProblem(fwd, terms, run_until_time(steps * dt), exact=exact), rho0
