@@ -13,6 +13,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libffip_gb300.so")
+CLI = os.path.join(LIBDIR, "run_sim_json")
 
 CUDA_SOURCES = ["kernels.cu", "adjoint.cu"]
 CXX_SOURCES = ["plan.cpp", "engine.cpp", "capi.cpp"]
@@ -53,6 +54,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs.append(o)
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", *inc,
                      "-I", "/usr/local/cuda/include", "-c", os.path.join(CSRC, s), "-o", o])
+    cli_obj = os.path.join(BUILD, "run_sim_json.cpp.o")
+    jobs.append(["g++", "-O2", "-std=c++17", "-Wall", *inc, "-c", os.path.join(CSRC, "run_sim_json.cpp"), "-o", cli_obj])
     procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)) for j in jobs]
     failed = []
     for j, p in procs:
@@ -70,6 +73,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError("native link failed:\n" + r.stdout.decode(errors="replace"))
     os.replace(tmp, LIB)
+    # the run_sim_json command-line driver, next to the library it loads
+    r = subprocess.run(["g++", "-o", CLI, cli_obj, "-L", LIBDIR, "-lffip_gb300", "-Wl,-rpath,$ORIGIN"],
+                       stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("run_sim_json link failed:\n" + r.stdout.decode(errors="replace"))
     return LIB
 
 

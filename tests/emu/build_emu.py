@@ -8,6 +8,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 CSRC = os.path.join(ROOT, "ffip_gb300", "csrc")
 OUT = os.path.join(ROOT, "tests", "_build", "libffip_emu.so")
+CLI = os.path.join(ROOT, "tests", "_build", "run_sim_json_emu")
 
 
 def build() -> str:
@@ -21,6 +22,19 @@ def build() -> str:
                            *srcs, "-o", tmp])
     os.replace(tmp, OUT)
     return OUT
+
+
+def build_cli() -> str:
+    """The run_sim_json driver linked with the emulation library."""
+    lib = build()
+    src = os.path.join(CSRC, "run_sim_json.cpp")
+    if os.path.exists(CLI) and os.path.getmtime(CLI) >= max(os.path.getmtime(src), os.path.getmtime(lib)):
+        return CLI
+    tmp = CLI + ".tmp%d" % os.getpid()
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", CSRC, "-I", os.path.join(ROOT, "include"), src,
+                           lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", tmp])
+    os.replace(tmp, CLI)
+    return CLI
 
 
 if __name__ == "__main__":
