@@ -181,7 +181,7 @@ def design_leg(iters, dev, world):
     first = time.perf_counter() - t0
     times, values = [], [F]
     for _ in range(iters):
-        step = 0.05 / max(np.abs(g).max(), 1e-30)
+        step = 0.002 / max(np.abs(g).max(), 1e-30)
         rho = np.clip(rho - step * g, 0.0, 1.0)
         barrier(world)
         t0 = time.perf_counter()
