@@ -18,6 +18,7 @@ struct DevSlots
     RowRange *rows{nullptr};
     T *g{nullptr}, *coef{nullptr}, *inv{nullptr};
     uint8_t *group{nullptr};
+    SlotRec<T> *rec{nullptr};
     T *A{nullptr}, *amp{nullptr}, *P{nullptr}, *P1{nullptr};
     int64_t n{0};
     int stride{0};
@@ -234,6 +235,16 @@ void Engine<T>::init_media()
         D.coef = upload(coef, kMedia);
         D.inv = upload(inv, kMedia);
         D.group = upload(grp, kMedia);
+        {
+            std::vector<SlotRec<T>> rec(D.n);
+            const auto &G = P_.groups[c / 3];
+            for (int64_t s = 0; s < D.n; ++s)
+            {
+                const int np = L.group[s] < (int)G.size() ? (int)G[L.group[s]].pool.size() : 0;
+                rec[s] = SlotRec<T>{coef[s], inv[s], g[s], (T)(grp[s] + 256 * np)};
+            }
+            D.rec = upload(rec, kMedia);
+        }
         if (D.poles)
         {
             if (c >= 3) D.A = dalloc<T>(D.n, kMedia);  // H sources are applied before the H update
@@ -468,6 +479,8 @@ void Engine<T>::bind_params()
             v.coef = D.coef;
             v.inv = D.inv;
             v.group = D.group;
+            v.rec = D.rec;
+            v.stride = D.stride;
             v.A = D.A;
             v.amp = D.amp;
             v.P = D.P;

@@ -357,7 +357,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int e
 // from the H ring planes rn (plane k) and rp (plane k-1).
 template <typename T>
 __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int eS, int rn, int rp, unsigned vb, bool pml,
-                                              bool slots, bool dft, int idx, const T (&pe)[3][2])
+                                              bool slots, bool dft, int idx, const T (&pe)[3][2], const int (&sl)[3])
 {
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX, TX = SH::TX;
@@ -395,13 +395,13 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
         const T term = plane_term(ec[a1], ec[a2], curl1[c], curl2[c], pe[c][0], pe[c][1], &ps1, &ps2);
         const T old = X.e_tile(eS, c)[offE];
         T v, vd;
-        if (!slots)
+        if (!slots || sl[c] < 0)
         {
             v = old + PE.coef_def * term;
             vd = PE.g_def * v;
         }
         else
-            v = material_at(PE, PE.slot[c], slot_of(PE.slot[c], PE.My, x, y, k, idx), old, term, &vd);
+            v = material_rec(PE, PE.slot[c], sl[c], old, term, &vd);
         if ((vb >> c) & 1u)
         {
             F.eout[c][idx] = v;
@@ -550,12 +550,20 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
     const int offN = (ty + 1) * (TX + 1) + tx + 1;  // own point in an H ring plane
     const T coefH = PH.coef_def, coefE = PE.coef_def, idh = PH.inv_dx, ide = PE.inv_dx;
 
+    // material slot indices of the E plane of the next iteration, loaded one
+    // iteration ahead (rows flagged in the plane word only)
+    int sl_next[3] = {-1, -1, -1};
     // iteration q: H at plane k = k0 - 1 + q (q <= NP - 2), E at plane k - 1 (q >= 2)
-    for (int q = 0; q < NP; ++q)
+    // running ring positions: E stages of planes q-1, q, q+1; H stage of
+    // plane q; H ring planes of H(k), H(k-1), H(k-2)
+    int eS = SE - 1, eA = 0, eB = 1 % SE, hA = 0, rn = 0, rp = 2, rpp = 1;
+    int idx = own0 + (X.k0 - 1) * sz;
+    for (int q = 0; q < NP; ++q, idx += sz)
     {
+        const int sl_e[3] = {sl_next[0], sl_next[1], sl_next[2]};
         const bool do_h = q <= NP - 2, do_e = q >= 2;
         const int k = X.k0 - 1 + q;
-        const int idx = own0 + k * sz, idx_e = idx - sz;
+        const int idx_e = idx - sz;
         const unsigned wh = info[q], we = q >= 1 ? info[q - 1] : 0u;
         const unsigned vbh = vxy & (wh >> kInfoZValidShift), vbe = vxy & (we >> kInfoZValidShift);
         const bool pml_h = pml_tables && (tile_pml || (wh & kInfoZPml));
@@ -589,6 +597,13 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
                 if (ve && ce[a1] != T(0)) pe[c][0] = PE.psi[c][0][idx_e];
                 if (ve && ce[a2] != T(0)) pe[c][1] = PE.psi[c][1][idx_e];
             }
+        }
+        sl_next[0] = sl_next[1] = sl_next[2] = -1;
+        if (q >= 1 && q <= NP - 2 && ((wh >> ty) & 1u))
+        {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+                if (PE.slot[c].map && ((vbh >> c) & 1u)) sl_next[c] = PE.slot[c].map[idx];
         }
         if (tid == 0)
         {
@@ -629,8 +644,6 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
                 h_issued = q + SHS;
             }
         }
-        const int eA = q % SE, eB = (q + 1) % SE, eS = (q + SE - 1) % SE, hA = q % SHS;
-        const int rn = q % 3, rp = (q + 2) % 3, rpp = (q + 1) % 3;  // ring planes of H(k), H(k-1), H(k-2)
         // 1. H(k) at the tile's own points, and the halo the E update of the
         //    next iteration reads: Hz, Hx on the low-y row, Hz, Hy on the
         //    low-x column (recomputed, not written)
@@ -714,8 +727,15 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
                 F.eout[2][idx_e] = ez;
             }
             else
-                e_own_general<T>(X, q - 1, eS, rp, rpp, vbe, pml_e, e_slots, dft_e, idx_e, pe);
+                e_own_general<T>(X, q - 1, eS, rp, rpp, vbe, pml_e, e_slots, dft_e, idx_e, pe, sl_e);
         }
+        eS = eA;
+        eA = eB;
+        eB = eB + 1 == SE ? 0 : eB + 1;
+        hA = hA + 1 == SHS ? 0 : hA + 1;
+        rpp = rp;
+        rp = rn;
+        rn = rn == 2 ? 0 : rn + 1;
     }
 }
 

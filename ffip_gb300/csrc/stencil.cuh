@@ -38,6 +38,14 @@ struct RowRange
     int lo, hi;  // x-index range of slot points in one (j,k) row; lo > hi if none
 };
 
+// one slot's constants in one aligned record: dt/g_inf, 1/g_inf, g_inf and
+// meta = group + 256 * (poles of the group), an exact small integer
+template <typename T>
+struct alignas(4 * sizeof(T)) SlotRec
+{
+    T coef, inv, g, meta;
+};
+
 template <typename T>
 struct SlotView
 {
@@ -45,10 +53,12 @@ struct SlotView
     const RowRange *rows;    // per (j,k) row
     const T *g, *coef, *inv; // g_inf, dt/g_inf, 1/g_inf per slot
     const uint8_t *group;    // pole group per slot
+    const SlotRec<T> *rec;   // the same per slot, packed
     T *A;                    // pending source sum per slot (H side, slots with poles; else null)
     const T *amp;            // [stride][n]
     T *P, *P1;               // [stride][n] polarisation P and its last increment J = P - P_prev
     int64_t n;
+    int stride;              // poles per slot in amp / P / P1
 };
 
 struct DftView
@@ -176,6 +186,26 @@ FFIP_HD int slot_of(const SlotView<T> &S, int My, int i, int j, int k, int64_t i
     return (i >= r.lo && i <= r.hi) ? S.map[idx] : -1;
 }
 
+// fused multiply-add with one rounding, the same on the host and the device
+FFIP_HD float fma_rn(float a, float b, float c) { return fmaf(a, b, c); }
+FFIP_HD double fma_rn(double a, double b, double c) { return fma(a, b, c); }
+
+// one pole of the (P, J) update: J_new = d1 P + d2 J + amp c3 E_old, with
+// its roundings fixed (explicit fma), so that every kernel that updates a
+// pole gives the same bits
+template <typename T>
+FFIP_HD T pole_increment(T d1, T d2, T c3, T P, T J, T amp, T old)
+{
+    return fma_rn(d1, P, fma_rn(d2, J, (amp * c3) * old));
+}
+
+// E_new = E_old + ((term + pend) dt - sum J_new) / g_inf, roundings fixed
+template <typename T>
+FFIP_HD T pole_field(T old, T term, T pend, T dt, T dsum, T inv)
+{
+    return fma_rn(fma_rn(term + pend, dt, -dsum), inv, old);
+}
+
 // Constitutive update of one point given its accdb increment `term`; `old`
 // is the point's field before this half step.  Returns the new field; *vd
 // receives the D/B value for D/B monitors.
@@ -193,7 +223,7 @@ FFIP_HD T material_at(const SideParams<T> &p, const SlotView<T> &S, int slot, T 
     const int np = p.grp_np[g];
     if (np == 0)
     {
-        v = old + S.coef[slot] * term;
+        v = fma_rn(S.coef[slot], term, old);
         *vd = S.g[slot] * v;
         return v;
     }
@@ -223,15 +253,64 @@ FFIP_HD T material_at(const SideParams<T> &p, const SlotView<T> &S, int slot, T 
         const T d1 = p.pool_c[3 * pool], d2 = p.pool_c[3 * pool + 1], c3 = p.pool_c[3 * pool + 2];
         const int64_t s = q * S.n + slot;
         const T Pq = S.P[s], Jq = S.P1[s];
-        const T Jn = d1 * Pq + d2 * Jq + S.amp[s] * c3 * old;
+        const T Jn = pole_increment(d1, d2, c3, Pq, Jq, S.amp[s], old);
         const T Pn = Pq + Jn;
         S.P1[s] = Jn;
         S.P[s] = Pn;
         dsum = dsum + Jn;
         psum = psum + Pn;
     }
-    v = old + ((term + pend) * p.dt - dsum) * S.inv[slot];
-    *vd = S.g[slot] * v + psum;  // D = g_inf E + sum P
+    v = pole_field(old, term, pend, p.dt, dsum, S.inv[slot]);
+    *vd = fma_rn(S.g[slot], v, psum);  // D = g_inf E + sum P
+    return v;
+}
+
+// material_at for a slot >= 0 of a side without pending sources (E side),
+// from the packed record; the loads of the first two poles do not wait for
+// the record, so one memory latency covers the point.  Same arithmetic and
+// evaluation order as material_at.
+template <typename T>
+FFIP_HD T material_rec(const SideParams<T> &p, const SlotView<T> &S, int slot, T old, T term, T *vd)
+{
+    T P0 = T(0), J0 = T(0), A0 = T(0), P1v = T(0), J1 = T(0), A1 = T(0);
+    if (S.stride >= 1)
+    {
+        P0 = S.P[slot];
+        J0 = S.P1[slot];
+        A0 = S.amp[slot];
+    }
+    if (S.stride >= 2)
+    {
+        P1v = S.P[S.n + slot];
+        J1 = S.P1[S.n + slot];
+        A1 = S.amp[S.n + slot];
+    }
+    const SlotRec<T> r = S.rec[slot];
+    const int meta = (int)r.meta, g = meta & 255, np = meta >> 8;
+    if (np == 0)
+    {
+        const T v = fma_rn(r.coef, term, old);
+        *vd = r.g * v;
+        return v;
+    }
+    T dsum = T(0), psum = T(0);
+    for (int q = 0; q < np; ++q)
+    {
+        const int pool = p.grp_pool[g * kMaxPolesDev + q];
+        const T d1 = p.pool_c[3 * pool], d2 = p.pool_c[3 * pool + 1], c3 = p.pool_c[3 * pool + 2];
+        const int64_t s = q * S.n + slot;
+        const T Pq = q == 0 ? P0 : q == 1 ? P1v : S.P[s];
+        const T Jq = q == 0 ? J0 : q == 1 ? J1 : S.P1[s];
+        const T Aq = q == 0 ? A0 : q == 1 ? A1 : S.amp[s];
+        const T Jn = pole_increment(d1, d2, c3, Pq, Jq, Aq, old);
+        const T Pn = Pq + Jn;
+        S.P1[s] = Jn;
+        S.P[s] = Pn;
+        dsum = dsum + Jn;
+        psum = psum + Pn;
+    }
+    const T v = pole_field(old, term, T(0), p.dt, dsum, r.inv);
+    *vd = fma_rn(r.g, v, psum);
     return v;
 }
 
