@@ -128,6 +128,8 @@ constexpr unsigned kInfoZValidShift = 8;   // bits 8..13: component c valid at t
 constexpr unsigned kInfoZPml = 1u << 14;   // CPML along z at this plane (either parity)
 constexpr unsigned kInfoDftE = 1u << 15;   // an E DFT unit meets this tile plane
 constexpr unsigned kInfoDftH = 1u << 16;   // an H DFT unit meets this tile plane
+constexpr unsigned kInfoFastH = 1u << 17;  // H of this tile plane takes the plain path
+constexpr unsigned kInfoFastE = 1u << 18;  // E of this tile plane takes the plain path (rows without slots)
                                            // bits 0..TY-1: tile row r has E material slots
 
 template <typename T>
@@ -544,6 +546,15 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
         inside = inside && PE.vlo[c][0] <= X.x0 - 1 && X.x0 + TX - 1 <= PE.vhi[c][0] && PE.vlo[c][1] <= X.y0 - 1 &&
                  X.y0 + TY - 1 <= PE.vhi[c][1] && PH.vlo[c][0] <= X.x0 - 1 && X.x0 + TX - 1 <= PH.vhi[c][0] &&
                  PH.vlo[c][1] <= X.y0 - 1 && X.y0 + TY - 1 <= PH.vhi[c][1];
+    // per plane: may each side take the plain path
+    for (int o = tid; o < LY::NZ; o += TX * TY)
+    {
+        const unsigned w = info[o];
+        const bool zpml = pml_tables && (tile_pml || (w & kInfoZPml));
+        if (inside && !zpml && !h_slots && !(w & kInfoDftH) && ((w >> (kInfoZValidShift + 3)) & 7u) == 7u) info[o] |= kInfoFastH;
+        if (inside && !zpml && !(w & kInfoDftE) && ((w >> kInfoZValidShift) & 7u) == 7u) info[o] |= kInfoFastE;
+    }
+    __syncthreads();
     const int sz = (int)PE.sz;
     const int own0 = x + y * (int)PE.sy;
     const int offE = (ty + 1) * BX + tx + XOFF;     // own point in an E or H box
@@ -565,13 +576,13 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
         const int k = X.k0 - 1 + q;
         const int idx_e = idx - sz;
         const unsigned wh = info[q], we = q >= 1 ? info[q - 1] : 0u;
-        const unsigned vbh = vxy & (wh >> kInfoZValidShift), vbe = vxy & (we >> kInfoZValidShift);
-        const bool pml_h = pml_tables && (tile_pml || (wh & kInfoZPml));
-        const bool pml_e = pml_tables && (tile_pml || (we & kInfoZPml));
-        const bool dft_h = wh & kInfoDftH, dft_e = we & kInfoDftE;
         const bool e_slots = (we >> ty) & 1u;
-        const bool fast_h = inside && ((wh >> (kInfoZValidShift + 3)) & 7u) == 7u && !pml_h && !h_slots && !dft_h;
-        const bool fast_e = inside && ((we >> kInfoZValidShift) & 7u) == 7u && !pml_e && !e_slots && !dft_e;
+        const bool fast_h = wh & kInfoFastH;
+        const bool fast_e = (we & kInfoFastE) && !e_slots;
+        const unsigned vbh = vxy & (wh >> kInfoZValidShift), vbe = vxy & (we >> kInfoZValidShift);
+        const bool pml_h = !fast_h && pml_tables && (tile_pml || (wh & kInfoZPml));
+        const bool pml_e = !fast_e && pml_tables && (tile_pml || (we & kInfoZPml));
+        const bool dft_h = wh & kInfoDftH, dft_e = we & kInfoDftE;
         // CPML psi of this iteration's own points, loaded before the TMA wait
         T ph[3][2] = {}, pe[3][2] = {};
         if (do_h && pml_h)
