@@ -162,6 +162,30 @@ def cpu_leg(cfg, steps, warmup, threads):
     return dt, setup
 
 
+def vacuum64_leg(dev, cpu):
+    """The plain fp64 vacuum box (64^3, 8-cell CPML, one Ez point current,
+    Ez DFT plane at 3 frequencies, 1000 steps): GPU fp64 device time, and the
+    oracle's restatement of the reference's loops on the host cores."""
+    from ffip_gb300 import native, workloads
+    cfg = workloads.vacuum_point(64, steps=1000, precision="fp64")
+    cfg["device"] = dev
+    s = native.NativeSim(cfg)
+    s.step(10)
+    ms = s.step_timed(1000)
+    cells = s.stats()["yee_cells"]
+    s.close()
+    out = {"workload": "vacuum 64^3, 8-cell CPML, Ez point source, 1000 steps, fp64", "gpu_ms_per_step": ms / 1000,
+           "gpu_gcell_updates_per_s": cells * 1000 / (ms * 1e-3) / 1e9}
+    if cpu:
+        threads = os.cpu_count() or 1
+        dt, _ = cpu_leg(workloads.vacuum_point(64, steps=1000, precision="fp64"), 200, 5, threads)
+        out["cpu_gcell_updates_per_s"] = cells * 200 / dt / 1e9
+        out["cpu_cores"] = threads
+        out["cpu_sample"] = "200 steps after 5 warm-up steps"
+        out["gpu_over_cpu"] = out["gpu_gcell_updates_per_s"] / out["cpu_gcell_updates_per_s"]
+    return out
+
+
 def design_leg(iters, dev, world):
     """Seconds per design iteration on the adjoint workload: 192 x 192 x 160
     cells, 16-cell CPML, 96 x 96 x 24 design box (97 x 97 x 25 density nodes,
@@ -319,6 +343,10 @@ def main():
                        "seconds": dt}
         out["e2e"] = e2e
         out["dft_rel_err_fp32_vs_fp64"] = dft_rel_err(full["fp32"], full["fp64"])
+
+    # ---- the plain fp64 vacuum box, GPU beside the CPU restatement
+    if not a.fp32_only:
+        out["vacuum64_fp64"] = vacuum64_leg(dev, rank == 0 and world == 1 and not a.no_cpu)
 
     # ---- design iterations of the adjoint workload (forward + one adjoint
     #      run per frequency + gradient), simulations kept between iterations

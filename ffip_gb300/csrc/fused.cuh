@@ -54,11 +54,15 @@ namespace ffipg
 {
 template <typename T>
 struct FusedShape;
-// SE / SH: TMA stages of the E / H plane rings; KCH: most z planes per CTA;
-// MINB: CTAs per SM the register budget is sized for (tuning builds may
-// override the defaults).  Tiles start at x0 = 1 + TX * bx, so the TMA box
-// starts at x0 - XOFF, a 16-byte boundary, and spans BX >= XOFF + TX + 1
-// elements (x0 - 1 .. x0 + TX are needed).
+// TY tile rows, RPT adjacent rows per thread (8 warps of 32 lanes, warp w
+// owns rows RPT w .. RPT w + RPT - 1); SE / SH: TMA stages of the E / H
+// plane rings; KCH: most z planes per CTA; MINB: CTAs per SM the register
+// budget is sized for (tuning builds may override the defaults).  Tiles start
+// at x0 = 1 + TX * bx, so the TMA box starts at x0 - XOFF, a 16-byte
+// boundary, and spans BX >= XOFF + TX + 1 elements (x0 - 1 .. x0 + TX).
+#ifndef FFIP_FUSED_F32_RPT
+#define FFIP_FUSED_F32_RPT 1
+#endif
 #ifndef FFIP_FUSED_F32_SE
 #define FFIP_FUSED_F32_SE 5
 #endif
@@ -67,6 +71,9 @@ struct FusedShape;
 #endif
 #ifndef FFIP_FUSED_F32_MINB
 #define FFIP_FUSED_F32_MINB 3
+#endif
+#ifndef FFIP_FUSED_F64_RPT
+#define FFIP_FUSED_F64_RPT 1
 #endif
 #ifndef FFIP_FUSED_F64_SE
 #define FFIP_FUSED_F64_SE 4
@@ -83,14 +90,14 @@ struct FusedShape;
 template <>
 struct FusedShape<float>
 {
-    static constexpr int TX = 32, TY = 8, XOFF = 5, BX = 40, SE = FFIP_FUSED_F32_SE, SH = FFIP_FUSED_F32_SH,
-                         KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F32_MINB;
+    static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 5, BX = 40, SE = FFIP_FUSED_F32_SE,
+                         SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F32_MINB;
 };
 template <>
 struct FusedShape<double>
 {
-    static constexpr int TX = 32, TY = 8, XOFF = 3, BX = 36, SE = FFIP_FUSED_F64_SE, SH = FFIP_FUSED_F64_SH,
-                         KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB;
+    static constexpr int TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 3, BX = 36, SE = FFIP_FUSED_F64_SE,
+                         SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB;
 };
 
 // CPML coefficients of one position along one axis: b, c, 1/k
@@ -118,19 +125,21 @@ struct FusedLayout
     static constexpr int INFO_OFF = PML_OFF + PML_BYTES;
     static constexpr int SMEM = INFO_OFF + NZ * 4;
     static_assert((SH::SE + SH::SH) * 8 <= 120, "mbarriers do not fit");
+    static_assert(SH::SE >= 4, "E planes q-1, q, q+1 are in use while one more loads");
     static_assert(SH::BX >= SH::XOFF + SH::TX + 1, "TMA box too narrow");
     static_assert((SH::XOFF - 1) * (int)sizeof(T) % 16 == 0, "TMA box start off a 16-byte boundary");
     static_assert(SH::BX * (int)sizeof(T) % 16 == 0, "TMA box width not a multiple of 16 bytes");
+    static_assert(SH::TX == 32 && SH::TY == 8 * SH::RPT && 2 * SH::TY <= 32, "8 warps of 32 lanes, halo in one warp");
 };
 
-// per-plane flag word (one per plane of the chunk, shared memory)
-constexpr unsigned kInfoZValidShift = 8;   // bits 8..13: component c valid at this z
-constexpr unsigned kInfoZPml = 1u << 14;   // CPML along z at this plane (either parity)
-constexpr unsigned kInfoDftE = 1u << 15;   // an E DFT unit meets this tile plane
-constexpr unsigned kInfoDftH = 1u << 16;   // an H DFT unit meets this tile plane
-constexpr unsigned kInfoFastH = 1u << 17;  // H of this tile plane takes the plain path
-constexpr unsigned kInfoFastE = 1u << 18;  // E of this tile plane takes the plain path (rows without slots)
-                                           // bits 0..TY-1: tile row r has E material slots
+// per-plane flag word (one per plane of the chunk, shared memory); bits
+// 0..TY-1: tile row r holds E material slots
+constexpr unsigned kInfoZValidShift = 16;  // bits 16..21: component c valid at this z
+constexpr unsigned kInfoZPml = 1u << 22;   // CPML along z at this plane (either parity)
+constexpr unsigned kInfoDftE = 1u << 23;   // an E DFT unit meets this tile plane
+constexpr unsigned kInfoDftH = 1u << 24;   // an H DFT unit meets this tile plane
+constexpr unsigned kInfoFastH = 1u << 25;  // H of this tile plane takes the plain path
+constexpr unsigned kInfoFastE = 1u << 26;  // E of this tile plane takes the plain path (rows without slots)
 
 template <typename T>
 struct FusedLaunch
@@ -206,10 +215,11 @@ struct FusedCtx
         return reinterpret_cast<const T *>(smem + LY::H_OFF + (st * 3 + c) * LY::H_TILE);
     }
     // new H, ring plane r (0..2), rows y0-1 .. y0+TY-1, columns x0-1 .. x0+TX-1
-    __device__ __forceinline__ T &hn_at(int r, int c, int row, int col) const
+    __device__ __forceinline__ T *hn_plane(int r, int c) const
     {
-        return reinterpret_cast<T *>(smem + LY::HN_OFF)[r * LY::HN_PLANE + (c * (SH::TY + 1) + row) * (SH::TX + 1) + col];
+        return reinterpret_cast<T *>(smem + LY::HN_OFF) + r * LY::HN_PLANE + c * (SH::TY + 1) * (SH::TX + 1);
     }
+    __device__ __forceinline__ T &hn_at(int r, int c, int row, int col) const { return hn_plane(r, c)[row * (SH::TX + 1) + col]; }
     // CPML table of axis a, parity q: entry o is position first_a + o, with
     // first = x0 - 1, y0 - 1, k0 - 1
     __device__ __forceinline__ PmlCoef<T> *tab(int a, int q) const
@@ -295,18 +305,20 @@ __device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &
     return pml_term(A1.c, A2.c, A1.b, A2.b, A1.ik, A2.ik, curl1, curl2, psi1, psi2, ps1, ps2);
 }
 
-// General H(k) at this thread's own tile point: validity bits, CPML from the
-// staged tables (psi values ph loaded by the caller), material slots, DFT.
+// General H(k) at this thread's own point of tile row `row`: validity bits,
+// CPML from the staged tables (psi values ph loaded by the caller), material
+// slots, DFT.
 template <typename T>
-__device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int eA, int eB, int hA, int slot_new, unsigned vb,
-                                              bool owned, bool pml, bool slots, bool dft, int idx, const T (&ph)[3][2])
+__device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int row, int eA, int eB, int hA, int slot_new,
+                                              unsigned vb, bool owned, bool pml, bool slots, bool dft, int idx,
+                                              const T (&ph)[3][2])
 {
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX;
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PH = F.h;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int offE = (ty + 1) * BX + tx + SH::XOFF;
+    const int tx = threadIdx.x;
+    const int offE = (row + 1) * BX + tx + SH::XOFF;
     const T idh = PH.inv_dx;
     const T *eA0 = X.e_tile(eA, 0), *eA1 = X.e_tile(eA, 1), *eA2 = X.e_tile(eA, 2);
     const T *eB0 = X.e_tile(eB, 0), *eB1 = X.e_tile(eB, 1);
@@ -324,10 +336,10 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int e
     if (pml)
     {
         hc[0] = X.tab(0, 1)[tx + 1];
-        hc[1] = X.tab(1, 1)[ty + 1];
+        hc[1] = X.tab(1, 1)[row + 1];
         hc[2] = X.tab(2, 1)[q];
     }
-    const int x = X.x0 + tx, y = X.y0 + ty, k = X.k0 - 1 + q;
+    const int x = X.x0 + tx, y = X.y0 + row, k = X.k0 - 1 + q;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
@@ -344,7 +356,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int e
         else
             v = material_at(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
         const bool val = (vb >> (3 + c)) & 1u;
-        X.hn_at(slot_new, c, ty + 1, tx + 1) = val ? v : T(0);
+        X.hn_at(slot_new, c, row + 1, tx + 1) = val ? v : T(0);
         if (owned && val)
         {
             F.hout[c][idx] = v;
@@ -355,29 +367,39 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int e
     }
 }
 
-// General E(k) at this thread's own tile point (E plane qe of the chunk),
-// from the H ring planes rn (plane k) and rp (plane k-1).
+// General E(k) at this thread's own point of tile row `row` (E plane qe of
+// the chunk), from the H ring planes rn (plane k) and rp (plane k-1); CPML
+// psi is read and written in place here; sl: material slot indices.
 template <typename T>
-__device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int eS, int rn, int rp, unsigned vb, bool pml,
-                                              bool slots, bool dft, int idx, const T (&pe)[3][2], const int (&sl)[3])
+__device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int eS, int rn, int rp, unsigned vb,
+                                              bool pml, bool slots, bool dft, int idx, const int (&sl)[3])
 {
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX, TX = SH::TX;
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PE = F.e;
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    const int offE = (ty + 1) * BX + tx + SH::XOFF;
-    const int offN = (ty + 1) * (TX + 1) + tx + 1;
+    const int tx = threadIdx.x;
+    const int offE = (row + 1) * BX + tx + SH::XOFF;
+    const int offN = (row + 1) * (TX + 1) + tx + 1;
     PmlCoef<T> ec[3] = {};  // per axis, parity 0
+    T pe[3][2] = {};
     if (pml)
     {
         ec[0] = X.tab(0, 0)[tx + 1];
-        ec[1] = X.tab(1, 0)[ty + 1];
+        ec[1] = X.tab(1, 0)[row + 1];
         ec[2] = X.tab(2, 0)[qe];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+        {
+            const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+            const bool ve = (vb >> c) & 1u;
+            if (ve && ec[a1].c != T(0)) pe[c][0] = PE.psi[c][0][idx];
+            if (ve && ec[a2].c != T(0)) pe[c][1] = PE.psi[c][1][idx];
+        }
     }
     const T ide = PE.inv_dx;
-    const T *n0 = &X.hn_at(rn, 0, 0, 0), *n1 = &X.hn_at(rn, 1, 0, 0), *n2 = &X.hn_at(rn, 2, 0, 0);
-    const T *p0 = &X.hn_at(rp, 0, 0, 0), *p1 = &X.hn_at(rp, 1, 0, 0);
+    const T *n0 = X.hn_plane(rn, 0), *n1 = X.hn_plane(rn, 1), *n2 = X.hn_plane(rn, 2);
+    const T *p0 = X.hn_plane(rp, 0), *p1 = X.hn_plane(rp, 1);
     const T hzr = n2[offN], hzy = n2[offN - (TX + 1)], hzx = n2[offN - 1];
     const T hyr = n1[offN], hyp = p1[offN], hyx = n1[offN - 1];
     const T hxr = n0[offN], hxp = p0[offN], hxy = n0[offN - (TX + 1)];
@@ -388,7 +410,7 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     curl2[1] = (hzr - hzx) * ide;
     curl1[2] = (hyr - hyx) * ide;  // Ez: dHy/dx - dHx/dy
     curl2[2] = (hxr - hxy) * ide;
-    const int x = X.x0 + tx, y = X.y0 + ty, k = X.k0 - 1 + qe;
+    const int x = X.x0 + tx, y = X.y0 + row, k = X.k0 - 1 + qe;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
@@ -419,12 +441,14 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
 {
     using SH = FusedShape<T>;
     using LY = FusedLayout<T>;
-    constexpr int TX = SH::TX, TY = SH::TY, XOFF = SH::XOFF, SE = SH::SE, SHS = SH::SH, BX = SH::BX;
+    constexpr int TX = SH::TX, TY = SH::TY, RPT = SH::RPT, XOFF = SH::XOFF, SE = SH::SE, SHS = SH::SH, BX = SH::BX;
+    constexpr int NTH = 256;
     extern __shared__ __align__(128) unsigned char smem[];
     const FusedParams<T> &F = L.fp;
     const SideParams<T> &PE = F.e;
     const SideParams<T> &PH = F.h;
-    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+    const int lane = threadIdx.x, wid = threadIdx.y, tid = wid * 32 + lane;
+    const int r0 = wid * RPT;  // first tile row of this thread
     FusedCtx<T> X;
     X.smem = smem;
     X.L = &L;
@@ -476,7 +500,7 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
             const int n = a == 0 ? LY::NX : a == 1 ? LY::NY : LY::NZ;
             const int first = a == 0 ? X.x0 - 1 : a == 1 ? X.y0 - 1 : X.k0 - 1;
             const int len = a == 0 ? PE.Mx : a == 1 ? PE.My : PE.Mz;
-            for (int t = tid; t < 2 * n; t += TX * TY)
+            for (int t = tid; t < 2 * n; t += NTH)
             {
                 const int q = t / n, o = t % n, pos = first + o;
                 const bool in = pos >= 0 && pos < len;
@@ -493,7 +517,7 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
     // per plane of the chunk: flag word (z validity, z CPML, DFT units
     // meeting the tile plane, tile rows with E material slots)
     unsigned *info = reinterpret_cast<unsigned *>(smem + LY::INFO_OFF);
-    for (int o = tid; o < LY::NZ; o += TX * TY)
+    for (int o = tid; o < LY::NZ; o += NTH)
     {
         const int k = X.k0 - 1 + o;
         unsigned w = 0;
@@ -520,7 +544,7 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
         info[o] = w;
     }
     __syncthreads();
-    for (int t = tid; t < LY::NZ * TY * 3; t += TX * TY)
+    for (int t = tid; t < LY::NZ * TY * 3; t += NTH)
     {
         const int c = t % 3, r = (t / 3) % TY, o = t / (3 * TY);
         const int kk = X.k0 - 1 + o, yy = X.y0 + r;
@@ -531,15 +555,21 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
     tile_pml = __syncthreads_or(tile_pml);
     const bool h_slots = PH.slot[0].map || PH.slot[1].map || PH.slot[2].map;
 
-    const int x = X.x0 + tx, y = X.y0 + ty;
-    // components with a grid point at (x, y) that this pass owns
-    unsigned vxy = 0;
-    if (x < L.xlim && y < L.ylim)
-        for (int c = 0; c < 3; ++c)
-        {
-            if (x >= PE.vlo[c][0] && x <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1]) vxy |= 1u << c;
-            if (x >= PH.vlo[c][0] && x <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1]) vxy |= 1u << (3 + c);
-        }
+    const int x = X.x0 + lane;
+    // per own row: components with a grid point at (x, y) that this pass owns
+    unsigned vxy[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r)
+    {
+        const int y = X.y0 + r0 + r;
+        vxy[r] = 0;
+        if (x < L.xlim && y < L.ylim)
+            for (int c = 0; c < 3; ++c)
+            {
+                if (x >= PE.vlo[c][0] && x <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1]) vxy[r] |= 1u << c;
+                if (x >= PH.vlo[c][0] && x <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1]) vxy[r] |= 1u << (3 + c);
+            }
+    }
     // every own and halo point of the tile valid in x and y for all six components
     bool inside = X.x0 + TX <= L.xlim && X.y0 + TY <= L.ylim;
     for (int c = 0; c < 3; ++c)
@@ -547,7 +577,7 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
                  X.y0 + TY - 1 <= PE.vhi[c][1] && PH.vlo[c][0] <= X.x0 - 1 && X.x0 + TX - 1 <= PH.vhi[c][0] &&
                  PH.vlo[c][1] <= X.y0 - 1 && X.y0 + TY - 1 <= PH.vhi[c][1];
     // per plane: may each side take the plain path
-    for (int o = tid; o < LY::NZ; o += TX * TY)
+    for (int o = tid; o < LY::NZ; o += NTH)
     {
         const unsigned w = info[o];
         const bool zpml = pml_tables && (tile_pml || (w & kInfoZPml));
@@ -555,66 +585,74 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
         if (inside && !zpml && !(w & kInfoDftE) && ((w >> kInfoZValidShift) & 7u) == 7u) info[o] |= kInfoFastE;
     }
     __syncthreads();
-    const int sz = (int)PE.sz;
-    const int own0 = x + y * (int)PE.sy;
-    const int offE = (ty + 1) * BX + tx + XOFF;     // own point in an E or H box
-    const int offN = (ty + 1) * (TX + 1) + tx + 1;  // own point in an H ring plane
+    const int sz = (int)PE.sz, sy = (int)PE.sy;
+    const int own0 = x + (X.y0 + r0) * sy;  // own point of row r0 at z = 0
+    const int offE = (r0 + 1) * BX + lane + XOFF;    // own point of row r0 in an E or H box
+    const int offN = (r0 + 1) * (TX + 1) + lane + 1;  // own point of row r0 in an H ring plane
     const T coefH = PH.coef_def, coefE = PE.coef_def, idh = PH.inv_dx, ide = PE.inv_dx;
+    const unsigned rowmask = ((1u << RPT) - 1u) << r0;
 
     // material slot indices of the E plane of the next iteration, loaded one
     // iteration ahead (rows flagged in the plane word only)
-    int sl_next[3] = {-1, -1, -1};
-    // iteration q: H at plane k = k0 - 1 + q (q <= NP - 2), E at plane k - 1 (q >= 2)
+    int sl_next[RPT][3];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r) sl_next[r][0] = sl_next[r][1] = sl_next[r][2] = -1;
     // running ring positions: E stages of planes q-1, q, q+1; H stage of
     // plane q; H ring planes of H(k), H(k-1), H(k-2)
     int eS = SE - 1, eA = 0, eB = 1 % SE, hA = 0, rn = 0, rp = 2, rpp = 1;
     int idx = own0 + (X.k0 - 1) * sz;
+    // iteration q: H at plane k = k0 - 1 + q (q <= NP - 2), E at plane k - 1 (q >= 2)
     for (int q = 0; q < NP; ++q, idx += sz)
     {
-        const int sl_e[3] = {sl_next[0], sl_next[1], sl_next[2]};
+        int sl_e[RPT][3];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r)
+            for (int c = 0; c < 3; ++c) sl_e[r][c] = sl_next[r][c];
         const bool do_h = q <= NP - 2, do_e = q >= 2;
         const int k = X.k0 - 1 + q;
         const int idx_e = idx - sz;
         const unsigned wh = info[q], we = q >= 1 ? info[q - 1] : 0u;
-        const bool e_slots = (we >> ty) & 1u;
+        const bool e_slots = (we & rowmask) != 0u;
         const bool fast_h = wh & kInfoFastH;
         const bool fast_e = (we & kInfoFastE) && !e_slots;
-        const unsigned vbh = vxy & (wh >> kInfoZValidShift), vbe = vxy & (we >> kInfoZValidShift);
         const bool pml_h = !fast_h && pml_tables && (tile_pml || (wh & kInfoZPml));
         const bool pml_e = !fast_e && pml_tables && (tile_pml || (we & kInfoZPml));
         const bool dft_h = wh & kInfoDftH, dft_e = we & kInfoDftE;
-        // CPML psi of this iteration's own points, loaded before the TMA wait
-        T ph[3][2] = {}, pe[3][2] = {};
+        // CPML psi of this iteration's own H points, loaded before the TMA wait
+        T ph[RPT][3][2];
+#pragma unroll
+        for (int r = 0; r < RPT; ++r)
+            for (int c = 0; c < 3; ++c) ph[r][c][0] = ph[r][c][1] = T(0);
         if (do_h && pml_h)
         {
-            const T ch[3] = {X.tab(0, 1)[tx + 1].c, X.tab(1, 1)[ty + 1].c, X.tab(2, 1)[q].c};  // H side (parity 1)
+            const T cx = X.tab(0, 1)[lane + 1].c, cz = X.tab(2, 1)[q].c;  // H side (parity 1)
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
+            for (int r = 0; r < RPT; ++r)
             {
-                const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-                const bool vh = (vbh >> (3 + c)) & 1u;
-                if (vh && ch[a1] != T(0)) ph[c][0] = F.psih_in[c][0][idx];
-                if (vh && ch[a2] != T(0)) ph[c][1] = F.psih_in[c][1][idx];
+                const T ch[3] = {cx, X.tab(1, 1)[r0 + r + 1].c, cz};
+                const unsigned vb = vxy[r] & (wh >> kInfoZValidShift);
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                {
+                    const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+                    const bool vh = (vb >> (3 + c)) & 1u;
+                    if (vh && ch[a1] != T(0)) ph[r][c][0] = F.psih_in[c][0][idx + r * sy];
+                    if (vh && ch[a2] != T(0)) ph[r][c][1] = F.psih_in[c][1][idx + r * sy];
+                }
             }
         }
-        if (do_e && pml_e)
-        {
-            const T ce[3] = {X.tab(0, 0)[tx + 1].c, X.tab(1, 0)[ty + 1].c, X.tab(2, 0)[q - 1].c};  // E side (parity 0)
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < RPT; ++r) sl_next[r][0] = sl_next[r][1] = sl_next[r][2] = -1;
+        if (q >= 1 && q <= NP - 2 && (wh & rowmask))
+        {
+#pragma unroll
+            for (int r = 0; r < RPT; ++r)
             {
-                const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-                const bool ve = (vbe >> c) & 1u;
-                if (ve && ce[a1] != T(0)) pe[c][0] = PE.psi[c][0][idx_e];
-                if (ve && ce[a2] != T(0)) pe[c][1] = PE.psi[c][1][idx_e];
-            }
-        }
-        sl_next[0] = sl_next[1] = sl_next[2] = -1;
-        if (q >= 1 && q <= NP - 2 && ((wh >> ty) & 1u))
-        {
+                const unsigned vb = vxy[r] & (wh >> kInfoZValidShift);
 #pragma unroll
-            for (int c = 0; c < 3; ++c)
-                if (PE.slot[c].map && ((vbh >> c) & 1u)) sl_next[c] = PE.slot[c].map[idx];
+                for (int c = 0; c < 3; ++c)
+                    if (PE.slot[c].map && ((vb >> c) & 1u)) sl_next[r][c] = PE.slot[c].map[idx + r * sy];
+            }
         }
         if (tid == 0)
         {
@@ -656,61 +694,83 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
             }
         }
         // 1. H(k) at the tile's own points, and the halo the E update of the
-        //    next iteration reads: Hz, Hx on the low-y row, Hz, Hy on the
-        //    low-x column (recomputed, not written)
+        //    next iteration reads: Hz, Hx on the low-y row (warps 7, 6), Hz,
+        //    Hy on the low-x column (warp 5) (recomputed, not written)
         if (do_h)
         {
             if (fast_h)
             {
-                const T *eA0 = X.e_tile(eA, 0), *eA1 = X.e_tile(eA, 1), *eA2 = X.e_tile(eA, 2);
-                const T *eB0 = X.e_tile(eB, 0), *eB1 = X.e_tile(eB, 1);
-                const T *hA0 = X.h_tile(hA, 0), *hA1 = X.h_tile(hA, 1), *hA2 = X.h_tile(hA, 2);
-                const T exa = eA0[offE], exy = eA0[offE + BX], exb = eB0[offE];
-                const T eya = eA1[offE], eyx = eA1[offE + 1], eyb = eB1[offE];
-                const T eza = eA2[offE], ezy = eA2[offE + BX], ezx = eA2[offE + 1];
-                const T hx = hA0[offE] + coefH * ((eza - ezy) * idh - (eya - eyb) * idh);
-                const T hy = hA1[offE] + coefH * ((exa - exb) * idh - (eza - ezx) * idh);
-                const T hz = hA2[offE] + coefH * ((eya - eyx) * idh - (exa - exy) * idh);
-                X.hn_at(rn, 0, ty + 1, tx + 1) = hx;
-                X.hn_at(rn, 1, ty + 1, tx + 1) = hy;
-                X.hn_at(rn, 2, ty + 1, tx + 1) = hz;
+                const T *eA0 = X.e_tile(eA, 0) + offE, *eA1 = X.e_tile(eA, 1) + offE, *eA2 = X.e_tile(eA, 2) + offE;
+                const T *eB0 = X.e_tile(eB, 0) + offE, *eB1 = X.e_tile(eB, 1) + offE;
+                const T *hA0 = X.h_tile(hA, 0) + offE, *hA1 = X.h_tile(hA, 1) + offE, *hA2 = X.h_tile(hA, 2) + offE;
+                T exa[RPT + 1], eza[RPT + 1];
+#pragma unroll
+                for (int r = 0; r <= RPT; ++r)
+                {
+                    exa[r] = eA0[r * BX];
+                    eza[r] = eA2[r * BX];
+                }
+                T hn0[RPT], hn1[RPT], hn2[RPT];
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                {
+                    const T eya = eA1[r * BX], eyx = eA1[r * BX + 1], eyb = eB1[r * BX];
+                    const T exb = eB0[r * BX], ezx = eA2[r * BX + 1];
+                    hn0[r] = hA0[r * BX] + coefH * ((eza[r] - eza[r + 1]) * idh - (eya - eyb) * idh);
+                    hn1[r] = hA1[r * BX] + coefH * ((exa[r] - exb) * idh - (eza[r] - ezx) * idh);
+                    hn2[r] = hA2[r * BX] + coefH * ((eya - eyx) * idh - (exa[r] - exa[r + 1]) * idh);
+                }
+                T *n0 = X.hn_plane(rn, 0) + offN, *n1 = X.hn_plane(rn, 1) + offN, *n2 = X.hn_plane(rn, 2) + offN;
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                {
+                    n0[r * (TX + 1)] = hn0[r];
+                    n1[r * (TX + 1)] = hn1[r];
+                    n2[r * (TX + 1)] = hn2[r];
+                }
                 if (q >= 1)
                 {
-                    F.hout[0][idx] = hx;
-                    F.hout[1][idx] = hy;
-                    F.hout[2][idx] = hz;
+#pragma unroll
+                    for (int r = 0; r < RPT; ++r)
+                    {
+                        F.hout[0][idx + r * sy] = hn0[r];
+                        F.hout[1][idx + r * sy] = hn1[r];
+                        F.hout[2][idx + r * sy] = hn2[r];
+                    }
                 }
-                if (tid < 2 * TX + 2 * TY)
+                const T *gA0 = X.e_tile(eA, 0), *gA1 = X.e_tile(eA, 1), *gA2 = X.e_tile(eA, 2), *gB0 = X.e_tile(eB, 0),
+                        *gB1 = X.e_tile(eB, 1);
+                if (wid >= 6)
                 {
-                    if (tid < 2 * TX)
-                    {
-                        const int u = tid < TX ? tid : tid - TX, o = u + XOFF;  // row y0 - 1 of the boxes
-                        if (tid < TX)
-                            X.hn_at(rn, 2, 0, u + 1) = hA2[o] + coefH * ((eA1[o] - eA1[o + 1]) * idh - (eA0[o] - eA0[o + BX]) * idh);
-                        else
-                            X.hn_at(rn, 0, 0, u + 1) = hA0[o] + coefH * ((eA2[o] - eA2[o + BX]) * idh - (eA1[o] - eB1[o]) * idh);
-                    }
+                    const int o = lane + XOFF;  // row y0 - 1 of the boxes
+                    if (wid == 7)
+                        X.hn_at(rn, 2, 0, lane + 1) = X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
                     else
-                    {
-                        const int v = tid < 2 * TX + TY ? tid - 2 * TX : tid - 2 * TX - TY;
-                        const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
-                        if (tid < 2 * TX + TY)
-                            X.hn_at(rn, 2, v + 1, 0) = hA2[o] + coefH * ((eA1[o] - eA1[o + 1]) * idh - (eA0[o] - eA0[o + BX]) * idh);
-                        else
-                            X.hn_at(rn, 1, v + 1, 0) = hA1[o] + coefH * ((eA0[o] - eB0[o]) * idh - (eA2[o] - eA2[o + 1]) * idh);
-                    }
+                        X.hn_at(rn, 0, 0, lane + 1) = X.h_tile(hA, 0)[o] + coefH * ((gA2[o] - gA2[o + BX]) * idh - (gA1[o] - gB1[o]) * idh);
+                }
+                else if (wid == 5 && lane < 2 * TY)
+                {
+                    const int v = lane < TY ? lane : lane - TY;
+                    const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
+                    if (lane < TY)
+                        X.hn_at(rn, 2, v + 1, 0) = X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
+                    else
+                        X.hn_at(rn, 1, v + 1, 0) = X.h_tile(hA, 1)[o] + coefH * ((gA0[o] - gB0[o]) * idh - (gA2[o] - gA2[o + 1]) * idh);
                 }
             }
             else
             {
-                h_own_general<T>(X, q, eA, eB, hA, rn, vbh, q >= 1, pml_h, h_slots, dft_h, idx, ph);
-                if (tid < 2 * TX + 2 * TY)
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                    h_own_general<T>(X, q, r0 + r, eA, eB, hA, rn, vxy[r] & (wh >> kInfoZValidShift), q >= 1, pml_h, h_slots,
+                                     dft_h, idx + r * sy, ph[r]);
+                if (wid >= 6 || (wid == 5 && lane < 2 * TY))
                 {
                     int hx, hy, comp, row, col;
-                    if (tid < TX) { hx = X.x0 + tid; hy = X.y0 - 1; comp = 2; row = 0; col = tid + 1; }
-                    else if (tid < 2 * TX) { hx = X.x0 + tid - TX; hy = X.y0 - 1; comp = 0; row = 0; col = tid - TX + 1; }
-                    else if (tid < 2 * TX + TY) { hx = X.x0 - 1; hy = X.y0 + tid - 2 * TX; comp = 2; row = tid - 2 * TX + 1; col = 0; }
-                    else { hx = X.x0 - 1; hy = X.y0 + tid - 2 * TX - TY; comp = 1; row = tid - 2 * TX - TY + 1; col = 0; }
+                    if (wid == 7) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 2; row = 0; col = lane + 1; }
+                    else if (wid == 6) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 0; row = 0; col = lane + 1; }
+                    else if (lane < TY) { hx = X.x0 - 1; hy = X.y0 + lane; comp = 2; row = lane + 1; col = 0; }
+                    else { hx = X.x0 - 1; hy = X.y0 + lane - TY; comp = 1; row = lane - TY + 1; col = 0; }
                     T v;
                     if (comp == 0) v = fused_h_halo<T, 3>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
                     else if (comp == 1) v = fused_h_halo<T, 4>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
@@ -724,21 +784,37 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
         {
             if (fast_e)
             {
-                const T *eS0 = X.e_tile(eS, 0), *eS1 = X.e_tile(eS, 1), *eS2 = X.e_tile(eS, 2);
-                const T *n0 = &X.hn_at(rp, 0, 0, 0), *n1 = &X.hn_at(rp, 1, 0, 0), *n2 = &X.hn_at(rp, 2, 0, 0);
-                const T *p0 = &X.hn_at(rpp, 0, 0, 0), *p1 = &X.hn_at(rpp, 1, 0, 0);
-                const T hzr = n2[offN], hzy = n2[offN - (TX + 1)], hzx = n2[offN - 1];
-                const T hyr = n1[offN], hyp = p1[offN], hyx = n1[offN - 1];
-                const T hxr = n0[offN], hxp = p0[offN], hxy = n0[offN - (TX + 1)];
-                const T ex = eS0[offE] + coefE * ((hzr - hzy) * ide - (hyr - hyp) * ide);
-                const T ey = eS1[offE] + coefE * ((hxr - hxp) * ide - (hzr - hzx) * ide);
-                const T ez = eS2[offE] + coefE * ((hyr - hyx) * ide - (hxr - hxy) * ide);
-                F.eout[0][idx_e] = ex;
-                F.eout[1][idx_e] = ey;
-                F.eout[2][idx_e] = ez;
+                const T *eS0 = X.e_tile(eS, 0) + offE, *eS1 = X.e_tile(eS, 1) + offE, *eS2 = X.e_tile(eS, 2) + offE;
+                const T *n0 = X.hn_plane(rp, 0) + offN, *n1 = X.hn_plane(rp, 1) + offN, *n2 = X.hn_plane(rp, 2) + offN;
+                const T *p0 = X.hn_plane(rpp, 0) + offN, *p1 = X.hn_plane(rpp, 1) + offN;
+                constexpr int RS = TX + 1;  // ring row stride
+                T hz[RPT + 1], hx[RPT + 1];  // rows r0-1 .. r0+RPT-1
+#pragma unroll
+                for (int r = 0; r <= RPT; ++r)
+                {
+                    hz[r] = n2[(r - 1) * RS];
+                    hx[r] = n0[(r - 1) * RS];
+                }
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                {
+                    const T hzx = n2[r * RS - 1], hyr = n1[r * RS], hyp = p1[r * RS], hyx = n1[r * RS - 1];
+                    const T hxp = p0[r * RS];
+                    const T ex = eS0[r * BX] + coefE * ((hz[r + 1] - hz[r]) * ide - (hyr - hyp) * ide);
+                    const T ey = eS1[r * BX] + coefE * ((hx[r + 1] - hxp) * ide - (hz[r + 1] - hzx) * ide);
+                    const T ez = eS2[r * BX] + coefE * ((hyr - hyx) * ide - (hx[r + 1] - hx[r]) * ide);
+                    F.eout[0][idx_e + r * sy] = ex;
+                    F.eout[1][idx_e + r * sy] = ey;
+                    F.eout[2][idx_e + r * sy] = ez;
+                }
             }
             else
-                e_own_general<T>(X, q - 1, eS, rp, rpp, vbe, pml_e, e_slots, dft_e, idx_e, pe, sl_e);
+            {
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                    e_own_general<T>(X, q - 1, r0 + r, eS, rp, rpp, vxy[r] & (we >> kInfoZValidShift), pml_e, e_slots, dft_e,
+                                     idx_e + r * sy, sl_e[r]);
+            }
         }
         eS = eA;
         eA = eB;

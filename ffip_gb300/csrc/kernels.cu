@@ -249,7 +249,7 @@ public:
         L.yend = yend;
         L.kbeg = kbeg;
         L.kend = std::max(kend, kbeg + 1);
-        dim3 block(SH::TX, SH::TY);
+        dim3 block(32, 8);  // 8 warps; each thread owns SH::RPT rows of the tile
         dim3 grid(std::max(nbx, 1), std::max(nby, 1), (L.kend - L.kbeg + SH::KCH - 1) / SH::KCH);
         k_fused<T><<<grid, block, LY::SMEM, stream_>>>(L);
         check(cudaGetLastError(), "k_fused launch");
