@@ -87,17 +87,25 @@ struct FusedShape;
 #ifndef FFIP_FUSED_KCH
 #define FFIP_FUSED_KCH 16
 #endif
+#ifndef FFIP_FUSED_F32_MINB_INTERIOR
+#define FFIP_FUSED_F32_MINB_INTERIOR 3
+#endif
+#ifndef FFIP_FUSED_F64_MINB_INTERIOR
+#define FFIP_FUSED_F64_MINB_INTERIOR 2
+#endif
 template <>
 struct FusedShape<float>
 {
     static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 5, BX = 40, SE = FFIP_FUSED_F32_SE,
-                         SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F32_MINB;
+                         SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F32_MINB,
+                         MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR;
 };
 template <>
 struct FusedShape<double>
 {
     static constexpr int TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 3, BX = 36, SE = FFIP_FUSED_F64_SE,
-                         SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB;
+                         SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB,
+                         MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR;
 };
 
 // CPML coefficients of one position along one axis: b, c, 1/k
@@ -150,7 +158,8 @@ struct FusedLaunch
     int *err;             // set to 1 when a wait times out
     int xlim, ylim;       // this pass updates 1 <= x < xlim, 1 <= y < ylim; k_face the rest
     int xend, yend;       // valid extents (max over components of vhi + 1)
-    int kbeg, kend;       // valid z range split over the grid's z blocks
+    int kbeg, kend;       // valid z range
+    const int4 *jobs;     // per CTA: x0, y0, k0, k1 (tile origin and owned z planes)
 };
 
 constexpr int kFusedWaitLimit = 1 << 22;
@@ -436,8 +445,11 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid_constant__ FusedLaunch<T> L)
+// PML = false: the instance for jobs whose tiles, halos and planes hold no
+// CPML point (the host sorts the jobs); it carries no CPML code.
+template <typename T, bool PML>
+__global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>::MINB_INTERIOR)
+    k_fused(const __grid_constant__ FusedLaunch<T> L)
 {
     using SH = FusedShape<T>;
     using LY = FusedLayout<T>;
@@ -452,10 +464,11 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
     FusedCtx<T> X;
     X.smem = smem;
     X.L = &L;
-    X.x0 = 1 + blockIdx.x * TX;
-    X.y0 = 1 + blockIdx.y * TY;
-    X.k0 = L.kbeg + (int)((int64_t)(L.kend - L.kbeg) * blockIdx.z / gridDim.z);
-    const int k1 = L.kbeg + (int)((int64_t)(L.kend - L.kbeg) * (blockIdx.z + 1) / gridDim.z);
+    const int4 job = L.jobs[blockIdx.x];
+    X.x0 = job.x;
+    X.y0 = job.y;
+    X.k0 = job.z;
+    const int k1 = job.w;
     const int NP = k1 - X.k0 + 2;  // planes k0-1 .. k1 (plane p is z = k0 - 1 + p)
     uint64_t *ebar = reinterpret_cast<uint64_t *>(smem);
     uint64_t *hbar = ebar + SE;
@@ -491,7 +504,7 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
     }
 
     // stage the CPML tables of this tile / chunk while the first planes load
-    const bool pml_tables = PE.pc[0][0] != nullptr;
+    const bool pml_tables = PML && PE.pc[0][0] != nullptr;
     bool tile_pml = false;
     if (pml_tables)
     {
@@ -499,7 +512,7 @@ __global__ void __launch_bounds__(256, FusedShape<T>::MINB) k_fused(const __grid
         {
             const int n = a == 0 ? LY::NX : a == 1 ? LY::NY : LY::NZ;
             const int first = a == 0 ? X.x0 - 1 : a == 1 ? X.y0 - 1 : X.k0 - 1;
-            const int len = a == 0 ? PE.Mx : a == 1 ? PE.My : PE.Mz;
+            const int len = a == 0 ? L.xend : a == 1 ? PE.My : PE.Mz;  // table lengths (x: valid extent, not the padded row)
             for (int t = tid; t < 2 * n; t += NTH)
             {
                 const int q = t / n, o = t % n, pos = first + o;

@@ -13,6 +13,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <vector>
 #include <map>
 #include <stdexcept>
 #include <string>
@@ -141,6 +143,10 @@ public:
         cudaSetDevice(dev_);
         cudaStreamSynchronize(stream_);
         if (err_) cudaFree(err_);
+        for (auto &kv : jobs_) cudaFree(kv.second.dev);
+        if (side_) cudaStreamDestroy(side_);
+        if (fork_) cudaEventDestroy(fork_);
+        if (join_) cudaEventDestroy(join_);
         cudaStreamDestroy(stream_);
     }
     // every entry re-selects the handle's device: calls may come from any thread
@@ -210,10 +216,13 @@ public:
         static bool attr_set = false;
         if (!attr_set)
         {
-            check(cudaFuncSetAttribute(k_fused<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM), "cudaFuncSetAttribute");
-            // shared memory before L1: several CTAs of the pass per SM
-            check(cudaFuncSetAttribute(k_fused<T>, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared),
-                  "cudaFuncSetAttribute");
+            for (auto fn : {k_fused<T, true>, k_fused<T, false>})
+            {
+                check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM), "cudaFuncSetAttribute");
+                // shared memory before L1: several CTAs of the pass per SM
+                check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared),
+                      "cudaFuncSetAttribute");
+            }
             attr_set = true;
         }
         FusedLaunch<T> L;
@@ -250,10 +259,39 @@ public:
         L.kbeg = kbeg;
         L.kend = std::max(kend, kbeg + 1);
         dim3 block(32, 8);  // 8 warps; each thread owns SH::RPT rows of the tile
-        dim3 grid(std::max(nbx, 1), std::max(nby, 1), (L.kend - L.kbeg + SH::KCH - 1) / SH::KCH);
-        k_fused<T><<<grid, block, LY::SMEM, stream_>>>(L);
-        check(cudaGetLastError(), "k_fused launch");
-        int n = 1;
+        const Jobs &J = jobs_for(p, L, nbx, nby, SH::TX, SH::TY, SH::KCH);
+        int n = 0;
+        if (J.ni > 0 && J.nb > 0)
+        {
+            // the interior instance runs beside the CPML one on a second stream
+            if (!side_)
+            {
+                check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "cudaStreamCreate");
+                check(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "cudaEventCreate");
+                check(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming), "cudaEventCreate");
+            }
+            check(cudaEventRecord(fork_, stream_), "cudaEventRecord");
+            check(cudaStreamWaitEvent(side_, fork_, 0), "cudaStreamWaitEvent");
+        }
+        if (J.nb > 0)
+        {
+            L.jobs = J.dev;
+            k_fused<T, true><<<J.nb, block, LY::SMEM, stream_>>>(L);
+            check(cudaGetLastError(), "k_fused launch");
+            ++n;
+        }
+        if (J.ni > 0)
+        {
+            L.jobs = J.dev + J.nb;
+            k_fused<T, false><<<J.ni, block, LY::SMEM, J.nb > 0 ? side_ : stream_>>>(L);
+            check(cudaGetLastError(), "k_fused launch");
+            ++n;
+        }
+        if (J.ni > 0 && J.nb > 0)
+        {
+            check(cudaEventRecord(join_, side_), "cudaEventRecord");
+            check(cudaStreamWaitEvent(stream_, join_, 0), "cudaStreamWaitEvent");
+        }
         const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
         if (nface > 0)
         {
@@ -268,6 +306,89 @@ public:
     }
     int fused(const FusedParams<double> &p) override { return fused_t(p); }
     int fused(const FusedParams<float> &p) override { return fused_t(p); }
+
+    // CTA jobs of the fused pass (x0, y0, k0, k1): the jobs whose tile, halo
+    // and planes touch a CPML point first (nb of them), then the others (ni).
+    // Built once per grid and CPML tables.
+    struct Jobs
+    {
+        int4 *dev{nullptr};
+        int nb{0}, ni{0};
+    };
+    template <typename T>
+    const Jobs &jobs_for(const FusedParams<T> &p, const FusedLaunch<T> &L, int nbx, int nby, int TX, int TY, int KCH)
+    {
+        const SideParams<T> &P = p.e;
+        char key[160];
+        std::snprintf(key, sizeof key, "%d %d %d %d %d %d %d %p %d", L.xlim, L.ylim, L.kbeg, L.kend, nbx, nby, TY,
+                      (const void *)P.pc[0][0], (int)sizeof(T));
+        auto it = jobs_.find(key);
+        if (it != jobs_.end()) return it->second;
+        // CPML flags per position along each axis (either parity)
+        std::vector<char> pml[3];
+        const int len[3] = {L.xend, P.My, P.Mz};  // table lengths (x: the valid extent, not the padded row)
+        for (int a = 0; a < 3; ++a)
+        {
+            pml[a].assign(len[a], 0);
+            if (!P.pc[0][0]) continue;
+            for (int q = 0; q < 2; ++q)
+            {
+                std::vector<T> c(len[a]);
+                check(cudaMemcpy(c.data(), P.pc[a][q], len[a] * sizeof(T), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+                for (int i = 0; i < len[a]; ++i) pml[a][i] |= c[i] != T(0);
+            }
+        }
+        auto any = [&](int a, int lo, int hi) {  // CPML anywhere in [lo, hi]
+            for (int i = std::max(lo, 0); i <= std::min(hi, len[a] - 1); ++i)
+                if (pml[a][i]) return true;
+            return false;
+        };
+        // z: chunks [a, b) whose planes a-1 .. b-1 hold no CPML point come
+        // from the longest run f0 .. f1 of such planes (a = f0 + 1,
+        // b = f1 + 1), chunked apart from the rest
+        int za = L.kbeg, zb = L.kbeg;
+        for (int f = L.kbeg - 1; f < L.kend;)
+        {
+            int e = f;
+            while (e < L.kend && !any(2, e, e)) ++e;  // planes f .. e-1 are free
+            const int a = std::max(f + 1, L.kbeg), bnd = std::min(e, L.kend);
+            if (bnd - a > zb - za) { za = a; zb = bnd; }
+            f = e + 1;
+        }
+        std::vector<std::pair<int, int>> chunks;
+        auto split = [&](int lo, int hi) {
+            if (hi <= lo) return;
+            const int nch = (hi - lo + KCH - 1) / KCH;
+            for (int i = 0; i < nch; ++i)
+                chunks.emplace_back(lo + (int)((int64_t)(hi - lo) * i / nch), lo + (int)((int64_t)(hi - lo) * (i + 1) / nch));
+        };
+        split(L.kbeg, za);
+        split(za, zb);
+        split(zb, L.kend);
+        std::vector<int4> b, in;
+        for (auto &ch : chunks)
+        {
+            const bool zin = !any(2, ch.first - 1, ch.second - 1);
+            for (int by = 0; by < std::max(nby, 1); ++by)
+            {
+                const int y0 = 1 + by * TY;
+                const bool yin = !any(1, y0 - 1, y0 + TY - 1);
+                for (int bx = 0; bx < std::max(nbx, 1); ++bx)
+                {
+                    const int x0 = 1 + bx * TX;
+                    const bool xin = !any(0, x0 - 1, x0 + TX - 1);
+                    (zin && yin && xin ? in : b).push_back(make_int4(x0, y0, ch.first, ch.second));
+                }
+            }
+        }
+        Jobs J;
+        J.nb = (int)b.size();
+        J.ni = (int)in.size();
+        b.insert(b.end(), in.begin(), in.end());
+        check(cudaMalloc(&J.dev, b.size() * sizeof(int4)), "cudaMalloc");
+        check(cudaMemcpy(J.dev, b.data(), b.size() * sizeof(int4), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        return jobs_[key] = J;
+    }
 
     template <typename T>
     CUtensorMap map_for(const T *base, int Mx, int My, int Mz, int bx, int by)
@@ -371,6 +492,9 @@ private:
     int dev_{0};
     int *err_{nullptr};
     std::map<std::pair<const void *, int>, CUtensorMap> maps_;
+    std::map<std::string, Jobs> jobs_;
+    cudaStream_t side_{nullptr};
+    cudaEvent_t fork_{nullptr}, join_{nullptr};
 };
 } // namespace
 
