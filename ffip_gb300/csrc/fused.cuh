@@ -148,6 +148,8 @@ constexpr unsigned kInfoDftE = 1u << 23;   // an E DFT unit meets this tile plan
 constexpr unsigned kInfoDftH = 1u << 24;   // an H DFT unit meets this tile plane
 constexpr unsigned kInfoFastH = 1u << 25;  // H of this tile plane takes the plain path
 constexpr unsigned kInfoFastE = 1u << 26;  // E of this tile plane takes the plain path (rows without slots)
+constexpr unsigned kInfoLeanH = 1u << 27;  // H: CPML, but every point valid, no slot, no DFT unit
+constexpr unsigned kInfoLeanE = 1u << 28;  // E: CPML, but every point valid, no DFT unit (rows without slots)
 
 template <typename T>
 struct FusedLaunch
@@ -317,11 +319,18 @@ __device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &
 // General H(k) at this thread's own point of tile row `row`: validity bits,
 // CPML from the staged tables (psi values ph loaded by the caller), material
 // slots, DFT.
-template <typename T>
+template <typename T, bool FULL = true>
 __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int row, int eA, int eB, int hA, int slot_new,
                                               unsigned vb, bool owned, bool pml, bool slots, bool dft, int idx,
                                               const T (&ph)[3][2])
 {
+    // FULL = false: the lean instance for CPML tile planes whose points are
+    // all valid, with no material slot and no DFT unit
+    if (!FULL)
+    {
+        vb = 63u;
+        slots = dft = false;
+    }
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX;
     const FusedParams<T> &F = X.L->fp;
@@ -379,12 +388,17 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
 // General E(k) at this thread's own point of tile row `row` (E plane qe of
 // the chunk), from the H ring planes rn (plane k) and rp (plane k-1); CPML
 // psi is read and written in place here; sl: material slot indices.
-template <typename T>
+template <typename T, bool FULL = true>
 __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int eS, int rn, int rp, unsigned vb,
                                               bool pml, bool slots, bool dft, int idx, const int (&sl)[3])
 {
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX, TX = SH::TX;
+    if (!FULL)
+    {
+        vb = 63u;
+        slots = dft = false;
+    }
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PE = F.e;
     const int tx = threadIdx.x;
@@ -594,8 +608,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     {
         const unsigned w = info[o];
         const bool zpml = pml_tables && (tile_pml || (w & kInfoZPml));
-        if (inside && !zpml && !h_slots && !(w & kInfoDftH) && ((w >> (kInfoZValidShift + 3)) & 7u) == 7u) info[o] |= kInfoFastH;
-        if (inside && !zpml && !(w & kInfoDftE) && ((w >> kInfoZValidShift) & 7u) == 7u) info[o] |= kInfoFastE;
+        const bool hok = inside && !h_slots && !(w & kInfoDftH) && ((w >> (kInfoZValidShift + 3)) & 7u) == 7u;
+        const bool eok = inside && !(w & kInfoDftE) && ((w >> kInfoZValidShift) & 7u) == 7u;
+        info[o] |= (hok ? (zpml ? kInfoLeanH : kInfoFastH) : 0u) | (eok ? (zpml ? kInfoLeanE : kInfoFastE) : 0u);
     }
     __syncthreads();
     const int sz = (int)PE.sz, sy = (int)PE.sy;
@@ -628,6 +643,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         const bool e_slots = (we & rowmask) != 0u;
         const bool fast_h = wh & kInfoFastH;
         const bool fast_e = (we & kInfoFastE) && !e_slots;
+        const bool lean_h = PML && (wh & kInfoLeanH);
+        const bool lean_e = PML && (we & kInfoLeanE) && !e_slots;
         const bool pml_h = !fast_h && pml_tables && (tile_pml || (wh & kInfoZPml));
         const bool pml_e = !fast_e && pml_tables && (tile_pml || (we & kInfoZPml));
         const bool dft_h = wh & kInfoDftH, dft_e = we & kInfoDftE;
@@ -773,10 +790,19 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             }
             else
             {
+                if (lean_h)
+                {
 #pragma unroll
-                for (int r = 0; r < RPT; ++r)
-                    h_own_general<T>(X, q, r0 + r, eA, eB, hA, rn, vxy[r] & (wh >> kInfoZValidShift), q >= 1, pml_h, h_slots,
-                                     dft_h, idx + r * sy, ph[r]);
+                    for (int r = 0; r < RPT; ++r)
+                        h_own_general<T, false>(X, q, r0 + r, eA, eB, hA, rn, 63u, q >= 1, true, false, false, idx + r * sy, ph[r]);
+                }
+                else
+                {
+#pragma unroll
+                    for (int r = 0; r < RPT; ++r)
+                        h_own_general<T>(X, q, r0 + r, eA, eB, hA, rn, vxy[r] & (wh >> kInfoZValidShift), q >= 1, pml_h,
+                                         h_slots, dft_h, idx + r * sy, ph[r]);
+                }
                 if (wid >= 6 || (wid == 5 && lane < 2 * TY))
                 {
                     int hx, hy, comp, row, col;
@@ -820,6 +846,12 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     F.eout[1][idx_e + r * sy] = ey;
                     F.eout[2][idx_e + r * sy] = ez;
                 }
+            }
+            else if (lean_e)
+            {
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+                    e_own_general<T, false>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false, false, idx_e + r * sy, sl_e[r]);
             }
             else
             {
