@@ -261,9 +261,13 @@ public:
         dim3 block(32, 8);  // 8 warps; each thread owns SH::RPT rows of the tile
         const Jobs &J = jobs_for(p, L, nbx, nby, SH::TX, SH::TY, SH::KCH);
         int n = 0;
-        if (J.ni > 0 && J.nb > 0)
+        const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
+        const unsigned face_blocks = (unsigned)((nface + 255) / 256);
+        // a second stream runs the interior instance beside the CPML one, and
+        // the H half of k_face (it reads only step-n fields) beside both
+        const bool fork = (J.ni > 0 && J.nb > 0) || nface > 0;
+        if (fork)
         {
-            // the interior instance runs beside the CPML one on a second stream
             if (!side_)
             {
                 check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -287,20 +291,23 @@ public:
             check(cudaGetLastError(), "k_fused launch");
             ++n;
         }
-        if (J.ni > 0 && J.nb > 0)
+        if (nface > 0)
+        {
+            k_face<T, false><<<face_blocks, 256, 0, side_>>>(L);
+            check(cudaGetLastError(), "k_face launch");
+            ++n;
+        }
+        if (fork)
         {
             check(cudaEventRecord(join_, side_), "cudaEventRecord");
             check(cudaStreamWaitEvent(stream_, join_, 0), "cudaStreamWaitEvent");
         }
-        const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
         if (nface > 0)
         {
-            const unsigned blocks = (unsigned)((nface + 255) / 256);
-            k_face<T, false><<<blocks, 256, 0, stream_>>>(L);
+            // E of the face layers reads the new H of the pass
+            k_face<T, true><<<face_blocks, 256, 0, stream_>>>(L);
             check(cudaGetLastError(), "k_face launch");
-            k_face<T, true><<<blocks, 256, 0, stream_>>>(L);
-            check(cudaGetLastError(), "k_face launch");
-            n += 2;
+            ++n;
         }
         return n;
     }
