@@ -380,7 +380,6 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
             F.hout[c][idx] = v;
             if (hc[a1].c != T(0)) F.psih_out[c][0][idx] = ps1;
             if (hc[a2].c != T(0)) F.psih_out[c][1][idx] = ps2;
-            if (dft) dft_point<T>(PH.nunits, PH.units, PH.phase, 3 + c, x, y, k, (double)v, (double)vd);
         }
     }
 }
@@ -454,7 +453,6 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
             F.eout[c][idx] = v;
             if (ec[a1].c != T(0)) PE.psi[c][0][idx] = ps1;
             if (ec[a2].c != T(0)) PE.psi[c][1][idx] = ps2;
-            if (dft) dft_point<T>(PE.nunits, PE.units, PE.phase, c, x, y, k, (double)v, (double)vd);
         }
     }
 }
@@ -868,6 +866,62 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         rpp = rp;
         rp = rn;
         rn = rn == 2 ? 0 : rn + 1;
+    }
+}
+
+// DFT sums of one side after the fused pass (DFT_Unit::update,
+// src/dft.cpp:29-62): one thread per monitored point of the side's units,
+// reading the new field from the pass's output buffers; for D/B monitors the
+// value is g_inf field + sum of the new polarisations, as material_at forms
+// it.  The fused pass itself leaves the sums alone, so that its registers
+// carry no DFT code; this runs before the E sources, which add their own
+// share of the sums.
+template <typename T>
+__global__ void k_dft(const __grid_constant__ SideParams<T> P, const T *f0, const T *f1, const T *f2, int64_t total)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    int u = 0;
+    int64_t base = 0;
+    for (; u < P.nunits; ++u)
+    {
+        if (t < base + P.units[u].npts) break;
+        base += P.units[u].npts;
+    }
+    if (u == P.nunits) return;
+    const DftView &U = P.units[u];
+    const int64_t l = t - base;
+    const int li = (int)(l % U.ld[0]), lj = (int)((l / U.ld[0]) % U.ld[1]), lk = (int)(l / ((int64_t)U.ld[0] * U.ld[1]));
+    const int i = U.i0[0] + li, j = U.i0[1] + lj, k = U.i0[2] + lk;
+    const int c = U.comp - P.comp_base;
+    if (i < P.vlo[c][0] || i > P.vhi[c][0] || j < P.vlo[c][1] || j > P.vhi[c][1] || k < P.vlo[c][2] || k > P.vhi[c][2]) return;
+    const int64_t idx = (int64_t)i + (int64_t)j * P.sy + (int64_t)k * P.sz;
+    const T v = (c == 0 ? f0 : c == 1 ? f1 : f2)[idx];
+    T vd = P.g_def * v;
+    if (U.is_db)
+    {
+        const SlotView<T> &S = P.slot[c];
+        const int slot = S.map ? S.map[idx] : -1;
+        if (slot >= 0)
+        {
+            const int g = S.group[slot];
+            const int np = P.grp_np[g];
+            if (np == 0)
+                vd = S.g[slot] * v;
+            else
+            {
+                T psum = T(0);
+                for (int q = 0; q < np; ++q) psum = psum + S.P[q * S.n + slot];
+                vd = fma_rn(S.g[slot], v, psum);
+            }
+        }
+    }
+    const double x = U.is_db ? (double)vd : (double)v;
+    for (int f = 0; f < U.nf; ++f)
+    {
+        const double cw = P.phase[U.foff + f][0], sw = P.phase[U.foff + f][1];
+        U.im[f * U.npts + l] += sw * x;
+        U.re[f * U.npts + l] += cw * x;
     }
 }
 

@@ -231,7 +231,10 @@ public:
             L.tm_e[c] = map_for(p.ein[c], p.e.Mx, p.e.My, p.e.Mz, SH::BX, SH::TY + 2);
             L.tm_h[c] = map_for(p.hin[c], p.e.Mx, p.e.My, p.e.Mz, SH::BX, SH::TY + 1);
         }
+        // DFT sums are added by k_dft after the pass, not inside it
         L.fp = p;
+        L.fp.e.nunits = 0;
+        L.fp.h.nunits = 0;
         L.err = err_;
         // valid extents over all six components
         int xend = 0, yend = 0, kbeg = p.e.Mz, kend = 0;
@@ -307,6 +310,18 @@ public:
             // E of the face layers reads the new H of the pass
             k_face<T, true><<<face_blocks, 256, 0, stream_>>>(L);
             check(cudaGetLastError(), "k_face launch");
+            ++n;
+        }
+        // DFT sums of both sides from the new fields
+        for (int sd = 0; sd < 2; ++sd)
+        {
+            const SideParams<T> &P = sd == 0 ? p.e : p.h;
+            int64_t total = 0;
+            for (int u = 0; u < P.nunits; ++u) total += P.units[u].npts;
+            if (!total) continue;
+            T *const *f = sd == 0 ? p.eout : p.hout;
+            k_dft<T><<<(unsigned)((total + 255) / 256), 256, 0, stream_>>>(P, f[0], f[1], f[2], total);
+            check(cudaGetLastError(), "k_dft launch");
             ++n;
         }
         return n;
