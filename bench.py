@@ -310,8 +310,8 @@ def main():
            "gpu_launches": res["fp32"]["launches"],
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                         "traffic": profiled_traffic(a.n) if res["fp32"]["fused"] else None,
-                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one k_fused launch, "
-                                          "profiles/k_fused_fp32_dispersive%d.md" % a.n, "peak_kind": peak_kind,
+                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one step's k_fused launches "
+                                          "(both instances), profiles/k_fused_fp32_dispersive%d.md" % a.n, "peak_kind": peak_kind,
                         "kernel": "k_fused" if res["fp32"]["fused"] else "k_update (H and E launches)",
                         "algorithmic_bytes_per_step": res["fp32"]["bytes_per_step"],
                         "timing": "CUDA events on the stepper's stream around the %d timed steps" % a.steps},

@@ -620,7 +620,12 @@ class Adjoint_Volume:
 
     def __init__(self, adjoint_simulation, forward_simulation, frequency=1.0, center=None, size=None, dim=None, density=None,
                  medium1=None, medium2=None, epsilon_fun=None, epsilon_der=None, e_sus=(), norm=1, geometry=None):
-        """geometry (rebuild-only): the design box of another Adjoint_Volume
+        """norm: the spectrum sum_n g(t_n) exp(-2 pi j f t_n) of the pulse g of
+        the adjoint sources at this frequency (the adjoint field carries that
+        pulse; when the forward pulse differs, the forward one is not the
+        right divisor).
+
+        geometry (rebuild-only): the design box of another Adjoint_Volume
         of the same forward simulation (another frequency); it is then added
         to the adjoint simulation only, so that the forward simulation holds
         the design box once."""

@@ -137,14 +137,15 @@ def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0
                float(rng.integers(dz // 2 + 8, nz / 2 - pml - 8))) for _ in range(nprobe)]
     rho0 = filtered_noise((dz + 1, dn + 1, dn + 1), 3.0, seed)
     dt = 0.5
-    t = np.arange(fwd_func.start_time, fwd_func.end_time, dt)
     terms, geom = [], None
     for f in freqs:
         adj = Simulation(size=V(n, n, nz), resolution=1, pmls=pmls, precision=precision)
         adj_func = Gaussian1(0.1, cutoff=4, start_time=0.5 / f)
         srcs = [Adjoint_Source(adj, fwd, function=adj_func, frequency=f, center=V(*p), size=V(0, 0, 0), dim=V(1, 1, 1),
                                udfs=[field_match_objective(np.zeros((1, 1, 1)), "Ex", weight=1.0)]) for p in probes]
-        norm = np.sum(np.exp(-2j * np.pi * f * t) * fwd_func(t))
+        # the adjoint field carries the adjoint pulse: normalise by its spectrum
+        t = np.arange(adj_func.start_time, adj_func.end_time, dt)
+        norm = np.sum(np.exp(-2j * np.pi * f * t) * adj_func(t))
         vol = Adjoint_Volume(adj, fwd, frequency=f, center=V(0, 0, 0), size=V(dn, dn, dz), dim=V(dn + 1, dn + 1, dz + 1),
                              density=rho0, medium1=Medium(epsilon=12), medium2=Medium(), norm=norm, geometry=geom)
         geom = vol.geom

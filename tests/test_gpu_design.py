@@ -6,7 +6,8 @@ Set-up: 24^3 cells, 6-cell CPML, Ex current sheet below a 6 x 6 x 3 design
 box (4 x 4 x 3 density nodes, eps = 1 + rho), objective |Ex|^2 summed over
 a 2 x 2 probe above it at f = 0.1 (field_match_objective with a zero target).
 The adjoint pulse starts at 1/(2 f) so that its phase shifts never cut the
-pulse at t = 0, and the runs are long enough (2400 time units) for the
+pulse at t = 0, the gradient is normalised by the adjoint pulse's spectrum
+(the forward pulse starts at 0), and the runs are long enough (2400 time units) for the
 fields to have decayed, so that the DFTs are the full transforms that the
 adjoint identity needs."""
 import numpy as np
@@ -23,17 +24,20 @@ def make_problem(precision="fp64", exact=True):
     import ffip_gb300 as ffip
     from ffip_gb300.design import AdjointProblem, AdjointTerm
     V = ffip.Vector3
-    src_func = ffip.Gaussian1(F0, cutoff=4, start_time=0.5 / F0)
+    # forward and adjoint pulses differ (start times 0 and 1/(2 f)): the
+    # gradient is normalised by the adjoint pulse's spectrum
+    fwd_func = ffip.Gaussian1(F0, cutoff=4, start_time=0.0)
+    adj_func = ffip.Gaussian1(F0, cutoff=4, start_time=0.5 / F0)
     pml = [ffip.PML(thickness=6, sigma_max=6.14)]
     fwd = ffip.Simulation(size=V(24, 24, 24), resolution=1, pmls=pml, precision=precision, device=0,
-                          sources=[ffip.Source(function=src_func, center=V(0, 0, -6), size=V(12, 12, 0),
+                          sources=[ffip.Source(function=fwd_func, center=V(0, 0, -6), size=V(12, 12, 0),
                                                field_component="Ex")])
     adj = ffip.Simulation(size=V(24, 24, 24), resolution=1, pmls=pml, precision=precision, device=0)
-    asrc = ffip.Adjoint_Source(adj, fwd, function=src_func, frequency=F0, center=V(0.5, 0, 5), size=V(2, 2, 0),
+    asrc = ffip.Adjoint_Source(adj, fwd, function=adj_func, frequency=F0, center=V(0.5, 0, 5), size=V(2, 2, 0),
                                dim=V(2, 2, 1), udfs=[ffip.field_match_objective(np.zeros((1, 2, 2)), "Ex", weight=2.0)])
     dt = fwd.dx * fwd.courant
-    t = np.arange(src_func.start_time, src_func.end_time, dt)
-    norm = np.sum(np.exp(-2j * np.pi * F0 * t) * src_func(t))
+    t = np.arange(adj_func.start_time, adj_func.end_time, dt)
+    norm = np.sum(np.exp(-2j * np.pi * F0 * t) * adj_func(t))
     rho0 = np.full((3, 4, 4), 0.5)
     vol = ffip.Adjoint_Volume(adj, fwd, frequency=F0, center=V(0, 0, 0), size=V(6, 6, 3), dim=V(4, 4, 3), density=rho0,
                               medium1=ffip.Medium(epsilon=2), medium2=ffip.Medium(), norm=norm)
