@@ -262,7 +262,14 @@ public:
         L.kbeg = kbeg;
         L.kend = std::max(kend, kbeg + 1);
         dim3 block(32, 8);  // 8 warps; each thread owns SH::RPT rows of the tile
-        const Jobs &J = jobs_for(p, L, nbx, nby, SH::TX, SH::TY, SH::KCH);
+        // z chunk length: at most KCH planes, fewer when the grid has too few
+        // tiles to fill the GPU (each chunk recomputes one H plane, so at
+        // least 4 planes)
+        if (!nsm_) check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
+        const int64_t tiles = (int64_t)std::max(nbx, 1) * std::max(nby, 1);
+        const int64_t want = 2LL * nsm_ * SH::MINB;  // CTAs for two waves
+        const int kch = (int)std::max<int64_t>(4, std::min<int64_t>(SH::KCH, ((int64_t)(L.kend - L.kbeg) * tiles + want - 1) / want));
+        const Jobs &J = jobs_for(p, L, nbx, nby, SH::TX, SH::TY, kch);
         int n = 0;
         const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
         const unsigned face_blocks = (unsigned)((nface + 255) / 256);
@@ -342,7 +349,7 @@ public:
     {
         const SideParams<T> &P = p.e;
         char key[160];
-        std::snprintf(key, sizeof key, "%d %d %d %d %d %d %d %p %d", L.xlim, L.ylim, L.kbeg, L.kend, nbx, nby, TY,
+        std::snprintf(key, sizeof key, "%d %d %d %d %d %d %d %d %p %d", L.xlim, L.ylim, L.kbeg, L.kend, nbx, nby, TY, KCH,
                       (const void *)P.pc[0][0], (int)sizeof(T));
         auto it = jobs_.find(key);
         if (it != jobs_.end()) return it->second;
@@ -516,6 +523,7 @@ private:
     std::map<std::pair<const void *, int>, CUtensorMap> maps_;
     std::map<std::string, Jobs> jobs_;
     cudaStream_t side_{nullptr};
+    int nsm_{0};
     cudaEvent_t fork_{nullptr}, join_{nullptr};
 };
 } // namespace
