@@ -15,7 +15,7 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libffip_gb300.so")
 CLI = os.path.join(LIBDIR, "run_sim_json")
 
-CUDA_SOURCES = ["kernels.cu", "adjoint.cu"]
+CUDA_SOURCES = ["kernels.cu", "adjoint.cu", "surrogate.cu"]
 CXX_SOURCES = ["plan.cpp", "engine.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

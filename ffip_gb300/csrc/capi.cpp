@@ -1,5 +1,6 @@
 // C ABI (include/ffip_gb300.h) over the engine and the CUDA backend.
 #include "../../include/ffip_gb300.h"
+#include "../../include/ffip_gb300_surrogate.h"
 
 #include <cstring>
 #include <map>
@@ -21,6 +22,10 @@ int adjoint_sensitivity(double w_re, double w_im, double norm_re, double norm_im
 int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
                               const double *pt, uint64_t npts, double *out);
 uint64_t adjoint_transpose_noalloc_capacity();
+int sg_gemm(int M, int N, int K, const void *A, int64_t ars, int64_t acs, const void *B, int64_t brs, int64_t bcs, float *C,
+            int64_t crs, int64_t ccs, const float *bias, int accumulate, void *stream);
+int sg_im2col(const void *x, const int *shape, const int *kernel, const int *stride, const int *pad, void *cols, void *stream);
+int sg_col2im(const float *dcols, const int *shape, const int *kernel, const int *stride, const int *pad, float *dx, void *stream);
 } // namespace ffipg
 
 struct ffip_sim
@@ -286,6 +291,33 @@ int ffip_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint
                                               " x " + std::to_string(nz) + " exceeds the fixed scratch of " +
                                               std::to_string(cap) + " doubles; use ffip_transpose");
         return ffipg::adjoint_transpose_noalloc(gx, nx, gy, ny, gz, nz, pt, npts, out);
+    });
+}
+
+int ffip_sg_gemm(int M, int N, int K, const void *A, int64_t ars, int64_t acs, const void *B, int64_t brs, int64_t bcs,
+                 float *C, int64_t crs, int64_t ccs, const float *bias, int accumulate, void *stream)
+{
+    return guard([&]() -> int {
+        if ((M > 0 && N > 0) && (!C || (K > 0 && (!A || !B)))) return fail(FFIP_ERR_INVALID, "null argument");
+        return ffipg::sg_gemm(M, N, K, A, ars, acs, B, brs, bcs, C, crs, ccs, bias, accumulate, stream);
+    });
+}
+
+int ffip_sg_im2col(const void *x, const int *shape5, const int *kernel3, const int *stride3, const int *pad3, void *cols,
+                   void *stream)
+{
+    return guard([&]() -> int {
+        if (!x || !shape5 || !kernel3 || !stride3 || !pad3 || !cols) return fail(FFIP_ERR_INVALID, "null argument");
+        return ffipg::sg_im2col(x, shape5, kernel3, stride3, pad3, cols, stream);
+    });
+}
+
+int ffip_sg_col2im(const float *dcols, const int *shape5, const int *kernel3, const int *stride3, const int *pad3, float *dx,
+                   void *stream)
+{
+    return guard([&]() -> int {
+        if (!dcols || !shape5 || !kernel3 || !stride3 || !pad3 || !dx) return fail(FFIP_ERR_INVALID, "null argument");
+        return ffipg::sg_col2im(dcols, shape5, kernel3, stride3, pad3, dx, stream);
     });
 }
 

@@ -127,4 +127,17 @@ int adjoint_transpose_noalloc(const double *, uint64_t, const double *, uint64_t
     throw std::runtime_error("not emulated");
 }
 uint64_t adjoint_transpose_noalloc_capacity() { return uint64_t(1) << 20; }
+int sg_gemm(int, int, int, const void *, int64_t, int64_t, const void *, int64_t, int64_t, float *, int64_t, int64_t,
+            const float *, int, void *)
+{
+    throw std::runtime_error("not emulated");
+}
+int sg_im2col(const void *, const int *, const int *, const int *, const int *, void *, void *)
+{
+    throw std::runtime_error("not emulated");
+}
+int sg_col2im(const float *, const int *, const int *, const int *, const int *, float *, void *)
+{
+    throw std::runtime_error("not emulated");
+}
 } // namespace ffipg

@@ -11,8 +11,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def header_functions():
-    txt = open(os.path.join(ROOT, "include", "ffip_gb300.h")).read()
+def header_functions(name="ffip_gb300.h"):
+    txt = open(os.path.join(ROOT, "include", name)).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
     return sorted(set(re.findall(r"\b(ffip_[a-z_]+)\s*\(", txt)))
 
@@ -30,6 +30,8 @@ def test_library_exports_every_declared_symbol():
     for f in header_functions():
         assert hasattr(lib, f), f
     assert sorted(native.EXPORTS) == header_functions()
+    for f in header_functions("ffip_gb300_surrogate.h"):
+        assert hasattr(lib, f), f
 
 
 def test_build_targets_sm_103a_only():

@@ -1,0 +1,83 @@
+"""The surrogate's kernels (tensor-core bf16 GEMM, im2col, col2im) and its
+convolution against plain PyTorch fp32 references of the same operations on
+the same bf16-rounded inputs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _bf(t):
+    return t.to(torch.bfloat16)
+
+
+@pytest.mark.parametrize("M,N,K", [(64, 64, 32), (37, 129, 70), (1, 5, 3), (256, 512, 6912), (32, 4099, 27)])
+def test_gemm_matches_fp32_reference(M, N, K):
+    from ffip_gb300 import surrogate as S
+    g = torch.Generator(device="cuda").manual_seed(M * 7 + N)
+    A = _bf(torch.randn(M, K, device="cuda", generator=g))
+    B = _bf(torch.randn(K, N, device="cuda", generator=g))
+    ref = A.float() @ B.float()
+    got = S.gemm(A, B)
+    # bf16 products are exact in fp32; only the summation order differs
+    tol = 1e-5 * K ** 0.5 * ref.abs().max().item() + 1e-6
+    assert (got - ref).abs().max().item() <= tol
+
+
+def test_gemm_strides_bias_and_accumulate():
+    from ffip_gb300 import surrogate as S
+    g = torch.Generator(device="cuda").manual_seed(1)
+    A = _bf(torch.randn(50, 40, device="cuda", generator=g))       # used transposed: [40, 50]
+    B = _bf(torch.randn(90, 50, device="cuda", generator=g)).t()   # [50, 90], column-major view
+    bias = torch.randn(40, device="cuda", generator=g)
+    C0 = torch.randn(40, 90, device="cuda", generator=g)
+    ref = C0 + (A.t().float() @ B.float() + bias[:, None])
+    out = C0.clone()
+    S.gemm(A.t(), B, bias=bias, out=out, accumulate=True)
+    assert (out - ref).abs().max().item() <= 1e-4
+
+
+@pytest.mark.parametrize("dims", [3, 2])
+def test_conv_forward_and_backward_match_fp32_reference(dims):
+    from ffip_gb300 import surrogate as S
+    F = torch.nn.functional
+    g = torch.Generator(device="cuda").manual_seed(dims)
+    if dims == 3:
+        x = _bf(torch.randn(3, 5, 6, 10, 9, device="cuda", generator=g))
+        w = _bf(torch.randn(7, 5, 3, 3, 3, device="cuda", generator=g) * 0.2).float()
+        stride, pad = (2, 2, 2), (1, 1, 1)
+    else:
+        x = _bf(torch.randn(3, 5, 1, 12, 11, device="cuda", generator=g))
+        w = _bf(torch.randn(7, 5, 1, 3, 3, device="cuda", generator=g) * 0.2).float()
+        stride, pad = (1, 1, 1), (0, 1, 1)
+    b = torch.randn(7, device="cuda", generator=g)
+    xr = x.float().requires_grad_(True)
+    wr = w.clone().requires_grad_(True)
+    br = b.clone().requires_grad_(True)
+    yr = F.conv3d(xr, wr, br, stride=stride, padding=pad)
+    dy = _bf(torch.randn(yr.shape, device="cuda", generator=g))
+    yr.backward(dy.float())
+    xs = x.clone().requires_grad_(True)
+    ws = w.clone().requires_grad_(True)
+    bs = b.clone().requires_grad_(True)
+    ys = S.conv(xs, ws, bs, stride, pad)
+    assert ys.dtype == torch.bfloat16 and ys.shape == yr.shape
+    # the forward output is rounded to bf16
+    assert (ys.float() - yr).abs().max().item() <= 1e-2 * yr.abs().max().item()
+    ys.backward(dy)
+    assert (ws.grad - wr.grad).abs().max().item() <= 1e-4 * wr.grad.abs().max().item()
+    assert (bs.grad - br.grad).abs().max().item() <= 1e-4 * br.grad.abs().max().item()
+    assert (xs.grad.float() - xr.grad).abs().max().item() <= 1e-2 * xr.grad.abs().max().item()
+
+
+def test_network_shapes_and_a_few_training_steps_reduce_the_loss():
+    from ffip_gb300 import surrogate as S
+    net = S.make_net(out_channels=12, width=8, seed=0).cuda()
+    rng = np.random.default_rng(0)
+    rho = rng.uniform(0, 1, size=(8, 16, 64, 64)).astype(np.float32)
+    y = rng.normal(size=(8, 12, 64, 64)).astype(np.float32) * 0.1 + rho[:, :1, ::1, :].mean(1, keepdims=True)[:, :, :64, :64]
+    out = net(torch.tensor(rho, device="cuda"))
+    assert tuple(out.shape) == (8, 12, 64, 64)
+    h = S.train(net, rho, y, epochs=6, batch=4, lr=3e-3)
+    assert h["loss"][-1] < h["loss"][0]
