@@ -54,17 +54,33 @@ __global__ void __launch_bounds__(128) k_sg_gemm(int M, int N, int K, const __nv
     const __nv_bfloat16 zero = __float2bfloat16(0.f);
     for (int k0 = 0; k0 < K; k0 += BK)
     {
-        // stage the A and B tiles (bounds-checked, zero filled)
-        for (int e = tid; e < BM * BK; e += 128)
-        {
-            const int r = e / BK, c = e % BK, m = m0 + r, k = k0 + c;
-            As[r][c] = (m < M && k < K) ? A[m * ars + k * acs] : zero;
-        }
-        for (int e = tid; e < BN * BK; e += 128)
-        {
-            const int r = e / BK, c = e % BK, n = n0 + r, k = k0 + c;
-            Bs[r][c] = (n < N && k < K) ? B[k * brs + n * bcs] : zero;
-        }
+        // stage the A and B tiles (bounds-checked, zero filled); consecutive
+        // threads walk the operand's unit-stride direction so that the
+        // global loads coalesce
+        if (acs == 1)
+            for (int e = tid; e < BM * BK; e += 128)
+            {
+                const int r = e / BK, c = e % BK, m = m0 + r, k = k0 + c;
+                As[r][c] = (m < M && k < K) ? A[m * ars + k] : zero;
+            }
+        else
+            for (int e = tid; e < BM * BK; e += 128)
+            {
+                const int r = e % BM, c = e / BM, m = m0 + r, k = k0 + c;
+                As[r][c] = (m < M && k < K) ? A[m * ars + k * acs] : zero;
+            }
+        if (bcs == 1)
+            for (int e = tid; e < BN * BK; e += 128)
+            {
+                const int r = e % BN, c = e / BN, n = n0 + r, k = k0 + c;
+                Bs[r][c] = (n < N && k < K) ? B[k * brs + n] : zero;
+            }
+        else
+            for (int e = tid; e < BN * BK; e += 128)
+            {
+                const int r = e / BK, c = e % BK, n = n0 + r, k = k0 + c;
+                Bs[r][c] = (n < N && k < K) ? B[k * brs + n * bcs] : zero;
+            }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < BK; kk += 16)

@@ -156,10 +156,13 @@ def conv(x, w, b, stride, pad):
 
 
 def make_net(out_channels: int = 12, width: int = 32, seed: int = 0):
-    """The surrogate: a 3-D encoder of four stride-2 blocks (width, 2, 4, 8 x
-    width channels; two 3x3x3 convolutions each) from a 16 x 64 x 64 density
-    to 8 width x 1 x 4 x 4, then a 2-D decoder of four (x2 nearest upsample,
-    3x3 convolution) stages to out_channels x 64 x 64."""
+    """The surrogate, a 3-D / 2-D U-Net: a 3-D encoder of four stride-2
+    blocks (width, 2, 4, 8 x width channels; two 3x3x3 convolutions each)
+    from a 16 x 64 x 64 density down to 8 width x 1 x 4 x 4, and a 2-D decoder
+    of four (x2 nearest upsample, concatenation with the encoder features of
+    that size folded to 2-D (channels x depth), 3x3 convolution) stages up to
+    64 x 64, where the density itself (16 depth channels) joins; a 1x1
+    convolution gives out_channels."""
     torch = _torch()
     nn = torch.nn
     F = torch.nn.functional
@@ -170,34 +173,43 @@ def make_net(out_channels: int = 12, width: int = 32, seed: int = 0):
             g = torch.Generator().manual_seed(seed)
             self.enc = nn.ParameterList()
             self.encb = nn.ParameterList()
-            c_in = 1
+            c_in, depth = 1, 16
+            skip = []  # channels x depth of each encoder stage's output
             for i in range(4):
                 c_out = width * (2 ** i)
-                for j, (ci, st) in enumerate(((c_in, 2), (c_out, 1))):
+                for ci in (c_in, c_out):
                     fan = ci * 27
                     self.enc.append(nn.Parameter(torch.randn(c_out, ci, 3, 3, 3, generator=g) * math.sqrt(2.0 / fan)))
                     self.encb.append(nn.Parameter(torch.zeros(c_out)))
+                depth //= 2
+                skip.append(c_out * depth)
                 c_in = c_out
             self.dec = nn.ParameterList()
             self.decb = nn.ParameterList()
-            chans = [c_in, 4 * width, 2 * width, width, width]
+            outs = [4 * width, 2 * width, width, width]
+            ins = [skip[3] + skip[2], outs[0] + skip[1], outs[1] + skip[0], outs[2] + 16]
             for i in range(4):
-                fan = chans[i] * 9
-                self.dec.append(nn.Parameter(torch.randn(chans[i + 1], chans[i], 1, 3, 3, generator=g) * math.sqrt(2.0 / fan)))
-                self.decb.append(nn.Parameter(torch.zeros(chans[i + 1])))
+                fan = ins[i] * 9
+                self.dec.append(nn.Parameter(torch.randn(outs[i], ins[i], 1, 3, 3, generator=g) * math.sqrt(2.0 / fan)))
+                self.decb.append(nn.Parameter(torch.zeros(outs[i])))
             self.head = nn.Parameter(torch.randn(out_channels, width, 1, 1, 1, generator=g) * math.sqrt(1.0 / width))
             self.headb = nn.Parameter(torch.zeros(out_channels))
 
         def forward(self, rho):
             # rho: [N, 16, 64, 64] (z, y, x) in [0, 1]
             x = (rho.unsqueeze(1) * 2 - 1).to(torch.bfloat16)
+            feats = []
             for i in range(8):
                 st = 2 if i % 2 == 0 else 1
                 x = F.relu(conv(x, self.enc[i], self.encb[i], (st, st, st), (1, 1, 1)))
-            N, C, D, H, W = x.shape
-            x = x.reshape(N, C * D, 1, H, W)
+                if i % 2 == 1:
+                    N, C, D, H, W = x.shape
+                    feats.append(x.reshape(N, C * D, 1, H, W))
+            skips = [feats[2], feats[1], feats[0], (rho.unsqueeze(2) * 2 - 1).to(torch.bfloat16)]
+            x = feats[3]
             for i in range(4):
                 x = F.interpolate(x, scale_factor=(1, 2, 2), mode="nearest")
+                x = torch.cat([x, skips[i]], dim=1)
                 x = F.relu(conv(x, self.dec[i], self.decb[i], (1, 1, 1), (0, 1, 1)))
             y = conv(x, self.head, self.headb, (1, 1, 1), (0, 0, 0))
             return y.float().squeeze(2)  # [N, out_channels, 64, 64]
