@@ -917,11 +917,32 @@ __global__ void k_dft(const __grid_constant__ SideParams<T> P, const T *f0, cons
         }
     }
     const double x = U.is_db ? (double)vd : (double)v;
-    for (int f = 0; f < U.nf; ++f)
+    // eight frequencies at a time: their sixteen loads are in flight together
+    for (int f0 = 0; f0 < U.nf; f0 += 8)
     {
-        const double cw = P.phase[U.foff + f][0], sw = P.phase[U.foff + f][1];
-        U.im[f * U.npts + l] += sw * x;
-        U.re[f * U.npts + l] += cw * x;
+        const int nb = min(8, U.nf - f0);
+        double re[8], im[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (j < nb)
+            {
+                im[j] = U.im[(f0 + j) * U.npts + l];
+                re[j] = U.re[(f0 + j) * U.npts + l];
+            }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (j < nb)
+            {
+                im[j] += P.phase[U.foff + f0 + j][1] * x;
+                re[j] += P.phase[U.foff + f0 + j][0] * x;
+            }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (j < nb)
+            {
+                U.im[(f0 + j) * U.npts + l] = im[j];
+                U.re[(f0 + j) * U.npts + l] = re[j];
+            }
     }
 }
 
