@@ -227,4 +227,90 @@ int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, u
     check(cudaMemcpy(out, dout, nout * sizeof(double), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
     return 0;
 }
+
+// Density filters of the design layer (_ffip.TO_convolve / _transpose,
+// app/ffip.cpp:222-306): a weighted average over the in-bounds part of an
+// odd filter window, and its transpose.  The filter is indexed with the
+// first half-width on both axes, as the reference does
+// (p2(m - i + r0, n - j + r0)); for square filters that is the usual index.
+namespace
+{
+__device__ __forceinline__ void to_window(int i, int j, int n0, int n1, int r0, int r1, int &l0, int &l1, int &u0, int &u1)
+{
+    l0 = max(i - r0, 0);
+    l1 = max(j - r1, 0);
+    u0 = min(i + r0 + 1, n0);
+    u1 = min(j + r1 + 1, n1);
+}
+
+__global__ void k_to_convolve(const double *in1, int n0, int n1, const double *in2, int m1, int r0, int r1, double *out)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)n0 * n1) return;
+    const int i = (int)(t / n1), j = (int)(t % n1);
+    int l0, l1, u0, u1;
+    to_window(i, j, n0, n1, r0, r1, l0, l1, u0, u1);
+    double w = 0, s = 0;
+    for (int m = l0; m < u0; ++m)
+        for (int n = l1; n < u1; ++n)
+        {
+            const double f = in2[(int64_t)(m - i + r0) * m1 + (n - j + r0)];
+            w += f;
+            s += in1[(int64_t)m * n1 + n] * f;
+        }
+    out[t] = s / w;
+}
+
+// transpose, gather form: out(m, n) = sum over (i, j) whose window holds
+// (m, n) of in1(i, j) f(m - i + r0, n - j + r0) / w(i, j)
+__global__ void k_to_convolve_t(const double *in1, int n0, int n1, const double *in2, int m1, int r0, int r1, double *out)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)n0 * n1) return;
+    const int m = (int)(t / n1), n = (int)(t % n1);
+    double s = 0;
+    for (int i = max(m - r0, 0); i < min(m + r0 + 1, n0); ++i)
+        for (int j = max(n - r1, 0); j < min(n + r1 + 1, n1); ++j)
+        {
+            int l0, l1, u0, u1;
+            to_window(i, j, n0, n1, r0, r1, l0, l1, u0, u1);
+            double w = 0;
+            for (int a = l0; a < u0; ++a)
+                for (int b = l1; b < u1; ++b) w += in2[(int64_t)(a - i + r0) * m1 + (b - j + r0)];
+            s += in1[(int64_t)i * n1 + j] * in2[(int64_t)(m - i + r0) * m1 + (n - j + r0)] / w;
+        }
+    out[t] = s;
+}
+} // namespace
+
+int to_convolve(const double *in1, int n0, int n1, const double *in2, int m0, int m1, double *out, int transpose)
+{
+    if (n0 < 0 || n1 < 0 || m0 < 1 || m1 < 1) throw std::invalid_argument("bad array shape");
+    if (m0 % 2 == 0 || m1 % 2 == 0) throw std::invalid_argument("filter shape is not odd");
+    const int r0 = m0 / 2, r1 = m1 / 2;
+    // the reference indexes both filter axes with the first half-width
+    // (app/ffip.cpp:255): only equal half-widths stay inside the filter
+    if (r0 != r1) throw std::invalid_argument("filters with different half-widths are not supported");
+    const int64_t n = (int64_t)n0 * n1;
+    if (!n) return 0;
+    std::vector<double *> keep;
+    try
+    {
+        double *d1 = to_device(in1, n, keep), *d2 = to_device(in2, (uint64_t)m0 * m1, keep);
+        double *dout = nullptr;
+        check(cudaMalloc(&dout, n * sizeof(double)), "cudaMalloc");
+        keep.push_back(dout);
+        if (transpose) k_to_convolve_t<<<(unsigned)((n + 255) / 256), 256>>>(d1, n0, n1, d2, m1, r0, r1, dout);
+        else k_to_convolve<<<(unsigned)((n + 255) / 256), 256>>>(d1, n0, n1, d2, m1, r0, r1, dout);
+        check(cudaGetLastError(), "to_convolve launch");
+        check(cudaMemcpy(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    }
+    catch (...)
+    {
+        for (double *p : keep) cudaFree(p);
+        throw;
+    }
+    for (double *p : keep) cudaFree(p);
+    return 0;
+}
 } // namespace ffipg

@@ -22,6 +22,7 @@ int adjoint_sensitivity(double w_re, double w_im, double norm_re, double norm_im
 int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
                               const double *pt, uint64_t npts, double *out);
 uint64_t adjoint_transpose_noalloc_capacity();
+int to_convolve(const double *in1, int n0, int n1, const double *in2, int m0, int m1, double *out, int transpose);
 int sg_gemm(int M, int N, int K, const void *A, int64_t ars, int64_t acs, const void *B, int64_t brs, int64_t bcs, float *C,
             int64_t crs, int64_t ccs, const float *bias, int accumulate, void *stream);
 int sg_im2col(const void *x, const int *shape, const int *kernel, const int *stride, const int *pad, void *cols, void *stream);
@@ -276,6 +277,17 @@ int ffip_sensitivity(double w_re, double w_im, double norm_re, double norm_im, c
         if (!gx || !gy || !gz || !out || (n && (!fwd || !adj || !deps || !xyz))) return fail(FFIP_ERR_INVALID, "null argument");
         if (nx < 1 || ny < 1 || nz < 1) return fail(FFIP_ERR_INVALID, "some grid size is 0");
         return ffipg::adjoint_sensitivity(w_re, w_im, norm_re, norm_im, fwd, adj, deps, xyz, n, gx, nx, gy, ny, gz, nz, out);
+    });
+}
+
+int ffip_to_convolve(const double *in1, uint64_t n0, uint64_t n1, const double *in2, uint64_t m0, uint64_t m1, double *out,
+                     int transpose)
+{
+    return guard([&]() -> int {
+        if (!out || (n0 * n1 && !in1) || !in2) return fail(FFIP_ERR_INVALID, "null argument");
+        if (n0 > (1u << 30) || n1 > (1u << 30) || m0 > (1u << 30) || m1 > (1u << 30))
+            return fail(FFIP_ERR_INVALID, "array too large");
+        return ffipg::to_convolve(in1, (int)n0, (int)n1, in2, (int)m0, (int)m1, out, transpose);
     });
 }
 

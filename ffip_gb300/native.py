@@ -36,7 +36,7 @@ class Stats(ctypes.Structure):
 EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_run", "ffip_output_count", "ffip_output_group", "ffip_output_array",
            "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync", "ffip_stream", "ffip_destroy",
            "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc",
-           "ffip_set_source_data"]
+           "ffip_set_source_data", "ffip_to_convolve"]
 
 
 def _declare(lib):
@@ -59,6 +59,7 @@ def _declare(lib):
     lib.ffip_last_error.restype = ctypes.c_char_p
     lib.ffip_transpose.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
     lib.ffip_transpose_noalloc.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
+    lib.ffip_to_convolve.argtypes = [D, U64, U64, D, U64, U64, D, ctypes.c_int]
     lib.ffip_sensitivity.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, U64,
                                      D, U64, D, U64, D, U64, D]
     for f in EXPORTS:
@@ -234,3 +235,30 @@ def transpose_noalloc(gx, gy, gz, pt, lib=None) -> np.ndarray:
     if rc != 0:
         raise FfipError(L.ffip_last_error().decode())
     return out
+
+
+def _to_convolve(in1, in2, transpose, lib=None):
+    L = lib if lib is not None else load()
+    a = np.ascontiguousarray(np.asarray(in1, dtype=np.float64))
+    f = np.ascontiguousarray(np.asarray(in2, dtype=np.float64))
+    if a.ndim != 2 or f.ndim != 2:
+        raise KeyError("dimensions are not 2")
+    if f.shape[0] % 2 == 0 or f.shape[1] % 2 == 0:
+        raise KeyError("filter shape is not odd")
+    out = np.zeros(a.shape, dtype=np.float64)
+    rc = L.ffip_to_convolve(_dptr(a), a.shape[0], a.shape[1], _dptr(f), f.shape[0], f.shape[1], _dptr(out),
+                            1 if transpose else 0)
+    if rc != 0:
+        raise FfipError(L.ffip_last_error().decode())
+    return out
+
+
+def to_convolve(in1, in2, lib=None) -> np.ndarray:
+    """_ffip.TO_convolve (app/ffip.cpp:222-261) on the GPU."""
+    return _to_convolve(in1, in2, False, lib)
+
+
+def to_convolve_transpose(in1, in2, lib=None) -> np.ndarray:
+    """_ffip.TO_convolve_transpose (app/ffip.cpp:263-306) on the GPU."""
+    return _to_convolve(in1, in2, True, lib)
+

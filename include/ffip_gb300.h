@@ -142,6 +142,16 @@ int ffip_sensitivity(double w_re, double w_im, double norm_re, double norm_im, c
                      const double *deps, const double *xyz, uint64_t n, const double *gx, uint64_t nx,
                      const double *gy, uint64_t ny, const double *gz, uint64_t nz, double *out);
 
+/* _ffip.TO_convolve / _ffip.TO_convolve_transpose (app/ffip.cpp:222-306):
+ * the density filter of the design scripts.  transpose = 0: out[i][j] is the
+ * average of in1 over the in-bounds part of the filter window centred at
+ * (i, j), weighted by the filter in2[m0][m1] (odd sizes); transpose = 1: its
+ * transpose.  in1 and out are n0 x n1, row-major, host buffers.  As in the
+ * reference, both filter axes are indexed with the first half-width, so only
+ * filters with equal half-widths are accepted. */
+int ffip_to_convolve(const double *in1, uint64_t n0, uint64_t n1, const double *in2, uint64_t m0, uint64_t m1, double *out,
+                     int transpose);
+
 /* ffip_transpose without any device allocation.  No counterpart in the
  * reference (its transpose runs on the host).  Same arguments, result and
  * errors as ffip_transpose, but the points and the output grid are staged in

@@ -127,6 +127,10 @@ int adjoint_transpose_noalloc(const double *, uint64_t, const double *, uint64_t
     throw std::runtime_error("not emulated");
 }
 uint64_t adjoint_transpose_noalloc_capacity() { return uint64_t(1) << 20; }
+int to_convolve(const double *, int, int, const double *, int, int, double *, int)
+{
+    throw std::runtime_error("not emulated");
+}
 int sg_gemm(int, int, int, const void *, int64_t, int64_t, const void *, int64_t, int64_t, float *, int64_t, int64_t,
             const float *, int, void *)
 {

@@ -72,3 +72,57 @@ def test_sensitivity_matches_numpy():
                               D(gx), 9, D(gy), 9, D(gz), 3, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     assert rc == 0
     np.testing.assert_allclose(out, ref, rtol=1e-10, atol=1e-12)
+
+
+def to_convolve_ref(in1, in2, transpose=False):
+    """Sequential restatement of app/ffip.cpp:222-306 (both filter axes
+    indexed with the first half-width, as there)."""
+    n0, n1 = in1.shape
+    r0, r1 = in2.shape[0] // 2, in2.shape[1] // 2
+    out = np.zeros_like(in1)
+    for i in range(n0):
+        for j in range(n1):
+            l0, l1, u0, u1 = max(i - r0, 0), max(j - r1, 0), min(i + r0 + 1, n0), min(j + r1 + 1, n1)
+            w = 0.0
+            for m in range(l0, u0):
+                for n in range(l1, u1):
+                    w += in2[m - i + r0, n - j + r0]
+            if not transpose:
+                s = 0.0
+                for m in range(l0, u0):
+                    for n in range(l1, u1):
+                        s += in1[m, n] * in2[m - i + r0, n - j + r0]
+                out[i, j] = s / w
+            else:
+                for m in range(l0, u0):
+                    for n in range(l1, u1):
+                        out[m, n] += in1[i, j] * in2[m - i + r0, n - j + r0] / w
+    return out
+
+
+@pytest.mark.parametrize("transpose", [False, True])
+def test_to_convolve_matches_reference_restatement(transpose):
+    from ffip_gb300 import native
+    rng = np.random.default_rng(11)
+    a = rng.uniform(0, 1, size=(13, 17))
+    f = rng.uniform(0.1, 1, size=(5, 5))
+    got = (native.to_convolve_transpose if transpose else native.to_convolve)(a, f)
+    np.testing.assert_allclose(got, to_convolve_ref(a, f, transpose), rtol=1e-12, atol=1e-14)
+
+
+def test_to_convolve_transpose_is_the_adjoint():
+    from ffip_gb300 import native
+    rng = np.random.default_rng(12)
+    a, b = rng.normal(size=(9, 11)), rng.normal(size=(9, 11))
+    f = rng.uniform(0.1, 1, size=(3, 3))
+    lhs = np.sum(native.to_convolve(a, f) * b)
+    rhs = np.sum(a * native.to_convolve_transpose(b, f))
+    assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+def test_to_convolve_errors():
+    from ffip_gb300 import native
+    with pytest.raises(KeyError):
+        native.to_convolve(np.zeros((3, 3)), np.ones((2, 3)))
+    with pytest.raises(native.FfipError, match="half-widths"):
+        native.to_convolve(np.zeros((3, 3)), np.ones((3, 5)))
