@@ -203,3 +203,27 @@ def test_bad_device_index_is_an_error():
     cfg["device"] = 999
     with pytest.raises(native.FfipError):
         native.NativeSim(cfg, ds)
+
+
+def test_fused_asymmetric_cpml_and_odd_sizes_match_separate_passes():
+    """CPML on some faces only, odd sizes, a monitor and a sphere: the split
+    of the fused pass into CPML / interior jobs and the face layers cover the
+    grid exactly once."""
+    from ffip_gb300 import native
+    cfg = random_config(7, n=20, steps=80)
+    cfg["size"] = [67.0, 41.0, 59.0]
+    cfg["PML"] = [{"thickness": 6.0, "direction": "z", "side": "negative", "k max": 1.0, "sigma max": 3.0, "order": 3},
+                  {"thickness": 9.0, "direction": "x", "k max": 2.0, "sigma max": 2.0, "order": 2}]
+    outs = {}
+    for eng in ("unfused", "fused"):
+        for prec in ("fp64", "fp32"):
+            c = dict(cfg)
+            c["engine"] = eng
+            c["precision"] = prec
+            with native.NativeSim(c) as s:
+                assert s.stats()["fused"] == (1 if eng == "fused" else 0)
+                s.run(c["stop condition"])
+                outs[eng, prec] = flatten(s.outputs())
+    for prec in ("fp64", "fp32"):
+        for k in outs["unfused", prec]:
+            assert np.array_equal(outs["unfused", prec][k], outs["fused", prec][k]), (prec, k)
