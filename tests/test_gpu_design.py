@@ -79,7 +79,7 @@ def grads(rho):
         r = torch.tensor(rho, dtype=torch.float64, requires_grad=True)
         F = DensityObjective.apply(r, prob)
         F.backward()
-        out[key] = (float(F), r.grad.numpy().copy())
+        out[key] = (float(F.detach()), r.grad.numpy().copy())
         prob.release()
     return out
 
