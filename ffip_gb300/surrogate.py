@@ -2,7 +2,7 @@
 a design density to the DFT fields on an output plane, trained on this
 project's own GPU FDTD runs.  The reference has no learned part; this is the
 rebuild's addition for design loops (a cheap proxy that ranks candidate
-design steps, while a full FDTD run judges every accepted step).
+design steps, while a full FDTD run checks every accepted step).
 
 Convolutions run on the project's own kernels (libffip_gb300.so,
 include/ffip_gb300_surrogate.h): im2col, a bf16 tensor-core GEMM with fp32
@@ -389,12 +389,12 @@ def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed
     loops of `iters` accepted iterations that minimise the spot objective
     (maximise the output-plane intensity in the central 8 x 8 cells), both
     stepping along the adjoint gradient:
-      plain:    `candidates` step sizes each judged by a forward FDTD run,
+      plain:    `candidates` step sizes each checked by a forward FDTD run,
                 then the gradient at the best (forward + adjoint runs);
       screened: the surrogate ranks the same step sizes, a forward run
-                judges the best (the second best if it fails), then the
+                checks the best (the second best if it fails), then the
                 adjoint runs.
-    Every accepted step is judged by a full FDTD run in both loops.  Reports
+    Every accepted step is checked by a full FDTD run in both loops.  Reports
     seconds and FDTD runs per accepted iteration."""
     wl = DesignWorkload()
     rho, y, t_gen = generate(designs, seed, wl)
@@ -426,7 +426,7 @@ def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed
             d = -g / max(np.abs(g).max(), 1e-30)
             cands = [np.clip(x + s_ * d, 0, 1) for s_ in steps]
             if mode == "plain":
-                # every candidate judged by a forward run, the best kept
+                # every candidate checked by a forward run, the best kept
                 vals = [prob.forward(c) for c in cands]
                 runs += len(cands)
                 best = int(np.argmin(vals))
@@ -439,7 +439,7 @@ def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed
                 else:
                     steps = steps / 4
             else:
-                # the surrogate ranks the candidates; a forward run judges
+                # the surrogate ranks the candidates; a forward run checks
                 # the best two in turn, and the adjoint runs follow at once
                 pred = predict(net, np.stack(cands), tr["scale"])
                 order = np.argsort([spot_objective(q) for q in pred])
