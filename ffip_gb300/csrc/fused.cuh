@@ -8,13 +8,18 @@
 //   memory by TMA (cp.async.bulk.tensor, one 3-D tensor map per field array)
 //   through two rings completed by mbarriers: E planes (box TY + 2 rows, also
 //   the E values of the E update one iteration later) and H planes (box
-//   TY + 1 rows).  The new H goes into a three-plane ring in shared memory,
+//   TY + 1 rows).  The new H goes into a four-plane ring in shared memory,
 //   on the tile and on the low-x column and low-y row that the tile's E
 //   update needs (those halo points belong to neighbouring CTAs and are
 //   recomputed here, not written).
-//   E(k-1) needs H(k-1) and H(k-2) from that ring, both completed in earlier
-//   iterations, so one block barrier per iteration orders everything: H(k)
-//   writes one ring plane while E(k-1) reads the other two.
+//   E(k-1) needs H(k-1) and H(k-2) from that ring, written by every thread
+//   in earlier iterations.  There is no block barrier in the march: every
+//   thread arrives on a per-ring-plane mbarrier once its H is written, and
+//   waits at the top of iteration q for all threads' H(q-1).  That one wait
+//   orders the ring (with four planes, H(k) overwrites the plane that E read
+//   two iterations ago) and frees the TMA stages for refill (the E stage of
+//   plane q-3, the H stage of plane q-1), while a thread that finished early
+//   can run ahead by an E update.
 // Every field value is read from HBM once and written once per time step.
 // Because neighbouring CTAs read the previous level while this CTA writes the
 // new one, field buffers (and the H-side CPML psi) ping-pong between steps;
@@ -64,7 +69,7 @@ struct FusedShape;
 #define FFIP_FUSED_F32_RPT 1
 #endif
 #ifndef FFIP_FUSED_F32_SE
-#define FFIP_FUSED_F32_SE 5
+#define FFIP_FUSED_F32_SE 6
 #endif
 #ifndef FFIP_FUSED_F32_SH
 #define FFIP_FUSED_F32_SH 3
@@ -76,7 +81,7 @@ struct FusedShape;
 #define FFIP_FUSED_F64_RPT 1
 #endif
 #ifndef FFIP_FUSED_F64_SE
-#define FFIP_FUSED_F64_SE 4
+#define FFIP_FUSED_F64_SE 5
 #endif
 #ifndef FFIP_FUSED_F64_SH
 #define FFIP_FUSED_F64_SH 3
@@ -123,17 +128,17 @@ struct FusedLayout
     static constexpr int H_BYTES = (SH::TY + 1) * SH::BX * (int)sizeof(T);  // one H box
     static constexpr int E_TILE = (E_BYTES + 127) / 128 * 128;
     static constexpr int H_TILE = (H_BYTES + 127) / 128 * 128;
-    static constexpr int E_OFF = 128;  // [0, 128): mbarriers and the wait flag
+    static constexpr int E_OFF = 128;  // [0, 128): mbarriers
     static constexpr int H_OFF = E_OFF + SH::SE * 3 * E_TILE;
     static constexpr int HN_OFF = H_OFF + SH::SH * 3 * H_TILE;
     static constexpr int HN_PLANE = 3 * (SH::TY + 1) * (SH::TX + 1);  // elements of one H ring plane
     static constexpr int NX = SH::TX + 1, NY = SH::TY + 1, NZ = SH::KCH + 2;  // CPML table lengths
-    static constexpr int PML_OFF = (HN_OFF + 3 * HN_PLANE * (int)sizeof(T) + 31) / 32 * 32;
+    static constexpr int PML_OFF = (HN_OFF + 4 * HN_PLANE * (int)sizeof(T) + 31) / 32 * 32;
     static constexpr int PML_BYTES = 2 * (NX + NY + NZ) * (int)sizeof(PmlCoef<T>);  // [axis][parity][n]
     static constexpr int INFO_OFF = PML_OFF + PML_BYTES;
     static constexpr int SMEM = INFO_OFF + NZ * 4;
-    static_assert((SH::SE + SH::SH) * 8 <= 120, "mbarriers do not fit");
-    static_assert(SH::SE >= 4, "E planes q-1, q, q+1 are in use while one more loads");
+    static_assert((SH::SE + SH::SH + 4) * 8 <= 120, "mbarriers do not fit");
+    static_assert(SH::SE >= 5, "E planes q-2 .. q+1 are in use while one more loads");
     static_assert(SH::BX >= SH::XOFF + SH::TX + 1, "TMA box too narrow");
     static_assert((SH::XOFF - 1) * (int)sizeof(T) % 16 == 0, "TMA box start off a 16-byte boundary");
     static_assert(SH::BX * (int)sizeof(T) % 16 == 0, "TMA box width not a multiple of 16 bytes");
@@ -176,6 +181,11 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
 {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
@@ -484,12 +494,13 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     const int NP = k1 - X.k0 + 2;  // planes k0-1 .. k1 (plane p is z = k0 - 1 + p)
     uint64_t *ebar = reinterpret_cast<uint64_t *>(smem);
     uint64_t *hbar = ebar + SE;
-    volatile int *flag = reinterpret_cast<volatile int *>(smem + 120);
+    uint64_t *hd = hbar + SHS;  // per H ring plane: every thread has written its H there
 
     if (tid == 0)
     {
         for (int s = 0; s < SE; ++s) mbar_init(&ebar[s], 1);
         for (int s = 0; s < SHS; ++s) mbar_init(&hbar[s], 1);
+        for (int s = 0; s < 4; ++s) mbar_init(&hd[s], NTH);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
@@ -625,7 +636,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     for (int r = 0; r < RPT; ++r) sl_next[r][0] = sl_next[r][1] = sl_next[r][2] = -1;
     // running ring positions: E stages of planes q-1, q, q+1; H stage of
     // plane q; H ring planes of H(k), H(k-1), H(k-2)
-    int eS = SE - 1, eA = 0, eB = 1 % SE, hA = 0, rn = 0, rp = 2, rpp = 1;
+    int eS = SE - 1, eA = 0, eB = 1 % SE, hA = 0, rn = 0, rp = 3, rpp = 2;
     int idx = own0 + (X.k0 - 1) * sz;
     // iteration q: H at plane k = k0 - 1 + q (q <= NP - 2), E at plane k - 1 (q >= 2)
     for (int q = 0; q < NP; ++q, idx += sz)
@@ -682,37 +693,19 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     if (PE.slot[c].map && ((vb >> c) & 1u)) sl_next[r][c] = PE.slot[c].map[idx + r * sy];
             }
         }
-        if (tid == 0)
-        {
-            bool ok = true;
-            if (q == 0) ok = mbar_wait_bounded(&ebar[0], 0);
-            if (q + 1 < NP) ok = ok && mbar_wait_bounded(&ebar[(q + 1) % SE], ((q + 1) / SE) & 1);
-            if (do_h) ok = ok && mbar_wait_bounded(&hbar[q % SHS], (q / SHS) & 1);
-            *flag = ok ? 1 : 0;
-        }
-        // (A): the planes are visible, and every thread is done with
-        // iteration q-1 (ring plane q % 3 is free, E plane q-2 and H plane
-        // q-1 can be refilled)
-        __syncthreads();
-        if (!*flag)
-        {
-            if (tid == 0)
-            {
-                atomicExch(L.err, 1);
-                for (int p = 0; p < e_issued; ++p) mbar_wait_bounded(&ebar[p % SE], (p / SE) & 1);
-                for (int p = 0; p < h_issued; ++p) mbar_wait_bounded(&hbar[p % SHS], (p / SHS) & 1);
-            }
-            return;
-        }
-        if (tid == 0)
+        // every thread has written H(q-1): the ring plane of H(q-2) is read
+        // and the one of H(k-3) free, the E stage of plane q-3 and the H
+        // stage of plane q-1 are no longer read by anyone
+        bool ok = q == 0 || mbar_wait_bounded(&hd[(q - 1) & 3], ((q - 1) >> 2) & 1);
+        if (tid == 0 && ok)
         {
             bool fence = false;
-            if (q >= 2 && q - 2 + SE < NP)
+            if (q >= 3 && q - 3 + SE < NP)
             {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 fence = true;
-                issue_e(q - 2 + SE);
-                e_issued = q - 1 + SE;
+                issue_e(q - 3 + SE);
+                e_issued = q - 2 + SE;
             }
             if (q >= 1 && q - 1 + SHS <= NP - 2)
             {
@@ -720,6 +713,22 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 issue_h(q - 1 + SHS);
                 h_issued = q + SHS;
             }
+        }
+        if (ok && q == 0) ok = mbar_wait_bounded(&ebar[0], 0);
+        if (ok && q + 1 < NP) ok = mbar_wait_bounded(&ebar[(q + 1) % SE], ((q + 1) / SE) & 1);
+        if (ok && do_h) ok = mbar_wait_bounded(&hbar[q % SHS], (q / SHS) & 1);
+        if (!ok)
+        {
+            // a wait gave up: record it, let thread 0 wait (bounded) for its
+            // copies, and leave; threads still waiting on this CTA's
+            // barriers give up in turn
+            atomicExch(L.err, 1);
+            if (tid == 0)
+            {
+                for (int p = 0; p < e_issued; ++p) mbar_wait_bounded(&ebar[p % SE], (p / SE) & 1);
+                for (int p = 0; p < h_issued; ++p) mbar_wait_bounded(&hbar[p % SHS], (p / SHS) & 1);
+            }
+            return;
         }
         // 1. H(k) at the tile's own points, and the halo the E update of the
         //    next iteration reads: Hz, Hx on the low-y row (warps 7, 6), Hz,
@@ -816,6 +825,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 }
             }
         }
+        mbar_arrive(&hd[q & 3]);
         // 2. E(k-1) on the tile from H(k-1) and H(k-2)
         if (do_e)
         {
@@ -865,7 +875,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         hA = hA + 1 == SHS ? 0 : hA + 1;
         rpp = rp;
         rp = rn;
-        rn = rn == 2 ? 0 : rn + 1;
+        rn = (rn + 1) & 3;
     }
 }
 
