@@ -62,7 +62,10 @@ struct FusedShape;
 // TY tile rows, RPT adjacent rows per thread (8 warps of 32 lanes, warp w
 // owns rows RPT w .. RPT w + RPT - 1); SE / SH: TMA stages of the E / H
 // plane rings; KCH: most z planes per CTA; MINB: CTAs per SM the register
-// budget is sized for (tuning builds may override the defaults).  Tiles start
+// budget is sized for (tuning builds may override the defaults); STAGE_PSI:
+// the CPML instance stages psi in shared memory by cp.async, ahead of use
+// (fp32 only: the fp64 pass is bound by fp64 arithmetic, and there the copy
+// instructions cost more than the latency they hide).  Tiles start
 // at x0 = 1 + TX * bx, so the TMA box starts at x0 - XOFF, a 16-byte
 // boundary, and spans BX >= XOFF + TX + 1 elements (x0 - 1 .. x0 + TX).
 #ifndef FFIP_FUSED_F32_RPT
@@ -103,14 +106,14 @@ struct FusedShape<float>
 {
     static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 5, BX = 40, SE = FFIP_FUSED_F32_SE,
                          SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F32_MINB,
-                         MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR;
+                         MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR, STAGE_PSI = 1;
 };
 template <>
 struct FusedShape<double>
 {
     static constexpr int TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 3, BX = 36, SE = FFIP_FUSED_F64_SE,
                          SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB,
-                         MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR;
+                         MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR, STAGE_PSI = 0;
 };
 
 // CPML coefficients of one position along one axis: b, c, 1/k
@@ -136,7 +139,14 @@ struct FusedLayout
     static constexpr int PML_OFF = (HN_OFF + 4 * HN_PLANE * (int)sizeof(T) + 31) / 32 * 32;
     static constexpr int PML_BYTES = 2 * (NX + NY + NZ) * (int)sizeof(PmlCoef<T>);  // [axis][parity][n]
     static constexpr int INFO_OFF = PML_OFF + PML_BYTES;
-    static constexpr int SMEM = INFO_OFF + NZ * 4;
+    // CPML instance with STAGE_PSI: E-side psi of the own points staged by
+    // cp.async, one slot of 256 elements (one per thread) per
+    // [row][component][axis]
+    static constexpr int PSI_OFF = (INFO_OFF + NZ * 4 + 15) / 16 * 16;
+    static constexpr int PSI_E = 0;
+    static constexpr int PSI_SLOTS = SH::STAGE_PSI ? 6 * SH::RPT : 0;
+    static constexpr int SMEM = PSI_OFF;  // the instance without CPML code
+    static constexpr int SMEM_PML = PSI_OFF + PSI_SLOTS * 256 * (int)sizeof(T);
     static_assert((SH::SE + SH::SH + 4) * 8 <= 120, "mbarriers do not fit");
     static_assert(SH::SE >= 5, "E planes q-2 .. q+1 are in use while one more loads");
     static_assert(SH::BX >= SH::XOFF + SH::TX + 1, "TMA box too narrow");
@@ -216,6 +226,18 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
         "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
         : "memory");
 }
+
+// one element global -> shared, asynchronous (completion per thread:
+// cp_async_wait_all)
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T *dst, const T *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)), "l"(src), "n"((int)sizeof(T)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Per-CTA context of the fused pass
 template <typename T>
@@ -396,17 +418,19 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
 
 // General E(k) at this thread's own point of tile row `row` (E plane qe of
 // the chunk), from the H ring planes rn (plane k) and rp (plane k-1); CPML
-// psi is read and written in place here; sl: material slot indices.
-template <typename T, bool FULL = true>
+// psi is read from the global arrays, or (STAGED) taken from the values ps
+// the caller read from its staging slots, and written back in place here;
+// sl: material slot indices.
+template <typename T, bool FULL = true, bool STAGED = false>
 __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int eS, int rn, int rp, unsigned vb,
-                                              bool pml, bool slots, bool dft, int idx, const int (&sl)[3])
+                                              bool pml, bool slots, int idx, const int (&sl)[3], const T (&ps)[3][2])
 {
     using SH = FusedShape<T>;
     constexpr int BX = SH::BX, TX = SH::TX;
     if (!FULL)
     {
         vb = 63u;
-        slots = dft = false;
+        slots = false;
     }
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PE = F.e;
@@ -425,8 +449,16 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
         {
             const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
             const bool ve = (vb >> c) & 1u;
-            if (ve && ec[a1].c != T(0)) pe[c][0] = PE.psi[c][0][idx];
-            if (ve && ec[a2].c != T(0)) pe[c][1] = PE.psi[c][1][idx];
+            if (STAGED)
+            {
+                pe[c][0] = ps[c][0];
+                pe[c][1] = ps[c][1];
+            }
+            else
+            {
+                if (ve && ec[a1].c != T(0)) pe[c][0] = PE.psi[c][0][idx];
+                if (ve && ec[a2].c != T(0)) pe[c][1] = PE.psi[c][1][idx];
+            }
         }
     }
     const T ide = PE.inv_dx;
@@ -638,6 +670,11 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     // plane q; H ring planes of H(k), H(k-1), H(k-2)
     int eS = SE - 1, eA = 0, eB = 1 % SE, hA = 0, rn = 0, rp = 3, rpp = 2;
     int idx = own0 + (X.k0 - 1) * sz;
+    // psi staging of the CPML instance (fp32): the E-side psi of the own
+    // points of iteration q is copied by cp.async at the top of the
+    // iteration, during the waits and the H update
+    constexpr bool STG = PML && SH::STAGE_PSI;
+    T *pstage = reinterpret_cast<T *>(smem + LY::PSI_OFF) + tid;
     // iteration q: H at plane k = k0 - 1 + q (q <= NP - 2), E at plane k - 1 (q >= 2)
     for (int q = 0; q < NP; ++q, idx += sz)
     {
@@ -656,7 +693,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         const bool lean_e = PML && (we & kInfoLeanE) && !e_slots;
         const bool pml_h = !fast_h && pml_tables && (tile_pml || (wh & kInfoZPml));
         const bool pml_e = !fast_e && pml_tables && (tile_pml || (we & kInfoZPml));
-        const bool dft_h = wh & kInfoDftH, dft_e = we & kInfoDftE;
+        const bool dft_h = wh & kInfoDftH;
         // CPML psi of this iteration's own H points, loaded before the TMA wait
         T ph[RPT][3][2];
 #pragma unroll
@@ -682,6 +719,28 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         }
 #pragma unroll
         for (int r = 0; r < RPT; ++r) sl_next[r][0] = sl_next[r][1] = sl_next[r][2] = -1;
+        // CPML psi of this iteration's own E points (plane k - 1; updated in
+        // place by this thread only), copied during the waits and the H update
+        if (STG && do_e && pml_e)
+        {
+            const T cx = X.tab(0, 0)[lane + 1].c, cz = X.tab(2, 0)[q - 1].c;  // E side (parity 0)
+#pragma unroll
+            for (int r = 0; r < RPT; ++r)
+            {
+                const T ce[3] = {cx, X.tab(1, 0)[r0 + r + 1].c, cz};
+                const unsigned vb = vxy[r] & (we >> kInfoZValidShift);
+#pragma unroll
+                for (int c = 0; c < 3; ++c)
+                {
+                    const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+                    const bool ve = (vb >> c) & 1u;
+                    T *dst = pstage + (LY::PSI_E + (r * 3 + c) * 2) * NTH;
+                    if (ve && ce[a1] != T(0)) cp_async_elem(dst, PE.psi[c][0] + idx_e + r * sy);
+                    if (ve && ce[a2] != T(0)) cp_async_elem(dst + NTH, PE.psi[c][1] + idx_e + r * sy);
+                }
+            }
+        }
+        if (STG) cp_async_commit();
         if (q >= 1 && q <= NP - 2 && (wh & rowmask))
         {
 #pragma unroll
@@ -723,6 +782,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             // copies, and leave; threads still waiting on this CTA's
             // barriers give up in turn
             atomicExch(L.err, 1);
+            cp_async_wait_all();
             if (tid == 0)
             {
                 for (int p = 0; p < e_issued; ++p) mbar_wait_bounded(&ebar[p % SE], (p / SE) & 1);
@@ -855,18 +915,31 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     F.eout[2][idx_e + r * sy] = ez;
                 }
             }
-            else if (lean_e)
-            {
-#pragma unroll
-                for (int r = 0; r < RPT; ++r)
-                    e_own_general<T, false>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false, false, idx_e + r * sy, sl_e[r]);
-            }
             else
             {
+                if (STG && pml_e) cp_async_wait_all();
 #pragma unroll
                 for (int r = 0; r < RPT; ++r)
-                    e_own_general<T>(X, q - 1, r0 + r, eS, rp, rpp, vxy[r] & (we >> kInfoZValidShift), pml_e, e_slots, dft_e,
-                                     idx_e + r * sy, sl_e[r]);
+                {
+                    // staged psi of the own point (stale where the copy was
+                    // skipped, i.e. where it is not used)
+                    T pe[3][2] = {};
+                    if (STG && pml_e)
+                    {
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                        {
+                            pe[c][0] = pstage[(LY::PSI_E + (r * 3 + c) * 2) * NTH];
+                            pe[c][1] = pstage[(LY::PSI_E + (r * 3 + c) * 2 + 1) * NTH];
+                        }
+                    }
+                    if (lean_e)
+                        e_own_general<T, false, STG>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false, idx_e + r * sy, sl_e[r],
+                                                     pe);
+                    else
+                        e_own_general<T, true, STG>(X, q - 1, r0 + r, eS, rp, rpp, vxy[r] & (we >> kInfoZValidShift), pml_e,
+                                                    e_slots, idx_e + r * sy, sl_e[r], pe);
+                }
             }
         }
         eS = eA;
@@ -877,6 +950,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         rp = rn;
         rn = (rn + 1) & 3;
     }
+    if (STG) cp_async_wait_all();
 }
 
 // DFT sums of one side after the fused pass (DFT_Unit::update,

@@ -216,9 +216,11 @@ public:
         static bool attr_set = false;
         if (!attr_set)
         {
-            for (auto fn : {k_fused<T, true>, k_fused<T, false>})
+            for (int pml = 0; pml < 2; ++pml)
             {
-                check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, LY::SMEM), "cudaFuncSetAttribute");
+                const auto fn = pml ? k_fused<T, true> : k_fused<T, false>;
+                check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pml ? LY::SMEM_PML : LY::SMEM),
+                      "cudaFuncSetAttribute");
                 // shared memory before L1: several CTAs of the pass per SM
                 check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared),
                       "cudaFuncSetAttribute");
@@ -290,7 +292,7 @@ public:
         if (J.nb > 0)
         {
             L.jobs = J.dev;
-            k_fused<T, true><<<J.nb, block, LY::SMEM, stream_>>>(L);
+            k_fused<T, true><<<J.nb, block, LY::SMEM_PML, stream_>>>(L);
             check(cudaGetLastError(), "k_fused launch");
             ++n;
         }
