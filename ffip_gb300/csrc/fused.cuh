@@ -45,9 +45,10 @@
 //
 // The per-point arithmetic is the same as the separate H/E kernels
 // (stencil.cuh: pml_term, material_at, dft_point), so both passes give the
-// same bits.  Only thread 0 waits on the mbarriers (bounded); on a timeout it
-// records an error word, waits (bounded) for its outstanding copies, and the
-// whole CTA returns.
+// same bits.  Every mbarrier wait is bounded; a thread whose wait gives up
+// records an error word and returns (thread 0 after waiting, bounded, for its
+// outstanding TMA copies), and the threads still waiting on the CTA's
+// barriers give up in turn.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
