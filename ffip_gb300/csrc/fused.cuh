@@ -67,8 +67,10 @@ struct FusedShape;
 // the CPML instance stages psi in shared memory by cp.async, ahead of use
 // (fp32 only: the fp64 pass is bound by fp64 arithmetic, and there the copy
 // instructions cost more than the latency they hide).  Tiles start
-// at x0 = 1 + TX * bx, so the TMA box starts at x0 - XOFF, a 16-byte
-// boundary, and spans BX >= XOFF + TX + 1 elements (x0 - 1 .. x0 + TX).
+// at x0 = 1 + TX * bx, so the TMA box starts at x0 - XOFF = TX * bx, a
+// 128-byte boundary (a box row then spans the fewest 32-byte sectors), and
+// spans BX >= XOFF + TX + 1 elements (x0 - 1 .. x0 + TX), rounded up to
+// 16 bytes.
 #ifndef FFIP_FUSED_F32_RPT
 #define FFIP_FUSED_F32_RPT 1
 #endif
@@ -105,14 +107,14 @@ struct FusedShape;
 template <>
 struct FusedShape<float>
 {
-    static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 5, BX = 40, SE = FFIP_FUSED_F32_SE,
+    static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 1, BX = 36, SE = FFIP_FUSED_F32_SE,
                          SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F32_MINB,
                          MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR, STAGE_PSI = 1;
 };
 template <>
 struct FusedShape<double>
 {
-    static constexpr int TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 3, BX = 36, SE = FFIP_FUSED_F64_SE,
+    static constexpr int TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 1, BX = 34, SE = FFIP_FUSED_F64_SE,
                          SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB,
                          MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR, STAGE_PSI = 0;
 };
