@@ -141,13 +141,31 @@ public:
     ~CudaBackend() override
     {
         cudaSetDevice(dev_);
+        if (dft_) cudaStreamSynchronize(dft_);
         cudaStreamSynchronize(stream_);
         if (err_) cudaFree(err_);
         for (auto &kv : jobs_) cudaFree(kv.second.dev);
         if (side_) cudaStreamDestroy(side_);
         if (fork_) cudaEventDestroy(fork_);
         if (join_) cudaEventDestroy(join_);
+        if (dft_)
+        {
+            cudaEventDestroy(dft_ready_);
+            cudaEventDestroy(dft_join_);
+            for (cudaEvent_t e : dft_done_) cudaEventDestroy(e);
+            cudaStreamDestroy(dft_);
+        }
         cudaStreamDestroy(stream_);
+    }
+    // The fused pass's DFT sums run on their own stream, beside the next
+    // pass (see fused_t); every other operation of the handle first orders
+    // the handle's stream after them.
+    void join_dft()
+    {
+        if (!dft_pending_) return;
+        check(cudaEventRecord(dft_join_, dft_), "cudaEventRecord");
+        check(cudaStreamWaitEvent(stream_, dft_join_, 0), "cudaStreamWaitEvent");
+        dft_pending_ = false;
     }
     // every entry re-selects the handle's device: calls may come from any thread
     void use() const { check(cudaSetDevice(dev_), "cudaSetDevice"); }
@@ -162,12 +180,14 @@ public:
     void release(void *p) override
     {
         cudaSetDevice(dev_);
+        if (dft_) cudaStreamSynchronize(dft_);
         cudaStreamSynchronize(stream_);
         cudaFree(p);
     }
     void h2d(void *dst, const void *src, size_t bytes) override
     {
         use();
+        join_dft();
         h2d_bytes += bytes;
         check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream_), "cudaMemcpy H2D");
         check(cudaStreamSynchronize(stream_), "h2d sync");
@@ -175,14 +195,21 @@ public:
     void d2h(void *dst, const void *src, size_t bytes) override
     {
         use();
+        join_dft();
         d2h_bytes += bytes;
         check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream_), "cudaMemcpy D2H");
         check(cudaStreamSynchronize(stream_), "d2h sync");
     }
-    void zero(void *p, size_t bytes) override { use(); check(cudaMemsetAsync(p, 0, bytes, stream_), "cudaMemsetAsync"); }
+    void zero(void *p, size_t bytes) override
+    {
+        use();
+        join_dft();
+        check(cudaMemsetAsync(p, 0, bytes, stream_), "cudaMemsetAsync");
+    }
     void sync() override
     {
         use();
+        join_dft();
         check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
         check_err();
     }
@@ -227,6 +254,12 @@ public:
             }
             attr_set = true;
         }
+        // the DFT sums of two passes ago (on dft_) read the output buffers of
+        // this pass
+        const int par = passes_ & 1;
+        if (dft_valid_[par]) check(cudaStreamWaitEvent(stream_, dft_done_[par], 0), "cudaStreamWaitEvent");
+        dft_valid_[par] = false;
+        ++passes_;
         FusedLaunch<T> L;
         for (int c = 0; c < 3; ++c)
         {
@@ -321,17 +354,51 @@ public:
             check(cudaGetLastError(), "k_face launch");
             ++n;
         }
-        // DFT sums of both sides from the new fields
+        // DFT sums of both sides from the new fields.  They read only this
+        // pass's output fields (and, for D/B monitors, the polarisations the
+        // next pass updates in place), so without D/B monitors they run on
+        // their own stream beside the next pass: the next-but-one pass, which
+        // overwrites these buffers, waits for them (above); sources, which
+        // add to the same sums, and every other operation join them first.
+        int64_t total[2] = {0, 0};
+        bool db = false;
         for (int sd = 0; sd < 2; ++sd)
         {
             const SideParams<T> &P = sd == 0 ? p.e : p.h;
-            int64_t total = 0;
-            for (int u = 0; u < P.nunits; ++u) total += P.units[u].npts;
-            if (!total) continue;
+            for (int u = 0; u < P.nunits; ++u)
+            {
+                total[sd] += P.units[u].npts;
+                db = db || P.units[u].is_db;
+            }
+        }
+        cudaStream_t ds = stream_;
+        if (total[0] + total[1] > 0 && !db)
+        {
+            if (!dft_)
+            {
+                check(cudaStreamCreateWithFlags(&dft_, cudaStreamNonBlocking), "cudaStreamCreate");
+                check(cudaEventCreateWithFlags(&dft_ready_, cudaEventDisableTiming), "cudaEventCreate");
+                check(cudaEventCreateWithFlags(&dft_join_, cudaEventDisableTiming), "cudaEventCreate");
+                for (cudaEvent_t &e : dft_done_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+            }
+            check(cudaEventRecord(dft_ready_, stream_), "cudaEventRecord");
+            check(cudaStreamWaitEvent(dft_, dft_ready_, 0), "cudaStreamWaitEvent");
+            ds = dft_;
+        }
+        for (int sd = 0; sd < 2; ++sd)
+        {
+            if (!total[sd]) continue;
+            const SideParams<T> &P = sd == 0 ? p.e : p.h;
             T *const *f = sd == 0 ? p.eout : p.hout;
-            k_dft<T><<<(unsigned)((total + 255) / 256), 256, 0, stream_>>>(P, f[0], f[1], f[2], total);
+            k_dft<T><<<(unsigned)((total[sd] + 255) / 256), 256, 0, ds>>>(P, f[0], f[1], f[2], total[sd]);
             check(cudaGetLastError(), "k_dft launch");
             ++n;
+        }
+        if (ds == dft_)
+        {
+            check(cudaEventRecord(dft_done_[par], dft_), "cudaEventRecord");
+            dft_valid_[par] = true;
+            dft_pending_ = true;
         }
         return n;
     }
@@ -436,6 +503,7 @@ public:
     void check_err()
     {
         if (!err_) return;
+        join_dft();
         int e = 0;
         check(cudaMemcpyAsync(&e, err_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "cudaMemcpy err flag");
         check(cudaStreamSynchronize(stream_), "sync");
@@ -447,6 +515,7 @@ public:
     {
         if (!p.npts) return;
         use();
+        join_dft();
         k_sources<T><<<(p.npts + 127) / 128, 128, 0, stream_>>>(p);
         check(cudaGetLastError(), "k_sources launch");
     }
@@ -463,6 +532,7 @@ public:
             mv = max(mv, p.faces[f].v1);
         }
         use();
+        join_dft();
         dim3 block(32, 8);
         dim3 grid((mu + 31) / 32, (mv + 7) / 8, p.nfaces);
         k_ghosts<T><<<grid, block, 0, stream_>>>(p);
@@ -486,6 +556,7 @@ public:
     void dft_norm(const double *re, const double *im, int64_t n, double *out) override
     {
         use();
+        join_dft();
         k_dft_norm<<<1, 256, 0, stream_>>>(re, im, n, out);
         check(cudaGetLastError(), "k_dft_norm launch");
     }
@@ -501,6 +572,7 @@ public:
         {
             check(cudaEventRecord(a, stream_), "cudaEventRecord");
             f();
+            join_dft();
             check(cudaEventRecord(b, stream_), "cudaEventRecord");
             check(cudaEventSynchronize(b), "cudaEventSynchronize");
             check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
@@ -516,7 +588,13 @@ public:
         cudaEventDestroy(b);
         return ms;
     }
-    cudaStream_t stream() const { return stream_; }
+    // the handle's stream, ordered after the DFT sums already issued
+    cudaStream_t stream()
+    {
+        use();
+        join_dft();
+        return stream_;
+    }
 
 private:
     cudaStream_t stream_{nullptr};
@@ -527,6 +605,12 @@ private:
     cudaStream_t side_{nullptr};
     int nsm_{0};
     cudaEvent_t fork_{nullptr}, join_{nullptr};
+    // DFT sums of the fused pass: their stream, the event they wait for, the
+    // event after them per pass parity, and a join event
+    cudaStream_t dft_{nullptr};
+    cudaEvent_t dft_ready_{nullptr}, dft_join_{nullptr}, dft_done_[2]{nullptr, nullptr};
+    bool dft_valid_[2]{false, false}, dft_pending_{false};
+    int64_t passes_{0};
 };
 } // namespace
 
