@@ -228,6 +228,146 @@ int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, u
     return 0;
 }
 
+// _ffip.check_inside (app/ffip.cpp:353-387): for each query point, whether
+// it lies strictly inside a 2-D polygon (CGAL Polygon_2::bounded_side ==
+// ON_BOUNDED_SIDE with the Exact_predicates_inexact_constructions_kernel,
+// CGAL >= 4.11).  Points on an edge or a vertex are not inside.  The test is
+// a crossing count along +x with exact predicates: a point on an edge (exact
+// orientation 0 inside the edge's bounding box) is on the boundary; otherwise
+// every edge whose end points straddle the point's y (one end above, the other
+// not) and passes to the right of it flips the parity.  The orientation sign
+// is exact: Shewchuk's orient2d error-bound filter ("Adaptive Precision
+// Floating-Point Arithmetic and Fast Robust Geometric Predicates", 1997), and
+// where the filter cannot decide, the determinant expanded into six products
+// of coordinates, each split exactly by fma, summed into a nonoverlapping
+// expansion (grow-expansion) whose largest component gives the sign.  Exact
+// as long as no product of two coordinates overflows or falls below 2^-969
+// in magnitude (zero is fine).  For a simple polygon, with or without its
+// first vertex repeated at the end, this is CGAL's answer; fewer than three
+// distinct vertices give no inside points.
+namespace
+{
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e)
+{
+    s = __dadd_rn(a, b);
+    const double bv = __dsub_rn(s, a);
+    const double av = __dsub_rn(s, bv);
+    e = __dadd_rn(__dsub_rn(a, av), __dsub_rn(b, bv));
+}
+
+// sign of (ax - cx)(by - cy) - (ay - cy)(bx - cx): > 0 when a, b, c turn
+// counter-clockwise
+__device__ int orient2d_sign(double ax, double ay, double bx, double by, double cx, double cy)
+{
+    const double detleft = __dmul_rn(__dsub_rn(ax, cx), __dsub_rn(by, cy));
+    const double detright = __dmul_rn(__dsub_rn(ay, cy), __dsub_rn(bx, cx));
+    const double det = __dsub_rn(detleft, detright);
+    double detsum;
+    if (detleft > 0)
+    {
+        if (detright <= 0) return (det > 0) - (det < 0);
+        detsum = __dadd_rn(detleft, detright);
+    }
+    else if (detleft < 0)
+    {
+        if (detright >= 0) return (det > 0) - (det < 0);
+        detsum = __dsub_rn(-detleft, detright);
+    }
+    else
+        return (det > 0) - (det < 0);
+    // (3 + 16 eps) eps, eps = 2^-53
+    const double bound = __dmul_rn((3.0 + 16.0 * 0x1p-53) * 0x1p-53, detsum);
+    if (det >= bound || -det >= bound) return (det > 0) - (det < 0);
+    // exact: ax by - ax cy - cx by - ay bx + ay cx + cy bx (the cx cy terms
+    // cancel); each product is hi + lo exactly
+    const double fa[6] = {ax, -ax, -cx, -ay, ay, cy};
+    const double fb[6] = {by, cy, by, bx, cx, bx};
+    double h[12];
+#pragma unroll
+    for (int t = 0; t < 12; ++t)
+    {
+        const double p = __dmul_rn(fa[t / 2], fb[t / 2]);
+        double q = (t & 1) ? fma(fa[t / 2], fb[t / 2], -p) : p;
+        // grow the expansion h[0 .. t-1] by q
+#pragma unroll
+        for (int i = 0; i < t; ++i)
+        {
+            double s, e;
+            two_sum(q, h[i], s, e);
+            h[i] = e;
+            q = s;
+        }
+        h[t] = q;
+    }
+#pragma unroll
+    for (int i = 11; i >= 0; --i)
+        if (h[i] != 0) return h[i] > 0 ? 1 : -1;
+    return 0;
+}
+
+constexpr int kPolyChunk = 2048;  // polygon vertices staged in shared memory per pass
+
+__global__ void __launch_bounds__(256) k_check_inside(const double2 *req, long long n, const double2 *poly, long long m,
+                                                      unsigned char *out)
+{
+    __shared__ double2 v[kPolyChunk + 1];
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    const bool live = t < n;
+    const double2 q = live ? req[t] : make_double2(0, 0);
+    bool inside = false, boundary = false;
+    for (long long c0 = 0; c0 < m; c0 += kPolyChunk)
+    {
+        const int len = (int)min((long long)kPolyChunk, m - c0);
+        __syncthreads();
+        for (int i = threadIdx.x; i <= len; i += blockDim.x) v[i] = poly[(c0 + i) % m];
+        __syncthreads();
+        if (!live || boundary) continue;
+        for (int i = 0; i < len; ++i)
+        {
+            const double2 a = v[i], b = v[i + 1];
+            const bool straddle = (a.y > q.y) != (b.y > q.y);
+            const bool in_box = fmin(a.x, b.x) <= q.x && q.x <= fmax(a.x, b.x) && fmin(a.y, b.y) <= q.y && q.y <= fmax(a.y, b.y);
+            if (!straddle && !in_box) continue;
+            const int o = orient2d_sign(a.x, a.y, b.x, b.y, q.x, q.y);
+            if (o == 0 && in_box)
+            {
+                boundary = true;
+                break;
+            }
+            // the edge crosses y = q.y to the right of q: q is left of the
+            // edge directed upwards
+            if (straddle && (b.y > a.y ? o > 0 : o < 0)) inside = !inside;
+        }
+    }
+    if (live) out[t] = (inside && !boundary) ? 1 : 0;
+}
+} // namespace
+
+int check_inside(const double *req, uint64_t n, const double *poly, uint64_t m, unsigned char *out)
+{
+    if (!n) return 0;
+    std::vector<double *> keep;
+    unsigned char *dout = nullptr;
+    try
+    {
+        double *dq = to_device(req, 2 * n, keep), *dp = to_device(poly, 2 * m, keep);
+        check(cudaMalloc(&dout, n), "cudaMalloc");
+        k_check_inside<<<(unsigned)((n + 255) / 256), 256>>>(reinterpret_cast<const double2 *>(dq), (long long)n,
+                                                              reinterpret_cast<const double2 *>(dp), (long long)m, dout);
+        check(cudaGetLastError(), "k_check_inside launch");
+        check(cudaMemcpy(out, dout, n, cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
+    }
+    catch (...)
+    {
+        cudaFree(dout);
+        for (double *p : keep) cudaFree(p);
+        throw;
+    }
+    cudaFree(dout);
+    for (double *p : keep) cudaFree(p);
+    return 0;
+}
+
 // Density filters of the design layer (_ffip.TO_convolve / _transpose,
 // app/ffip.cpp:222-306): a weighted average over the in-bounds part of an
 // odd filter window, and its transpose.  The filter is indexed with the

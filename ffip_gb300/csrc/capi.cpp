@@ -23,6 +23,7 @@ int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, u
                               const double *pt, uint64_t npts, double *out);
 uint64_t adjoint_transpose_noalloc_capacity();
 int to_convolve(const double *in1, int n0, int n1, const double *in2, int m0, int m1, double *out, int transpose);
+int check_inside(const double *req, uint64_t n, const double *poly, uint64_t m, unsigned char *out);
 int sg_gemm(int M, int N, int K, const void *A, int64_t ars, int64_t acs, const void *B, int64_t brs, int64_t bcs, float *C,
             int64_t crs, int64_t ccs, const float *bias, int accumulate, void *stream);
 int sg_im2col(const void *x, const int *shape, const int *kernel, const int *stride, const int *pad, void *cols, void *stream);
@@ -288,6 +289,15 @@ int ffip_to_convolve(const double *in1, uint64_t n0, uint64_t n1, const double *
         if (n0 > (1u << 30) || n1 > (1u << 30) || m0 > (1u << 30) || m1 > (1u << 30))
             return fail(FFIP_ERR_INVALID, "array too large");
         return ffipg::to_convolve(in1, (int)n0, (int)n1, in2, (int)m0, (int)m1, out, transpose);
+    });
+}
+
+int ffip_check_inside(const double *req_pts, uint64_t n, const double *poly_pts, uint64_t m, uint8_t *out)
+{
+    return guard([&]() -> int {
+        if ((n && (!req_pts || !out)) || (m && !poly_pts)) return fail(FFIP_ERR_INVALID, "null argument");
+        if (n > (uint64_t(1) << 40) || m > (uint64_t(1) << 40)) return fail(FFIP_ERR_INVALID, "array too large");
+        return ffipg::check_inside(req_pts, n, poly_pts, m, out);
     });
 }
 

@@ -398,6 +398,37 @@ class General_Medium_Box(_DensityBox):
                 "magnetic susceptibility amplitudes dataset": self.m_sus_amp_dataset, "medium": self.medium.get_json()}
 
 
+def planar_polygon(polygon, center=None, height=np.inf):
+    """Density function of an extruded planar polygon (ffip/geom.py:569-590):
+    returns f(req_pts) with req_pts[..., (z, y, x)] giving 1 where (x, y) -
+    center lies strictly inside the polygon (check_inside on the GPU) and
+    |z - center.z| < height / 2, else 0.  `polygon` is a shapely-like object
+    (`.exterior` coordinates, or `.geoms` of several) or an (m, 2) vertex
+    array; several polygons are OR-ed."""
+    from .native import check_inside
+    center = center if center is not None else Vector3()
+
+    def rings(g):
+        if hasattr(g, "geoms"):
+            for h in g.geoms:
+                yield from rings(h)
+        elif hasattr(g, "exterior"):
+            yield np.asarray(g.exterior.coords if hasattr(g.exterior, "coords") else g.exterior, dtype=np.float64)
+        else:
+            yield np.asarray(g, dtype=np.float64)
+
+    def internal(req_pts):
+        req_pts = np.asarray(req_pts, dtype=np.float64)
+        xy = np.stack((req_pts[..., 2] - center.x, req_pts[..., 1] - center.y), axis=-1)
+        z_check = np.abs(req_pts[..., 0] - center.z) < (height / 2)
+        res = np.zeros(req_pts.shape[:-1], dtype=bool)
+        for ring in rings(polygon):
+            res |= check_inside(req_pts=xy, poly_pts=ring) & z_check
+        return res * 1
+
+    return internal
+
+
 def getgrid(center=None, size=None, dim=None):
     center = center if center is not None else Vector3()
     size = size if size is not None else Vector3()

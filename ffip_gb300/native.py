@@ -36,7 +36,7 @@ class Stats(ctypes.Structure):
 EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_run", "ffip_output_count", "ffip_output_group", "ffip_output_array",
            "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync", "ffip_stream", "ffip_destroy",
            "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc",
-           "ffip_set_source_data", "ffip_to_convolve"]
+           "ffip_set_source_data", "ffip_to_convolve", "ffip_check_inside"]
 
 
 def _declare(lib):
@@ -60,6 +60,7 @@ def _declare(lib):
     lib.ffip_transpose.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
     lib.ffip_transpose_noalloc.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
     lib.ffip_to_convolve.argtypes = [D, U64, U64, D, U64, U64, D, ctypes.c_int]
+    lib.ffip_check_inside.argtypes = [D, U64, D, U64, ctypes.POINTER(ctypes.c_uint8)]
     lib.ffip_sensitivity.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, U64,
                                      D, U64, D, U64, D, U64, D]
     for f in EXPORTS:
@@ -256,6 +257,28 @@ def _to_convolve(in1, in2, transpose, lib=None):
 def to_convolve(in1, in2, lib=None) -> np.ndarray:
     """_ffip.TO_convolve (app/ffip.cpp:222-261) on the GPU."""
     return _to_convolve(in1, in2, False, lib)
+
+
+def check_inside(req_pts, poly_pts, lib=None) -> np.ndarray:
+    """_ffip.check_inside (app/ffip.cpp:353-387) on the GPU: for points
+    req_pts[..., 2], whether each lies strictly inside the polygon
+    poly_pts[..., 2] (CGAL bounded_side == ON_BOUNDED_SIDE; points on the
+    boundary are not inside).  Returns bool of shape req_pts.shape[:-1]; the
+    same ValueErrors as the reference for bad shapes."""
+    L = lib if lib is not None else load()
+    q = np.ascontiguousarray(np.asarray(req_pts, dtype=np.float64))
+    p = np.ascontiguousarray(np.asarray(poly_pts, dtype=np.float64))
+    if q.ndim < 2 or p.ndim < 2:
+        raise ValueError("ndim is not bigger than 1")
+    if q.shape[-1] != 2:
+        raise ValueError("req_pts.shape[-1] is not 2")
+    if p.shape[-1] != 2:
+        raise ValueError("poly_pts.shape[-1] is not 2")
+    out = np.zeros(q.shape[:-1], dtype=np.uint8)
+    rc = L.ffip_check_inside(_dptr(q), q.size // 2, _dptr(p), p.size // 2, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)))
+    if rc != 0:
+        raise FfipError(L.ffip_last_error().decode())
+    return out.astype(bool)
 
 
 def to_convolve_transpose(in1, in2, lib=None) -> np.ndarray:

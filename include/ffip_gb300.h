@@ -152,6 +152,15 @@ int ffip_sensitivity(double w_re, double w_im, double norm_re, double norm_im, c
 int ffip_to_convolve(const double *in1, uint64_t n0, uint64_t n1, const double *in2, uint64_t m0, uint64_t m1, double *out,
                      int transpose);
 
+/* _ffip.check_inside (app/ffip.cpp:353-387): out[i] = 1 when query point i,
+ * (req_pts[2i], req_pts[2i+1]), lies strictly inside the polygon of m
+ * vertices (poly_pts[2j], poly_pts[2j+1]) -- CGAL's Polygon_2::bounded_side
+ * == ON_BOUNDED_SIDE -- and 0 on an edge, on a vertex or outside.  The polygon
+ * is simple; its first vertex may be repeated at the end (a closed ring).
+ * Orientation tests are exact.  Host buffers; computed on the current CUDA
+ * device. */
+int ffip_check_inside(const double *req_pts, uint64_t n, const double *poly_pts, uint64_t m, uint8_t *out);
+
 /* ffip_transpose without any device allocation.  No counterpart in the
  * reference (its transpose runs on the host).  Same arguments, result and
  * errors as ffip_transpose, but the points and the output grid are staged in

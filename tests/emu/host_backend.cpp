@@ -131,6 +131,10 @@ int to_convolve(const double *, int, int, const double *, int, int, double *, in
 {
     throw std::runtime_error("not emulated");
 }
+int check_inside(const double *, uint64_t, const double *, uint64_t, unsigned char *)
+{
+    throw std::runtime_error("not emulated");
+}
 int sg_gemm(int, int, int, const void *, int64_t, int64_t, const void *, int64_t, int64_t, float *, int64_t, int64_t,
             const float *, int, void *)
 {
