@@ -168,6 +168,8 @@ constexpr unsigned kInfoFastH = 1u << 25;  // H of this tile plane takes the pla
 constexpr unsigned kInfoFastE = 1u << 26;  // E of this tile plane takes the plain path (rows without slots)
 constexpr unsigned kInfoLeanH = 1u << 27;  // H: CPML, but every point valid, no slot, no DFT unit
 constexpr unsigned kInfoLeanE = 1u << 28;  // E: CPML, but every point valid, no DFT unit (rows without slots)
+constexpr unsigned kInfoZeroCol = 1u << 29;  // the low-x halo column holds no grid point (the same in every plane word)
+constexpr unsigned kInfoZeroRow = 1u << 30;  // the low-y halo row holds no grid point (the same in every plane word)
 
 template <typename T>
 struct FusedLaunch
@@ -641,12 +643,23 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 if (x >= PH.vlo[c][0] && x <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1]) vxy[r] |= 1u << (3 + c);
             }
     }
-    // every own and halo point of the tile valid in x and y for all six components
+    // the low-x halo column / low-y halo row holds no grid point of any
+    // component (the ghost layer below the first tile): the plain path takes
+    // its new H as zero, as the general path does
+    bool zcol = true, zrow = true;
+    for (int c = 0; c < 3; ++c)
+    {
+        zcol = zcol && X.x0 - 1 < PE.vlo[c][0] && X.x0 - 1 < PH.vlo[c][0];
+        zrow = zrow && X.y0 - 1 < PE.vlo[c][1] && X.y0 - 1 < PH.vlo[c][1];
+    }
+    // every own point of the tile valid in x and y for all six components,
+    // and every halo point too unless its whole column / row is the ghost layer
     bool inside = X.x0 + TX <= L.xlim && X.y0 + TY <= L.ylim;
     for (int c = 0; c < 3; ++c)
-        inside = inside && PE.vlo[c][0] <= X.x0 - 1 && X.x0 + TX - 1 <= PE.vhi[c][0] && PE.vlo[c][1] <= X.y0 - 1 &&
-                 X.y0 + TY - 1 <= PE.vhi[c][1] && PH.vlo[c][0] <= X.x0 - 1 && X.x0 + TX - 1 <= PH.vhi[c][0] &&
-                 PH.vlo[c][1] <= X.y0 - 1 && X.y0 + TY - 1 <= PH.vhi[c][1];
+        inside = inside && PE.vlo[c][0] <= X.x0 - (zcol ? 0 : 1) && X.x0 + TX - 1 <= PE.vhi[c][0] &&
+                 PE.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PE.vhi[c][1] &&
+                 PH.vlo[c][0] <= X.x0 - (zcol ? 0 : 1) && X.x0 + TX - 1 <= PH.vhi[c][0] &&
+                 PH.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PH.vhi[c][1];
     // per plane: may each side take the plain path
     for (int o = tid; o < LY::NZ; o += NTH)
     {
@@ -654,7 +667,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         const bool zpml = pml_tables && (tile_pml || (w & kInfoZPml));
         const bool hok = inside && !h_slots && !(w & kInfoDftH) && ((w >> (kInfoZValidShift + 3)) & 7u) == 7u;
         const bool eok = inside && !(w & kInfoDftE) && ((w >> kInfoZValidShift) & 7u) == 7u;
-        info[o] |= (hok ? (zpml ? kInfoLeanH : kInfoFastH) : 0u) | (eok ? (zpml ? kInfoLeanE : kInfoFastE) : 0u);
+        info[o] |= (hok ? (zpml ? kInfoLeanH : kInfoFastH) : 0u) | (eok ? (zpml ? kInfoLeanE : kInfoFastE) : 0u) |
+                   (zcol ? kInfoZeroCol : 0u) | (zrow ? kInfoZeroRow : 0u);
     }
     __syncthreads();
     const int sz = (int)PE.sz, sy = (int)PE.sy;
@@ -844,18 +858,22 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 {
                     const int o = lane + XOFF;  // row y0 - 1 of the boxes
                     if (wid == 7)
-                        X.hn_at(rn, 2, 0, lane + 1) = X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
+                        X.hn_at(rn, 2, 0, lane + 1) =
+                            (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
                     else
-                        X.hn_at(rn, 0, 0, lane + 1) = X.h_tile(hA, 0)[o] + coefH * ((gA2[o] - gA2[o + BX]) * idh - (gA1[o] - gB1[o]) * idh);
+                        X.hn_at(rn, 0, 0, lane + 1) =
+                            (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 0)[o] + coefH * ((gA2[o] - gA2[o + BX]) * idh - (gA1[o] - gB1[o]) * idh);
                 }
                 else if (wid == 5 && lane < 2 * TY)
                 {
                     const int v = lane < TY ? lane : lane - TY;
                     const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
                     if (lane < TY)
-                        X.hn_at(rn, 2, v + 1, 0) = X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
+                        X.hn_at(rn, 2, v + 1, 0) =
+                            (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
                     else
-                        X.hn_at(rn, 1, v + 1, 0) = X.h_tile(hA, 1)[o] + coefH * ((gA0[o] - gB0[o]) * idh - (gA2[o] - gA2[o + 1]) * idh);
+                        X.hn_at(rn, 1, v + 1, 0) =
+                            (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 1)[o] + coefH * ((gA0[o] - gB0[o]) * idh - (gA2[o] - gA2[o + 1]) * idh);
                 }
             }
             else
