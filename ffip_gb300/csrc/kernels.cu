@@ -107,6 +107,12 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
+// shared-memory carveout of the fused pass in percent of the maximum; -1:
+// sized from the instances' shared memory (tuning builds may override it)
+#ifndef FFIP_FUSED_CARVEOUT
+#define FFIP_FUSED_CARVEOUT -1
+#endif
+
 // 3-D tiled map over one (Mx_pad, My, Mz) field array with a box of
 // (bx, by, 1) elements; out-of-range boxes fill zeros.
 template <typename T>
@@ -243,14 +249,24 @@ public:
         static bool attr_set = false;
         if (!attr_set)
         {
+            // shared memory for the CTAs per SM each instance is built for
+            // (plus the 1 KB the system reserves per CTA), the same carveout
+            // for both so that they share SMs; the rest of the unified
+            // L1/shared array stays L1 (about 60 KB instead of 28 KB in fp32),
+            // which the psi staging, the slot loads and the small pole tables
+            // go through
+            int maxsm = 0;
+            check(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev_), "cudaDeviceGetAttribute");
+            const int64_t need = std::max<int64_t>((int64_t)SH::MINB * (LY::SMEM_PML + 1024),
+                                                   (int64_t)SH::MINB_INTERIOR * (LY::SMEM + 1024));
+            const int carve = FFIP_FUSED_CARVEOUT >= 0 ? FFIP_FUSED_CARVEOUT
+                                                       : (int)std::min<int64_t>(100, (need * 100 + maxsm - 1) / std::max(maxsm, 1));
             for (int pml = 0; pml < 2; ++pml)
             {
                 const auto fn = pml ? k_fused<T, true> : k_fused<T, false>;
                 check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pml ? LY::SMEM_PML : LY::SMEM),
                       "cudaFuncSetAttribute");
-                // shared memory before L1: several CTAs of the pass per SM
-                check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared),
-                      "cudaFuncSetAttribute");
+                check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve), "cudaFuncSetAttribute");
             }
             attr_set = true;
         }
