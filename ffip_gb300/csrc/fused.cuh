@@ -161,7 +161,7 @@ struct FusedLayout
 // per-plane flag word (one per plane of the chunk, shared memory); bits
 // 0..TY-1: tile row r holds E material slots
 constexpr unsigned kInfoZValidShift = 16;  // bits 16..21: component c valid at this z
-constexpr unsigned kInfoZPml = 1u << 22;   // CPML along z at this plane (either parity)
+constexpr unsigned kInfoZPml = 1u << 22;   // CPML at this tile plane: along z (either parity), or the tile's x / y
 constexpr unsigned kInfoDftE = 1u << 23;   // an E DFT unit meets this tile plane
 constexpr unsigned kInfoDftH = 1u << 24;   // an H DFT unit meets this tile plane
 constexpr unsigned kInfoFastH = 1u << 25;  // H of this tile plane takes the plain path
@@ -241,6 +241,59 @@ __device__ __forceinline__ void cp_async_elem(T *dst, const T *src)
 }
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// Loads of the pass's small per-launch metadata (CTA jobs, CPML tables, slot
+// row ranges) with an L2 evict-last policy, so that the field streaming of one
+// step does not push them out of L2 before the next step reads them again
+__device__ __forceinline__ uint64_t l2_keep_policy()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ int4 ld_keep(const int4 *a, uint64_t pol)
+{
+    int4 v;
+    asm volatile("ld.global.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int2 ld_keep(const int2 *a, uint64_t pol)
+{
+    int2 v;
+    asm volatile("ld.global.L2::cache_hint.v2.s32 {%0, %1}, [%2], %3;" : "=r"(v.x), "=r"(v.y) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_keep(const float *a, uint64_t pol)
+{
+    float v;
+    asm volatile("ld.global.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ld_keep(const double *a, uint64_t pol)
+{
+    double v;
+    asm volatile("ld.global.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
+// barrier 1 over warps 1..7 (224 threads) of the CTA, plain and with an OR
+// reduction; warp 0 meanwhile issues the first TMA copies
+__device__ __forceinline__ void bar_warps_1_7() { asm volatile("bar.sync 1, 224;" ::: "memory"); }
+__device__ __forceinline__ bool bar_warps_1_7_or(bool v)
+{
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, 224, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)v)
+        : "memory");
+    return r != 0;
+}
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
@@ -523,7 +576,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     FusedCtx<T> X;
     X.smem = smem;
     X.L = &L;
-    const int4 job = L.jobs[blockIdx.x];
+    const uint64_t keep = l2_keep_policy();
+    const int4 job = ld_keep(L.jobs + blockIdx.x, keep);
     X.x0 = job.x;
     X.y0 = job.y;
     X.k0 = job.z;
@@ -555,16 +609,28 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             tma_load_3d(smem + LY::H_OFF + (st * 3 + c) * LY::H_TILE, &L.tm_h[c], X.x0 - XOFF, X.y0 - 1, X.k0 - 1 + p,
                         &hbar[st]);
     };
-    // E planes 0 .. NP-1 are used; H planes 0 .. NP-2
+    // E planes 0 .. NP-1 are used; H planes 0 .. NP-2.  Warp 0 issues the
+    // first copies, the planes the first iterations wait for first (E0, E1,
+    // H0, E2, H1, ...), while warps 1..7 stage the tables and flag words
+    // below (barrier 1 among themselves); everyone meets at the end.
     int e_issued = min(SE, NP), h_issued = min(SHS, NP - 1);
     if (tid == 0)
     {
-        for (int p = 0; p < e_issued; ++p) issue_e(p);
-        for (int p = 0; p < h_issued; ++p) issue_h(p);
+        int pe = 0, ph = 0;
+        while (pe < e_issued || ph < h_issued)
+        {
+            if (pe < e_issued && (pe <= ph + 1 || ph >= h_issued)) issue_e(pe++);
+            else issue_h(ph++);
+        }
     }
-
-    // stage the CPML tables of this tile / chunk while the first planes load
     const bool pml_tables = PML && PE.pc[0][0] != nullptr;
+    constexpr int PT = NTH - 32;   // threads of warps 1..7
+    const int pt = tid - 32;        // this thread's index among them (< 0 in warp 0)
+    unsigned *info = reinterpret_cast<unsigned *>(smem + LY::INFO_OFF);
+    const bool h_slots = PH.slot[0].map || PH.slot[1].map || PH.slot[2].map;
+    if (wid > 0)
+    {
+    // stage the CPML tables of this tile / chunk while the first planes load
     bool tile_pml = false;
     if (pml_tables)
     {
@@ -573,24 +639,23 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             const int n = a == 0 ? LY::NX : a == 1 ? LY::NY : LY::NZ;
             const int first = a == 0 ? X.x0 - 1 : a == 1 ? X.y0 - 1 : X.k0 - 1;
             const int len = a == 0 ? L.xend : a == 1 ? PE.My : PE.Mz;  // table lengths (x: valid extent, not the padded row)
-            for (int t = tid; t < 2 * n; t += NTH)
+            for (int t = pt; t < 2 * n; t += PT)
             {
                 const int q = t / n, o = t % n, pos = first + o;
                 const bool in = pos >= 0 && pos < len;
                 PmlCoef<T> e;
-                e.b = in ? PE.pb[a][q][pos] : T(0);
-                e.c = in ? PE.pc[a][q][pos] : T(0);
-                e.ik = in ? PE.pik[a][q][pos] : T(1);
+                e.b = in ? ld_keep(PE.pb[a][q] + pos, keep) : T(0);
+                e.c = in ? ld_keep(PE.pc[a][q] + pos, keep) : T(0);
+                e.ik = in ? ld_keep(PE.pik[a][q] + pos, keep) : T(1);
                 e.pad = T(0);
                 X.tab(a, q)[o] = e;
                 if (a < 2 && e.c != T(0)) tile_pml = true;
             }
         }
     }
-    // per plane of the chunk: flag word (z validity, z CPML, DFT units
-    // meeting the tile plane, tile rows with E material slots)
-    unsigned *info = reinterpret_cast<unsigned *>(smem + LY::INFO_OFF);
-    for (int o = tid; o < LY::NZ; o += NTH)
+    // per plane of the chunk: flag word (z validity, CPML at the tile plane,
+    // DFT units meeting the tile plane, tile rows with E material slots)
+    for (int o = pt; o < LY::NZ; o += PT)
     {
         const int k = X.k0 - 1 + o;
         unsigned w = 0;
@@ -599,7 +664,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             if (k >= PE.vlo[c][2] && k <= PE.vhi[c][2]) w |= 1u << (kInfoZValidShift + c);
             if (k >= PH.vlo[c][2] && k <= PH.vhi[c][2]) w |= 1u << (kInfoZValidShift + 3 + c);
         }
-        if (pml_tables && k >= 0 && k < PE.Mz && (PE.pc[2][0][k] != T(0) || PE.pc[2][1][k] != T(0))) w |= kInfoZPml;
+        if (pml_tables && k >= 0 && k < PE.Mz && (ld_keep(PE.pc[2][0] + k, keep) != T(0) || ld_keep(PE.pc[2][1] + k, keep) != T(0)))
+            w |= kInfoZPml;
         for (int u = 0; u < PE.nunits; ++u)
         {
             const DftView &U = PE.units[u];
@@ -616,33 +682,16 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         }
         info[o] = w;
     }
-    __syncthreads();
-    for (int t = tid; t < LY::NZ * TY * 3; t += NTH)
+    bar_warps_1_7();
+    for (int t = pt; t < LY::NZ * TY * 3; t += PT)
     {
         const int c = t % 3, r = (t / 3) % TY, o = t / (3 * TY);
         const int kk = X.k0 - 1 + o, yy = X.y0 + r;
         if (!PE.slot[c].map || kk < 0 || kk >= PE.Mz || yy >= PE.My) continue;
-        const RowRange rr = PE.slot[c].rows[yy + (int64_t)kk * PE.My];
-        if (rr.lo <= rr.hi && rr.lo < X.x0 + TX && rr.hi >= X.x0) atomicOr(&info[o], 1u << r);
+        const int2 rr = ld_keep(reinterpret_cast<const int2 *>(PE.slot[c].rows + yy + (int64_t)kk * PE.My), keep);
+        if (rr.x <= rr.y && rr.x < X.x0 + TX && rr.y >= X.x0) atomicOr(&info[o], 1u << r);
     }
-    tile_pml = __syncthreads_or(tile_pml);
-    const bool h_slots = PH.slot[0].map || PH.slot[1].map || PH.slot[2].map;
-
-    const int x = X.x0 + lane;
-    // per own row: components with a grid point at (x, y) that this pass owns
-    unsigned vxy[RPT];
-#pragma unroll
-    for (int r = 0; r < RPT; ++r)
-    {
-        const int y = X.y0 + r0 + r;
-        vxy[r] = 0;
-        if (x < L.xlim && y < L.ylim)
-            for (int c = 0; c < 3; ++c)
-            {
-                if (x >= PE.vlo[c][0] && x <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1]) vxy[r] |= 1u << c;
-                if (x >= PH.vlo[c][0] && x <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1]) vxy[r] |= 1u << (3 + c);
-            }
-    }
+    tile_pml = bar_warps_1_7_or(tile_pml);
     // the low-x halo column / low-y halo row holds no grid point of any
     // component (the ghost layer below the first tile): the plain path takes
     // its new H as zero, as the general path does
@@ -660,15 +709,33 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                  PE.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PE.vhi[c][1] &&
                  PH.vlo[c][0] <= X.x0 - (zcol ? 0 : 1) && X.x0 + TX - 1 <= PH.vhi[c][0] &&
                  PH.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PH.vhi[c][1];
-    // per plane: may each side take the plain path
-    for (int o = tid; o < LY::NZ; o += NTH)
+    // per plane: may each side take the plain path; kInfoZPml becomes "CPML
+    // at this tile plane" (the tile's x / y tables or the plane's z)
+    for (int o = pt; o < LY::NZ; o += PT)
     {
         const unsigned w = info[o];
         const bool zpml = pml_tables && (tile_pml || (w & kInfoZPml));
         const bool hok = inside && !h_slots && !(w & kInfoDftH) && ((w >> (kInfoZValidShift + 3)) & 7u) == 7u;
         const bool eok = inside && !(w & kInfoDftE) && ((w >> kInfoZValidShift) & 7u) == 7u;
-        info[o] |= (hok ? (zpml ? kInfoLeanH : kInfoFastH) : 0u) | (eok ? (zpml ? kInfoLeanE : kInfoFastE) : 0u) |
-                   (zcol ? kInfoZeroCol : 0u) | (zrow ? kInfoZeroRow : 0u);
+        info[o] = w | (zpml ? kInfoZPml : 0u) | (hok ? (zpml ? kInfoLeanH : kInfoFastH) : 0u) |
+                  (eok ? (zpml ? kInfoLeanE : kInfoFastE) : 0u) | (zcol ? kInfoZeroCol : 0u) | (zrow ? kInfoZeroRow : 0u);
+    }
+    }
+
+    const int x = X.x0 + lane;
+    // per own row: components with a grid point at (x, y) that this pass owns
+    unsigned vxy[RPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r)
+    {
+        const int y = X.y0 + r0 + r;
+        vxy[r] = 0;
+        if (x < L.xlim && y < L.ylim)
+            for (int c = 0; c < 3; ++c)
+            {
+                if (x >= PE.vlo[c][0] && x <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1]) vxy[r] |= 1u << c;
+                if (x >= PH.vlo[c][0] && x <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1]) vxy[r] |= 1u << (3 + c);
+            }
     }
     __syncthreads();
     const int sz = (int)PE.sz, sy = (int)PE.sy;
@@ -708,8 +775,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         const bool fast_e = (we & kInfoFastE) && !e_slots;
         const bool lean_h = PML && (wh & kInfoLeanH);
         const bool lean_e = PML && (we & kInfoLeanE) && !e_slots;
-        const bool pml_h = !fast_h && pml_tables && (tile_pml || (wh & kInfoZPml));
-        const bool pml_e = !fast_e && pml_tables && (tile_pml || (we & kInfoZPml));
+        const bool pml_h = !fast_h && pml_tables && (wh & kInfoZPml);
+        const bool pml_e = !fast_e && pml_tables && (we & kInfoZPml);
         const bool dft_h = wh & kInfoDftH;
         // CPML psi of this iteration's own H points, loaded before the TMA wait
         T ph[RPT][3][2];
