@@ -353,6 +353,16 @@ __device__ __forceinline__ T fused_term(const FusedCtx<T> &X, bool pml_plane, in
                        pin2, pout1, pout2, idx);
 }
 
+// curl term of one component from its two curls with the CPML coefficients
+// of its two curl axes (cv == 0 on both: plain curl, as Curl_Stepping)
+template <typename T>
+__device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &A2, T curl1, T curl2, T psi1, T psi2, T *ps1,
+                                        T *ps2)
+{
+    if (A1.c == T(0) && A2.c == T(0)) return curl1 - curl2;
+    return pml_term(A1.c, A2.c, A1.b, A2.b, A1.ik, A2.ik, curl1, curl2, psi1, psi2, ps1, ps2);
+}
+
 // H at the new level of a halo point (not owned: nothing is written),
 // component GC (3..5), point (x, y) of plane k; E stages eA/eB hold planes
 // k/k+1, H stage hA plane k.  Returns 0 where the component has no grid point.
@@ -396,14 +406,20 @@ __device__ __forceinline__ T fused_h_halo(const FusedCtx<T> &X, int x, int y, in
     return material_at(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
 }
 
-// curl term of one component from its two curls with the CPML coefficients
-// of its two curl axes (cv == 0 on both: plain curl, as Curl_Stepping)
+// The halo H point of this thread, if any: Hz / Hx of the low-y row (warps
+// 7 / 6), Hz / Hy of the low-x column (warp 5, lanes < TY / < 2 TY), with
+// its place (row, col) in an H ring plane
 template <typename T>
-__device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &A2, T curl1, T curl2, T psi1, T psi2, T *ps1,
-                                        T *ps2)
+__device__ __forceinline__ bool halo_point(const FusedCtx<T> &X, int wid, int lane, int &hx, int &hy, int &comp, int &row,
+                                           int &col)
 {
-    if (A1.c == T(0) && A2.c == T(0)) return curl1 - curl2;
-    return pml_term(A1.c, A2.c, A1.b, A2.b, A1.ik, A2.ik, curl1, curl2, psi1, psi2, ps1, ps2);
+    constexpr int TY = FusedShape<T>::TY;
+    if (wid == 7) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 2; row = 0; col = lane + 1; }
+    else if (wid == 6) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 0; row = 0; col = lane + 1; }
+    else if (wid == 5 && lane < TY) { hx = X.x0 - 1; hy = X.y0 + lane; comp = 2; row = lane + 1; col = 0; }
+    else if (wid == 5 && lane < 2 * TY) { hx = X.x0 - 1; hy = X.y0 + lane - TY; comp = 1; row = lane - TY + 1; col = 0; }
+    else return false;
+    return true;
 }
 
 // General H(k) at this thread's own point of tile row `row`: validity bits,
@@ -958,13 +974,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                         h_own_general<T>(X, q, r0 + r, eA, eB, hA, rn, vxy[r] & (wh >> kInfoZValidShift), q >= 1, pml_h,
                                          h_slots, dft_h, idx + r * sy, ph[r]);
                 }
-                if (wid >= 6 || (wid == 5 && lane < 2 * TY))
+                int hx, hy, comp, row, col;
+                if (halo_point(X, wid, lane, hx, hy, comp, row, col))
                 {
-                    int hx, hy, comp, row, col;
-                    if (wid == 7) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 2; row = 0; col = lane + 1; }
-                    else if (wid == 6) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 0; row = 0; col = lane + 1; }
-                    else if (lane < TY) { hx = X.x0 - 1; hy = X.y0 + lane; comp = 2; row = lane + 1; col = 0; }
-                    else { hx = X.x0 - 1; hy = X.y0 + lane - TY; comp = 1; row = lane - TY + 1; col = 0; }
                     T v;
                     if (comp == 0) v = fused_h_halo<T, 3>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
                     else if (comp == 1) v = fused_h_halo<T, 4>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
