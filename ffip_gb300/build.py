@@ -68,7 +68,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         msg = "\n\n".join(" ".join(j) + "\n" + out for j, out in failed)
         raise RuntimeError("native build failed:\n" + msg)
     tmp = LIB + ".tmp%d" % os.getpid()
-    link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs]
+    link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("native link failed:\n" + r.stdout.decode(errors="replace"))

@@ -4,7 +4,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <exception>
 #include <stdexcept>
+#include <thread>
 
 namespace ffipg
 {
@@ -637,21 +639,23 @@ void rasterize_media(Plan &p)
         p.group_index[side].clear();
     }
     const double tol = 1e-4;
-    for (int c = 0; c < 6; ++c)
-    {
-        const int side = c < 3 ? 0 : 1;
-        const size_t npool = p.pool[side].size();
-        SlotList &sl = p.slots[c];
-        sl = SlotList();
+    // phase 1, one host thread per component: the points each geometry owns
+    // (the first geometry in list order containing the point), as linear
+    // indices within the component's valid box in scan order (k, j, i), with
+    // the owning geometry
+    std::vector<uint64_t> own_li[6];
+    std::vector<int> own_g[6];
+    auto own = [&](int c) {
         int n[3], first[3];
         for (int a = 0; a < 3; ++a)
         {
             first[a] = p.vlo[c][a];
             n[a] = std::max(0, p.vhi[c][a] - p.vlo[c][a] + 1);
         }
-        const size_t total = (size_t)n[0] * n[1] * n[2];
-        if (!total) continue;
-        std::vector<int> owner(total, -1);
+        const uint64_t total = (uint64_t)n[0] * n[1] * n[2];
+        if (!total) return;
+        std::vector<uint64_t> taken((total + 63) / 64, 0);
+        std::vector<std::pair<uint64_t, int>> list;
         for (size_t g = 0; g < p.geoms.size(); ++g)
         {
             double blo[3], bhi[3];
@@ -673,81 +677,168 @@ void rasterize_media(Plan &p)
                 for (int j = r0[1]; j <= r1[1]; ++j)
                     for (int i = r0[0]; i <= r1[0]; ++i)
                     {
-                        size_t li = ((size_t)(k - first[2]) * n[1] + (j - first[1])) * n[0] + (i - first[0]);
-                        if (owner[li] >= 0) continue;
+                        const uint64_t li = ((uint64_t)(k - first[2]) * n[1] + (j - first[1])) * n[0] + (i - first[0]);
+                        if ((taken[li >> 6] >> (li & 63)) & 1) continue;
                         double x = p.coord_of(0, i, comp_parity(c, 0)), y = p.coord_of(1, j, comp_parity(c, 1)),
                                z = p.coord_of(2, k, comp_parity(c, 2));
-                        if (p.geoms[g].inside(x, y, z)) owner[li] = (int)g;
+                        if (p.geoms[g].inside(x, y, z))
+                        {
+                            taken[li >> 6] |= uint64_t(1) << (li & 63);
+                            list.emplace_back(li, (int)g);
+                        }
                     }
         }
+        if (p.geoms.size() > 1) std::sort(list.begin(), list.end());
+        own_li[c].resize(list.size());
+        own_g[c].resize(list.size());
+        for (size_t t = 0; t < list.size(); ++t)
+        {
+            own_li[c][t] = list[t].first;
+            own_g[c][t] = list[t].second;
+        }
+    };
+    {
+        std::exception_ptr err[6];
+        std::vector<std::thread> th;
+        for (int c = 0; c < 6; ++c)
+            th.emplace_back([&, c] {
+                try
+                {
+                    own(c);
+                }
+                catch (...)
+                {
+                    err[c] = std::current_exception();
+                }
+            });
+        for (auto &t : th) t.join();
+        for (auto &e : err)
+            if (e) std::rethrow_exception(e);
+    }
+    // phase 2, components in order (pole groups are numbered by first
+    // appearance): slots
+    for (int c = 0; c < 6; ++c)
+    {
+        const int side = c < 3 ? 0 : 1;
+        const size_t npool = p.pool[side].size();
+        SlotList &sl = p.slots[c];
+        sl = SlotList();
+        int n[3], first[3];
+        for (int a = 0; a < 3; ++a)
+        {
+            first[a] = p.vlo[c][a];
+            n[a] = std::max(0, p.vhi[c][a] - p.vlo[c][a] + 1);
+        }
+        const uint64_t total = (uint64_t)n[0] * n[1] * n[2];
+        if (!total) continue;
         const std::vector<double> &def_amp = side == 0 ? p.default_medium.e_amp : p.default_medium.m_amp;
         const double g_def = p.g_default[side];
         std::vector<int> def_bits;
         for (size_t i = 0; i < npool; ++i)
             if (std::abs(def_amp[i]) > tol) def_bits.push_back((int)i);
         const bool all_slots = !def_bits.empty();
-        std::vector<double> amps_tmp;
-        std::vector<std::vector<double>> slot_amps;
-        for (int k = 0; k < n[2]; ++k)
-            for (int j = 0; j < n[1]; ++j)
-                for (int i = 0; i < n[0]; ++i)
+        // the medium of a point: g_inf, its active poles (amplitude above tol)
+        // and their amplitudes; homogeneous geometries (boxes, spheres) and
+        // the default medium are resolved once, at their first point in scan
+        // order, so that pole groups are registered at the same points (and
+        // numbered the same) as point by point
+        struct PointMedium
+        {
+            bool ready{false};
+            double g{0};
+            int nb{0}, grp{-1};
+            int bits[kMaxPoles];
+            double a[kMaxPoles];
+        };
+        auto resolve = [&](PointMedium &m, double g, const std::vector<double> &amps) {
+            m.g = g;
+            m.nb = 0;
+            for (size_t q = 0; q < npool && q < amps.size(); ++q)
+                if (std::abs(amps[q]) > tol)
                 {
-                    size_t li = ((size_t)k * n[1] + j) * n[0] + i;
-                    int gi = owner[li];
-                    if (gi < 0 && !all_slots) continue;
-                    double g;
-                    const std::vector<double> *amps;
-                    PoolMedium tmp;
-                    if (gi < 0)
-                    {
-                        g = g_def;
-                        amps = &def_amp;
-                    }
-                    else
-                    {
-                        const Geometry &geo = p.geoms[gi];
-                        if (geo.type == Geometry::BOX || geo.type == Geometry::SPHERE)
-                            tmp = geo.medium;
-                        else
-                        {
-                            int ii = i + first[0], jj = j + first[1], kk = k + first[2];
-                            tmp = geo.medium_at(p.coord_of(0, ii, comp_parity(c, 0)), p.coord_of(1, jj, comp_parity(c, 1)),
-                                                p.coord_of(2, kk, comp_parity(c, 2)));
-                        }
-                        g = side == 0 ? tmp.epsilon : tmp.mu;
-                        amps = side == 0 ? &tmp.e_amp : &tmp.m_amp;
-                    }
-                    std::vector<int> bits;
-                    for (size_t q = 0; q < npool && q < amps->size(); ++q)
-                        if (std::abs((*amps)[q]) > tol) bits.push_back((int)q);
-                    if (bits.empty() && g == g_def) continue;
-                    if ((int)bits.size() > kMaxPoles)
+                    if (m.nb == kMaxPoles)
                         throw std::runtime_error("a grid point has more than " + std::to_string(kMaxPoles) + " active poles");
-                    auto it = p.group_index[side].find(bits);
-                    int grp;
-                    if (it == p.group_index[side].end())
-                    {
-                        grp = (int)p.groups[side].size();
-                        p.group_index[side][bits] = grp;
-                        PoleGroup pg;
-                        pg.pool = bits;
-                        p.groups[side].push_back(pg);
-                    }
-                    else
-                        grp = it->second;
-                    sl.lin.push_back(p.lin(i + first[0], j + first[1], k + first[2]));
-                    sl.g.push_back(g);
-                    sl.group.push_back(grp);
-                    std::vector<double> a;
-                    for (int b : bits) a.push_back((*amps)[b]);
-                    sl.npole_stride = std::max(sl.npole_stride, (int)bits.size());
-                    slot_amps.push_back(a);
+                    m.bits[m.nb] = (int)q;
+                    m.a[m.nb++] = amps[q];
                 }
+            m.grp = -1;
+            m.ready = true;
+        };
+        auto group_of = [&](const PointMedium &m) {
+            std::vector<int> bits(m.bits, m.bits + m.nb);
+            auto it = p.group_index[side].find(bits);
+            if (it != p.group_index[side].end()) return it->second;
+            const int grp = (int)p.groups[side].size();
+            p.group_index[side][bits] = grp;
+            PoleGroup pg;
+            pg.pool = bits;
+            p.groups[side].push_back(pg);
+            return grp;
+        };
+        std::vector<PointMedium> cached(p.geoms.size() + 1);  // per geometry; the last: the default medium
+        std::vector<double> amp_flat;                         // active-pole amplitudes of the slots, in slot order
+        std::vector<uint8_t> amp_n;                           // their count per slot
+        // every point in scan order when the default medium makes slots too,
+        // else the owned points only
+        const std::vector<uint64_t> &OL = own_li[c];
+        const std::vector<int> &OG = own_g[c];
+        const uint64_t count = all_slots ? total : OL.size();
+        for (uint64_t t = 0, cur = 0; t < count; ++t)
+        {
+            uint64_t li;
+            int gi;
+            if (all_slots)
+            {
+                li = t;
+                gi = cur < OL.size() && OL[cur] == li ? OG[cur++] : -1;
+            }
+            else
+            {
+                li = OL[t];
+                gi = OG[t];
+            }
+            const int i = (int)(li % n[0]), j = (int)(li / n[0] % n[1]), k = (int)(li / ((uint64_t)n[0] * n[1]));
+            PointMedium local;
+            PointMedium *m;
+            if (gi < 0)
+            {
+                m = &cached.back();
+                if (!m->ready) resolve(*m, g_def, def_amp);
+            }
+            else
+            {
+                const Geometry &geo = p.geoms[gi];
+                if (geo.type == Geometry::BOX || geo.type == Geometry::SPHERE)
+                {
+                    m = &cached[gi];
+                    if (!m->ready)
+                        resolve(*m, side == 0 ? geo.medium.epsilon : geo.medium.mu,
+                                side == 0 ? geo.medium.e_amp : geo.medium.m_amp);
+                }
+                else
+                {
+                    int ii = i + first[0], jj = j + first[1], kk = k + first[2];
+                    const PoolMedium tmp = geo.medium_at(p.coord_of(0, ii, comp_parity(c, 0)),
+                                                         p.coord_of(1, jj, comp_parity(c, 1)),
+                                                         p.coord_of(2, kk, comp_parity(c, 2)));
+                    resolve(local, side == 0 ? tmp.epsilon : tmp.mu, side == 0 ? tmp.e_amp : tmp.m_amp);
+                    m = &local;
+                }
+            }
+            if (m->nb == 0 && m->g == g_def) continue;
+            if (m->grp < 0) m->grp = group_of(*m);
+            sl.lin.push_back(p.lin(i + first[0], j + first[1], k + first[2]));
+            sl.g.push_back(m->g);
+            sl.group.push_back(m->grp);
+            amp_flat.insert(amp_flat.end(), m->a, m->a + m->nb);
+            amp_n.push_back((uint8_t)m->nb);
+            sl.npole_stride = std::max(sl.npole_stride, m->nb);
+        }
         const size_t ns = sl.lin.size();
         sl.any_poles = sl.npole_stride > 0;
         sl.amp.assign((size_t)sl.npole_stride * ns, 0.0);
-        for (size_t s = 0; s < ns; ++s)
-            for (size_t q = 0; q < slot_amps[s].size(); ++q) sl.amp[q * ns + s] = slot_amps[s][q];
+        for (size_t s = 0, o = 0; s < ns; o += amp_n[s], ++s)
+            for (size_t q = 0; q < amp_n[s]; ++q) sl.amp[q * ns + s] = amp_flat[o + q];
     }
 }
 
