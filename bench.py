@@ -229,7 +229,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=256, help="cells per axis of the workload")
+    ap.add_argument("--n", "--cells", dest="n", type=int, default=256, help="cells per axis of the workload")
     ap.add_argument("--cpu-steps", type=int, default=8, help="steps timed for the CPU baseline sample")
     ap.add_argument("--skip-full-run", action="store_true", help="skip the full-length fp32/fp64 runs")
     ap.add_argument("--engine", default="auto")
