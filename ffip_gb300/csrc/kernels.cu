@@ -154,6 +154,7 @@ public:
         if (side_) cudaStreamDestroy(side_);
         if (fork_) cudaEventDestroy(fork_);
         if (join_) cudaEventDestroy(join_);
+        if (face_h_) cudaEventDestroy(face_h_);
         if (dft_)
         {
             cudaEventDestroy(dft_ready_);
@@ -334,9 +335,19 @@ public:
                 check(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking), "cudaStreamCreate");
                 check(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "cudaEventCreate");
                 check(cudaEventCreateWithFlags(&join_, cudaEventDisableTiming), "cudaEventCreate");
+                check(cudaEventCreateWithFlags(&face_h_, cudaEventDisableTiming), "cudaEventCreate");
             }
             check(cudaEventRecord(fork_, stream_), "cudaEventRecord");
             check(cudaStreamWaitEvent(side_, fork_, 0), "cudaStreamWaitEvent");
+        }
+        // the H half of k_face reads only step-n fields: first on the side
+        // stream, ahead of the interior instance
+        if (nface > 0)
+        {
+            k_face<T, false><<<face_blocks, 256, 0, side_>>>(L);
+            check(cudaGetLastError(), "k_face launch");
+            check(cudaEventRecord(face_h_, side_), "cudaEventRecord");
+            ++n;
         }
         if (J.nb > 0)
         {
@@ -352,9 +363,14 @@ public:
             check(cudaGetLastError(), "k_fused launch");
             ++n;
         }
-        if (nface > 0)
+        // E of the face layers reads the new H of the face layers and of the
+        // tiles next to them; when those tiles are all CPML jobs it follows the
+        // CPML instance on the main stream, beside the interior instance
+        const bool early_face = nface > 0 && J.nb > 0 && J.face_in_pml;
+        if (early_face)
         {
-            k_face<T, false><<<face_blocks, 256, 0, side_>>>(L);
+            check(cudaStreamWaitEvent(stream_, face_h_, 0), "cudaStreamWaitEvent");
+            k_face<T, true><<<face_blocks, 256, 0, stream_>>>(L);
             check(cudaGetLastError(), "k_face launch");
             ++n;
         }
@@ -363,9 +379,8 @@ public:
             check(cudaEventRecord(join_, side_), "cudaEventRecord");
             check(cudaStreamWaitEvent(stream_, join_, 0), "cudaStreamWaitEvent");
         }
-        if (nface > 0)
+        if (nface > 0 && !early_face)
         {
-            // E of the face layers reads the new H of the pass
             k_face<T, true><<<face_blocks, 256, 0, stream_>>>(L);
             check(cudaGetLastError(), "k_face launch");
             ++n;
@@ -428,6 +443,10 @@ public:
     {
         int4 *dev{nullptr};
         int nb{0}, ni{0};
+        // no job of the instance without CPML code holds the last x tile or
+        // the last y tile: the tiles whose new H the E half of k_face reads
+        // all belong to the CPML instance
+        bool face_in_pml{false};
     };
     template <typename T>
     const Jobs &jobs_for(const FusedParams<T> &p, const FusedLaunch<T> &L, int nbx, int nby, int TX, int TY, int KCH)
@@ -498,6 +517,9 @@ public:
         Jobs J;
         J.nb = (int)b.size();
         J.ni = (int)in.size();
+        J.face_in_pml = true;
+        for (const int4 &j : in)
+            if (j.x + TX >= L.xlim || j.y + TY >= L.ylim) J.face_in_pml = false;
         b.insert(b.end(), in.begin(), in.end());
         check(cudaMalloc(&J.dev, b.size() * sizeof(int4)), "cudaMalloc");
         check(cudaMemcpy(J.dev, b.data(), b.size() * sizeof(int4), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
@@ -620,7 +642,7 @@ private:
     std::map<std::string, Jobs> jobs_;
     cudaStream_t side_{nullptr};
     int nsm_{0};
-    cudaEvent_t fork_{nullptr}, join_{nullptr};
+    cudaEvent_t fork_{nullptr}, join_{nullptr}, face_h_{nullptr};
     // DFT sums of the fused pass: their stream, the event they wait for, the
     // event after them per pass parity, and a join event
     cudaStream_t dft_{nullptr};
