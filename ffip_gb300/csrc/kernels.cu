@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <vector>
 #include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -94,16 +95,16 @@ __global__ void k_dft_norm(const double *re, const double *im, int64_t n, double
 // cuTensorMapEncodeTiled from the driver, without linking libcuda
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn)
-    {
+    // looked up once per process (a function-local static is initialised by
+    // one thread; a throw leaves it to the next call)
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         check(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q),
               "cudaGetDriverEntryPoint(cuTensorMapEncodeTiled)");
         if (q != cudaDriverEntryPointSuccess || !p) throw std::runtime_error("cuTensorMapEncodeTiled not available");
-        fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
+        return (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }();
     return fn;
 }
 
@@ -247,9 +248,11 @@ public:
             check(cudaMalloc(&err_, sizeof(int)), "cudaMalloc");
             check(cudaMemsetAsync(err_, 0, sizeof(int), stream_), "cudaMemsetAsync");
         }
-        static bool attr_set = false;
-        if (!attr_set)
-        {
+        // kernel attributes, set once per process (std::call_once: the first
+        // handle sets them before any launch; no handle changes them while
+        // another one's kernels run)
+        static std::once_flag attr_once;
+        std::call_once(attr_once, [&] {
             // shared memory for the CTAs per SM each instance is built for
             // (plus the 1 KB the system reserves per CTA), the same carveout
             // for both so that they share SMs; the rest of the unified
@@ -269,8 +272,7 @@ public:
                       "cudaFuncSetAttribute");
                 check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve), "cudaFuncSetAttribute");
             }
-            attr_set = true;
-        }
+        });
         // the DFT sums of two passes ago (on dft_) read the output buffers of
         // this pass
         const int par = passes_ & 1;
