@@ -16,8 +16,10 @@
  * and never aborts; ffip_last_error() gives the message of the calling
  * thread's last failure.  Host buffers belong to the caller; device memory
  * belongs to the handle.  Calls on one handle must be serialised; distinct
- * handles are independent.  A handle runs on one CUDA device, on its own
- * stream.
+ * handles hold separate state (fields, streams, job lists), but driving
+ * several handles from several host threads at once is not supported: call
+ * them from one thread.  A handle runs on one CUDA device, on its own
+ * streams.
  */
 #ifndef FFIP_GB300_H
 #define FFIP_GB300_H
