@@ -162,6 +162,33 @@ def cpu_leg(cfg, steps, warmup, threads):
     return dt, setup
 
 
+def large_leg(dev, steps=100):
+    """The large design workload's forward simulation (workloads.large_design:
+    512 x 512 x 384 cells, 24-cell CPML, Drude backplane, 256 x 256 x 32
+    Lorentz/vacuum design box, three 256 x 256 DFT planes at 16 frequencies),
+    fp32 state: set-up time and device-timed step rate.  One design
+    iteration there is a forward run and one adjoint run per objective
+    frequency, 20000 steps each."""
+    from ffip_gb300 import native, workloads
+    cfg, ds = workloads.large_design(precision="fp32")
+    cfg["device"] = dev
+    t0 = time.perf_counter()
+    s = native.NativeSim(cfg, ds)
+    setup = time.perf_counter() - t0
+    s.step(3)
+    s.sync()
+    ms = s.step_timed(steps) / steps
+    st = s.stats()
+    s.close()
+    cells = st["yee_cells"]
+    run_s = 20000 * ms / 1e3
+    return {"workload": "large design 512x512x384, 24-cell CPML, Drude backplane, 256x256x32 Lorentz/vacuum design box, "
+                        "3 DFT planes x 16 freqs, fp32 state", "cells": cells, "steps_timed": steps, "ms_per_step": ms,
+            "gcell_updates_per_s": cells / ms / 1e6, "achieved_gbs": st["bytes_per_step"] / (ms * 1e-3) / 1e9,
+            "setup_s": setup, "seconds_per_20000_step_run": run_s,
+            "seconds_per_design_iter_1fwd_16adj": 17 * run_s}
+
+
 def vacuum64_leg(dev, cpu):
     """The plain fp64 vacuum box (64^3, 8-cell CPML, one Ez point current,
     Ez DFT plane at 3 frequencies, 1000 steps): GPU fp64 device time, and the
@@ -235,6 +262,7 @@ def main():
     ap.add_argument("--engine", default="auto")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--fp32-only", action="store_true", help="time only the fp32 stepper (profiling runs)")
+    ap.add_argument("--no-large", action="store_true", help="skip the large design workload's step rate")
     ap.add_argument("--design-iters", type=int, default=2,
                     help="timed design iterations of the adjoint workload (0: skip that leg)")
     a = ap.parse_args()
@@ -352,6 +380,11 @@ def main():
     #      run per frequency + gradient), simulations kept between iterations
     if a.design_iters > 0 and not a.fp32_only:
         out["design_iter"] = design_leg(a.design_iters, dev, world)
+    if not a.no_large and not a.fp32_only:
+        try:
+            out["large_design"] = large_leg(dev)
+        except Exception as e:  # reported, not fatal: the headline line stands without it
+            out["large_design"] = {"error": str(e)[:300]}
 
     # ---- CPU baseline sample (rank 0 only)
     if rank == 0 and world == 1 and not a.no_cpu:

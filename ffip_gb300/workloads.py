@@ -96,6 +96,52 @@ def vacuum_point(n: int = 64, steps: int = 1000, seed: int = 7, precision: str =
     }
 
 
+def large_design(n: int = 512, nz: int = 384, pml: int = 24, design=(256, 32), nfreq: int = 16, steps: int = 20000,
+                 seed: int = 2024, precision: str = "fp32", engine: str = "auto"):
+    """The large design workload (one forward simulation of the
+    surrogate-screened design loop at scale): an n x n x nz cell box (dx = 1,
+    Courant 0.5) with a `pml`-cell CPML; a Drude metal backplane (omega_p
+    0.8, gamma 0.02, angular rates as in dispersive_spheres) 8 cells thick
+    across the interior, 8 cells above the lower CPML; on it a design box of
+    design[0] x design[0] x design[1] cells whose density (nodes at every
+    cell corner) is seeded filtered noise (sigma = 4 nodes) between a 2-pole
+    Lorentz design material (the dispersive_spheres recipe) and vacuum; an Ex
+    current sheet (Gaussian1, f = 0.1) half-way up; three 256 x 256 DFT
+    planes (Ex and Ey at one height, Ex at another) at `nfreq` frequencies in
+    [0.06, 0.14]; `steps` time steps.  Returns (config, datasets)."""
+    rng = np.random.default_rng(seed)
+    dn, dz = design
+    lor = medium(2.0, esus=[{"type": "Lorentz", "frequency": rng.uniform(0.05, 0.2) / TWO_PI,
+                             "gamma": rng.uniform(0.001, 0.02) / TWO_PI, "amplitude": rng.uniform(0.5, 3.0)}
+                            for _ in range(2)])
+    dru = medium(1.0, esus=[{"type": "Drude", "frequency": 0.8 / TWO_PI, "gamma": 0.02 / TWO_PI, "amplitude": 1.0}])
+    z_lo = -nz / 2.0 + pml
+    inner = n - 2.0 * pml
+    z_plate = z_lo + 8 + 4.0
+    z_design = z_lo + 16 + dz / 2.0
+    rho = filtered_noise((dz + 1, dn + 1, dn + 1), 4.0, seed)
+    freqs = [float(f) for f in np.linspace(0.06, 0.14, nfreq)]
+    cfg = {
+        "courant number": 0.5, "resolution": 1.0, "size": [float(n), float(n), float(nz)],
+        "input file": "input.h5", "fields output file": "output.h5",
+        "default material": medium(), "progress interval": 1e9,
+        "PML": [{"thickness": float(pml), "k max": 1.0, "sigma max": sigma_max(3, pml), "order": 3}],
+        "geometry": [{"type": "box", "center": [0.0, 0.0, z_plate], "size": [inner, inner, 8.0], "medium": dru},
+                     {"type": "two medium box", "center": [0.0, 0.0, z_design], "size": [float(dn), float(dn), float(dz)],
+                      "dimension": [dn + 1, dn + 1, dz + 1], "density dataset": "two medium box 0",
+                      "medium1": lor, "medium2": medium()}],
+        "sources": [{"type": "volume source", "center": [0.0, 0.0, 0.0], "size": [inner, inner, 0.0],
+                     "amplitude": 1.0, "field component": "Ex",
+                     "function": {"type": "Gaussian1", "frequency": 0.1, "cutoff": 4.0, "start time": 0.0}}],
+        "fields output": [{"type": "volume fields dft", "center": [0.0, 0.0, zc], "size": [256.0, 256.0, 0.0],
+                           "frequency": freqs, "field component": comp, "output group": "volume fields dft %d" % i}
+                          for i, (comp, zc) in enumerate((("Ex", nz / 4.0), ("Ey", nz / 4.0), ("Ex", nz / 2.0 - pml - 16.0)))],
+        "stop condition": {"type": "time", "time": steps * 0.5},
+        "precision": precision, "engine": engine,
+    }
+    return cfg, {"two medium box 0": rho.ravel()}
+
+
 def filtered_noise(shape, sigma, seed):
     """Seeded uniform noise, Gaussian-filtered (sigma in nodes), min-max
     rescaled to [0, 1]: the design-density recipe of the adjoint workload."""
