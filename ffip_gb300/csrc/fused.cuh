@@ -54,6 +54,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "engine.hpp"
 
 namespace ffipg
@@ -351,6 +353,16 @@ __device__ __forceinline__ T fused_term(const FusedCtx<T> &X, bool pml_plane, in
     return pml_combine(cv1, cv2, X.template pml_val<C::a1>(C::q1, 0, p1), X.template pml_val<C::a2>(C::q2, 0, p2),
                        X.template pml_val<C::a1>(C::q1, 2, p1), X.template pml_val<C::a2>(C::q2, 2, p2), curl1, curl2, pin1,
                        pin2, pout1, pout2, idx);
+}
+
+// (a - b) / dx - (c - d) / dx of the plain curl update, 1/dx given; UNIT:
+// 1/dx is 1 and the two multiplications are left out (the same bits: x * 1
+// is x)
+template <bool UNIT, typename T>
+__device__ __forceinline__ T curl_diff(T a, T b, T c, T d, T inv)
+{
+    if (UNIT) return (a - b) - (c - d);
+    return (a - b) * inv - (c - d) * inv;
 }
 
 // curl term of one component from its two curls with the CPML coefficients
@@ -759,6 +771,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     const int offE = (r0 + 1) * BX + lane + XOFF;    // own point of row r0 in an E or H box
     const int offN = (r0 + 1) * (TX + 1) + lane + 1;  // own point of row r0 in an H ring plane
     const T coefH = PH.coef_def, coefE = PE.coef_def, idh = PH.inv_dx, ide = PE.inv_dx;
+    // fp64: the plain path without the 1/dx multiplications when 1/dx is 1
+    // (the pass is bound by the fp64 pipe there)
+    const bool unit_dx = sizeof(T) == 8 && idh == T(1) && ide == T(1);
     const unsigned rowmask = ((1u << RPT) - 1u) << r0;
 
     // material slot indices of the E plane of the next iteration, loaded one
@@ -897,44 +912,54 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         {
             if (fast_h)
             {
-                const T *eA0 = X.e_tile(eA, 0) + offE, *eA1 = X.e_tile(eA, 1) + offE, *eA2 = X.e_tile(eA, 2) + offE;
-                const T *eB0 = X.e_tile(eB, 0) + offE, *eB1 = X.e_tile(eB, 1) + offE;
-                const T *hA0 = X.h_tile(hA, 0) + offE, *hA1 = X.h_tile(hA, 1) + offE, *hA2 = X.h_tile(hA, 2) + offE;
-                T exa[RPT + 1], eza[RPT + 1];
+                auto fast_h_own = [&](auto unit) {
+                    constexpr bool U = decltype(unit)::value;
+                    const T *eA0 = X.e_tile(eA, 0) + offE, *eA1 = X.e_tile(eA, 1) + offE, *eA2 = X.e_tile(eA, 2) + offE;
+                    const T *eB0 = X.e_tile(eB, 0) + offE, *eB1 = X.e_tile(eB, 1) + offE;
+                    const T *hA0 = X.h_tile(hA, 0) + offE, *hA1 = X.h_tile(hA, 1) + offE, *hA2 = X.h_tile(hA, 2) + offE;
+                    T exa[RPT + 1], eza[RPT + 1];
 #pragma unroll
-                for (int r = 0; r <= RPT; ++r)
-                {
-                    exa[r] = eA0[r * BX];
-                    eza[r] = eA2[r * BX];
-                }
-                T hn0[RPT], hn1[RPT], hn2[RPT];
-#pragma unroll
-                for (int r = 0; r < RPT; ++r)
-                {
-                    const T eya = eA1[r * BX], eyx = eA1[r * BX + 1], eyb = eB1[r * BX];
-                    const T exb = eB0[r * BX], ezx = eA2[r * BX + 1];
-                    hn0[r] = hA0[r * BX] + coefH * ((eza[r] - eza[r + 1]) * idh - (eya - eyb) * idh);
-                    hn1[r] = hA1[r * BX] + coefH * ((exa[r] - exb) * idh - (eza[r] - ezx) * idh);
-                    hn2[r] = hA2[r * BX] + coefH * ((eya - eyx) * idh - (exa[r] - exa[r + 1]) * idh);
-                }
-                T *n0 = X.hn_plane(rn, 0) + offN, *n1 = X.hn_plane(rn, 1) + offN, *n2 = X.hn_plane(rn, 2) + offN;
-#pragma unroll
-                for (int r = 0; r < RPT; ++r)
-                {
-                    n0[r * (TX + 1)] = hn0[r];
-                    n1[r * (TX + 1)] = hn1[r];
-                    n2[r * (TX + 1)] = hn2[r];
-                }
-                if (q >= 1)
-                {
+                    for (int r = 0; r <= RPT; ++r)
+                    {
+                        exa[r] = eA0[r * BX];
+                        eza[r] = eA2[r * BX];
+                    }
+                    T hn0[RPT], hn1[RPT], hn2[RPT];
 #pragma unroll
                     for (int r = 0; r < RPT; ++r)
                     {
-                        F.hout[0][idx + r * sy] = hn0[r];
-                        F.hout[1][idx + r * sy] = hn1[r];
-                        F.hout[2][idx + r * sy] = hn2[r];
+                        const T eya = eA1[r * BX], eyx = eA1[r * BX + 1], eyb = eB1[r * BX];
+                        const T exb = eB0[r * BX], ezx = eA2[r * BX + 1];
+                        hn0[r] = hA0[r * BX] + coefH * curl_diff<U>(eza[r], eza[r + 1], eya, eyb, idh);
+                        hn1[r] = hA1[r * BX] + coefH * curl_diff<U>(exa[r], exb, eza[r], ezx, idh);
+                        hn2[r] = hA2[r * BX] + coefH * curl_diff<U>(eya, eyx, exa[r], exa[r + 1], idh);
                     }
+                    T *n0 = X.hn_plane(rn, 0) + offN, *n1 = X.hn_plane(rn, 1) + offN, *n2 = X.hn_plane(rn, 2) + offN;
+#pragma unroll
+                    for (int r = 0; r < RPT; ++r)
+                    {
+                        n0[r * (TX + 1)] = hn0[r];
+                        n1[r * (TX + 1)] = hn1[r];
+                        n2[r * (TX + 1)] = hn2[r];
+                    }
+                    if (q >= 1)
+                    {
+#pragma unroll
+                        for (int r = 0; r < RPT; ++r)
+                        {
+                            F.hout[0][idx + r * sy] = hn0[r];
+                            F.hout[1][idx + r * sy] = hn1[r];
+                            F.hout[2][idx + r * sy] = hn2[r];
+                        }
+                    }
+                };
+                if constexpr (sizeof(T) == 8)
+                {
+                    if (unit_dx) fast_h_own(std::true_type{});
+                    else fast_h_own(std::false_type{});
                 }
+                else
+                    fast_h_own(std::false_type{});
                 const T *gA0 = X.e_tile(eA, 0), *gA1 = X.e_tile(eA, 1), *gA2 = X.e_tile(eA, 2), *gB0 = X.e_tile(eB, 0),
                         *gB1 = X.e_tile(eB, 1);
                 if (wid >= 6)
@@ -991,29 +1016,39 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         {
             if (fast_e)
             {
-                const T *eS0 = X.e_tile(eS, 0) + offE, *eS1 = X.e_tile(eS, 1) + offE, *eS2 = X.e_tile(eS, 2) + offE;
-                const T *n0 = X.hn_plane(rp, 0) + offN, *n1 = X.hn_plane(rp, 1) + offN, *n2 = X.hn_plane(rp, 2) + offN;
-                const T *p0 = X.hn_plane(rpp, 0) + offN, *p1 = X.hn_plane(rpp, 1) + offN;
-                constexpr int RS = TX + 1;  // ring row stride
-                T hz[RPT + 1], hx[RPT + 1];  // rows r0-1 .. r0+RPT-1
+                auto fast_e_own = [&](auto unit) {
+                    constexpr bool U = decltype(unit)::value;
+                    const T *eS0 = X.e_tile(eS, 0) + offE, *eS1 = X.e_tile(eS, 1) + offE, *eS2 = X.e_tile(eS, 2) + offE;
+                    const T *n0 = X.hn_plane(rp, 0) + offN, *n1 = X.hn_plane(rp, 1) + offN, *n2 = X.hn_plane(rp, 2) + offN;
+                    const T *p0 = X.hn_plane(rpp, 0) + offN, *p1 = X.hn_plane(rpp, 1) + offN;
+                    constexpr int RS = TX + 1;  // ring row stride
+                    T hz[RPT + 1], hx[RPT + 1];  // rows r0-1 .. r0+RPT-1
 #pragma unroll
-                for (int r = 0; r <= RPT; ++r)
-                {
-                    hz[r] = n2[(r - 1) * RS];
-                    hx[r] = n0[(r - 1) * RS];
-                }
+                    for (int r = 0; r <= RPT; ++r)
+                    {
+                        hz[r] = n2[(r - 1) * RS];
+                        hx[r] = n0[(r - 1) * RS];
+                    }
 #pragma unroll
-                for (int r = 0; r < RPT; ++r)
+                    for (int r = 0; r < RPT; ++r)
+                    {
+                        const T hzx = n2[r * RS - 1], hyr = n1[r * RS], hyp = p1[r * RS], hyx = n1[r * RS - 1];
+                        const T hxp = p0[r * RS];
+                        const T ex = eS0[r * BX] + coefE * curl_diff<U>(hz[r + 1], hz[r], hyr, hyp, ide);
+                        const T ey = eS1[r * BX] + coefE * curl_diff<U>(hx[r + 1], hxp, hz[r + 1], hzx, ide);
+                        const T ez = eS2[r * BX] + coefE * curl_diff<U>(hyr, hyx, hx[r + 1], hx[r], ide);
+                        F.eout[0][idx_e + r * sy] = ex;
+                        F.eout[1][idx_e + r * sy] = ey;
+                        F.eout[2][idx_e + r * sy] = ez;
+                    }
+                };
+                if constexpr (sizeof(T) == 8)
                 {
-                    const T hzx = n2[r * RS - 1], hyr = n1[r * RS], hyp = p1[r * RS], hyx = n1[r * RS - 1];
-                    const T hxp = p0[r * RS];
-                    const T ex = eS0[r * BX] + coefE * ((hz[r + 1] - hz[r]) * ide - (hyr - hyp) * ide);
-                    const T ey = eS1[r * BX] + coefE * ((hx[r + 1] - hxp) * ide - (hz[r + 1] - hzx) * ide);
-                    const T ez = eS2[r * BX] + coefE * ((hyr - hyx) * ide - (hx[r + 1] - hx[r]) * ide);
-                    F.eout[0][idx_e + r * sy] = ex;
-                    F.eout[1][idx_e + r * sy] = ey;
-                    F.eout[2][idx_e + r * sy] = ez;
+                    if (unit_dx) fast_e_own(std::true_type{});
+                    else fast_e_own(std::false_type{});
                 }
+                else
+                    fast_e_own(std::false_type{});
             }
             else
             {
