@@ -437,7 +437,7 @@ __device__ __forceinline__ bool halo_point(const FusedCtx<T> &X, int wid, int la
 // General H(k) at this thread's own point of tile row `row`: validity bits,
 // CPML from the staged tables (psi values ph loaded by the caller), material
 // slots, DFT.
-template <typename T, bool FULL = true>
+template <typename T, bool FULL = true, bool UNIT = false>
 __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int row, int eA, int eB, int hA, int slot_new,
                                               unsigned vb, bool owned, bool pml, bool slots, bool dft, int idx,
                                               const T (&ph)[3][2])
@@ -462,12 +462,14 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
     const T eya = eA1[offE], eyx = eA1[offE + 1], eyb = eB1[offE];
     const T eza = eA2[offE], ezy = eA2[offE + BX], ezx = eA2[offE + 1];
     T curl1[3], curl2[3];
-    curl1[0] = (eza - ezy) * idh;  // Hx: -(dEz/dy) + dEy/dz
-    curl2[0] = (eya - eyb) * idh;
-    curl1[1] = (exa - exb) * idh;  // Hy: -(dEx/dz) + dEz/dx
-    curl2[1] = (eza - ezx) * idh;
-    curl1[2] = (eya - eyx) * idh;  // Hz: -(dEy/dx) + dEx/dy
-    curl2[2] = (exa - exy) * idh;
+    // UNIT: 1/dx is 1 and the multiplications are left out (the same bits)
+    const T m = UNIT ? T(1) : idh;
+    curl1[0] = UNIT ? eza - ezy : (eza - ezy) * m;  // Hx: -(dEz/dy) + dEy/dz
+    curl2[0] = UNIT ? eya - eyb : (eya - eyb) * m;
+    curl1[1] = UNIT ? exa - exb : (exa - exb) * m;  // Hy: -(dEx/dz) + dEz/dx
+    curl2[1] = UNIT ? eza - ezx : (eza - ezx) * m;
+    curl1[2] = UNIT ? eya - eyx : (eya - eyx) * m;  // Hz: -(dEy/dx) + dEx/dy
+    curl2[2] = UNIT ? exa - exy : (exa - exy) * m;
     PmlCoef<T> hc[3] = {};  // per axis, parity 1
     if (pml)
     {
@@ -507,7 +509,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
 // psi is read from the global arrays, or (STAGED) taken from the values ps
 // the caller read from its staging slots, and written back in place here;
 // sl: material slot indices.
-template <typename T, bool FULL = true, bool STAGED = false>
+template <typename T, bool FULL = true, bool STAGED = false, bool UNIT = false>
 __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int eS, int rn, int rp, unsigned vb,
                                               bool pml, bool slots, int idx, const int (&sl)[3], const T (&ps)[3][2])
 {
@@ -554,12 +556,13 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     const T hyr = n1[offN], hyp = p1[offN], hyx = n1[offN - 1];
     const T hxr = n0[offN], hxp = p0[offN], hxy = n0[offN - (TX + 1)];
     T curl1[3], curl2[3];
-    curl1[0] = (hzr - hzy) * ide;  // Ex: dHz/dy - dHy/dz
-    curl2[0] = (hyr - hyp) * ide;
-    curl1[1] = (hxr - hxp) * ide;  // Ey: dHx/dz - dHz/dx
-    curl2[1] = (hzr - hzx) * ide;
-    curl1[2] = (hyr - hyx) * ide;  // Ez: dHy/dx - dHx/dy
-    curl2[2] = (hxr - hxy) * ide;
+    const T m = UNIT ? T(1) : ide;
+    curl1[0] = UNIT ? hzr - hzy : (hzr - hzy) * m;  // Ex: dHz/dy - dHy/dz
+    curl2[0] = UNIT ? hyr - hyp : (hyr - hyp) * m;
+    curl1[1] = UNIT ? hxr - hxp : (hxr - hxp) * m;  // Ey: dHx/dz - dHz/dx
+    curl2[1] = UNIT ? hzr - hzx : (hzr - hzx) * m;
+    curl1[2] = UNIT ? hyr - hyx : (hyr - hyx) * m;  // Ez: dHy/dx - dHx/dy
+    curl2[2] = UNIT ? hxr - hxy : (hxr - hxy) * m;
     const int x = X.x0 + tx, y = X.y0 + row, k = X.k0 - 1 + qe;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
@@ -986,19 +989,30 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             }
             else
             {
-                if (lean_h)
-                {
+                auto general_h_own = [&](auto unit) {
+                    constexpr bool U = decltype(unit)::value;
+                    if (lean_h)
+                    {
 #pragma unroll
-                    for (int r = 0; r < RPT; ++r)
-                        h_own_general<T, false>(X, q, r0 + r, eA, eB, hA, rn, 63u, q >= 1, true, false, false, idx + r * sy, ph[r]);
+                        for (int r = 0; r < RPT; ++r)
+                            h_own_general<T, false, U>(X, q, r0 + r, eA, eB, hA, rn, 63u, q >= 1, true, false, false, idx + r * sy,
+                                                       ph[r]);
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int r = 0; r < RPT; ++r)
+                            h_own_general<T, true, U>(X, q, r0 + r, eA, eB, hA, rn, vxy[r] & (wh >> kInfoZValidShift), q >= 1,
+                                                      pml_h, h_slots, dft_h, idx + r * sy, ph[r]);
+                    }
+                };
+                if constexpr (sizeof(T) == 8)
+                {
+                    if (unit_dx) general_h_own(std::true_type{});
+                    else general_h_own(std::false_type{});
                 }
                 else
-                {
-#pragma unroll
-                    for (int r = 0; r < RPT; ++r)
-                        h_own_general<T>(X, q, r0 + r, eA, eB, hA, rn, vxy[r] & (wh >> kInfoZValidShift), q >= 1, pml_h,
-                                         h_slots, dft_h, idx + r * sy, ph[r]);
-                }
+                    general_h_own(std::false_type{});
                 int hx, hy, comp, row, col;
                 if (halo_point(X, wid, lane, hx, hy, comp, row, col))
                 {
@@ -1068,12 +1082,22 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                             pe[c][1] = pstage[(LY::PSI_E + (r * 3 + c) * 2 + 1) * NTH];
                         }
                     }
-                    if (lean_e)
-                        e_own_general<T, false, STG>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false, idx_e + r * sy, sl_e[r],
-                                                     pe);
+                    auto general_e_own = [&](auto unit) {
+                        constexpr bool U = decltype(unit)::value;
+                        if (lean_e)
+                            e_own_general<T, false, STG, U>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false, idx_e + r * sy,
+                                                            sl_e[r], pe);
+                        else
+                            e_own_general<T, true, STG, U>(X, q - 1, r0 + r, eS, rp, rpp, vxy[r] & (we >> kInfoZValidShift),
+                                                           pml_e, e_slots, idx_e + r * sy, sl_e[r], pe);
+                    };
+                    if constexpr (sizeof(T) == 8)
+                    {
+                        if (unit_dx) general_e_own(std::true_type{});
+                        else general_e_own(std::false_type{});
+                    }
                     else
-                        e_own_general<T, true, STG>(X, q - 1, r0 + r, eS, rp, rpp, vxy[r] & (we >> kInfoZValidShift), pml_e,
-                                                    e_slots, idx_e + r * sy, sl_e[r], pe);
+                        general_e_own(std::false_type{});
                 }
             }
         }
