@@ -378,7 +378,7 @@ __device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &
 // H at the new level of a halo point (not owned: nothing is written),
 // component GC (3..5), point (x, y) of plane k; E stages eA/eB hold planes
 // k/k+1, H stage hA plane k.  Returns 0 where the component has no grid point.
-template <typename T, int GC>
+template <typename T, int GC, bool UNIT = false>
 __device__ __forceinline__ T fused_h_halo(const FusedCtx<T> &X, int x, int y, int k, int eA, int eB, int hA, bool pml_plane,
                                           bool slots)
 {
@@ -391,23 +391,25 @@ __device__ __forceinline__ T fused_h_halo(const FusedCtx<T> &X, int x, int y, in
         return T(0);
     const int o = (y - (X.y0 - 1)) * BX + x - (X.x0 - XOFF);
     T curl1, curl2;
+    // UNIT: 1/dx is 1 and the multiplications are left out (the same bits)
+    auto scale = [&](T d) { return UNIT ? d : d * PH.inv_dx; };
     if (c == 0)  // Hx: -(dEz/dy) + dEy/dz
     {
         const T *Ez = X.e_tile(eA, 2), *Ey = X.e_tile(eA, 1);
-        curl1 = (Ez[o] - Ez[o + BX]) * PH.inv_dx;
-        curl2 = (Ey[o] - X.e_tile(eB, 1)[o]) * PH.inv_dx;
+        curl1 = scale(Ez[o] - Ez[o + BX]);
+        curl2 = scale(Ey[o] - X.e_tile(eB, 1)[o]);
     }
     else if (c == 1)  // Hy: -(dEx/dz) + dEz/dx
     {
         const T *Ex = X.e_tile(eA, 0), *Ez = X.e_tile(eA, 2);
-        curl1 = (Ex[o] - X.e_tile(eB, 0)[o]) * PH.inv_dx;
-        curl2 = (Ez[o] - Ez[o + 1]) * PH.inv_dx;
+        curl1 = scale(Ex[o] - X.e_tile(eB, 0)[o]);
+        curl2 = scale(Ez[o] - Ez[o + 1]);
     }
     else  // Hz: -(dEy/dx) + dEx/dy
     {
         const T *Ey = X.e_tile(eA, 1), *Ex = X.e_tile(eA, 0);
-        curl1 = (Ey[o] - Ey[o + 1]) * PH.inv_dx;
-        curl2 = (Ex[o] - Ex[o + BX]) * PH.inv_dx;
+        curl1 = scale(Ey[o] - Ey[o + 1]);
+        curl2 = scale(Ex[o] - Ex[o + BX]);
     }
     const int idx = x + y * (int)PH.sy + k * (int)PH.sz;
     const T term = fused_term<T, GC>(X, pml_plane, x, y, k, idx, curl1, curl2, F.psih_in[c][0], F.psih_in[c][1], nullptr,
@@ -965,27 +967,37 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     fast_h_own(std::false_type{});
                 const T *gA0 = X.e_tile(eA, 0), *gA1 = X.e_tile(eA, 1), *gA2 = X.e_tile(eA, 2), *gB0 = X.e_tile(eB, 0),
                         *gB1 = X.e_tile(eB, 1);
-                if (wid >= 6)
+                auto fast_h_halo = [&](auto unit) {
+                    constexpr bool U = decltype(unit)::value;
+                    if (wid >= 6)
+                    {
+                        const int o = lane + XOFF;  // row y0 - 1 of the boxes
+                        if (wid == 7)
+                            X.hn_at(rn, 2, 0, lane + 1) =
+                                (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh);
+                        else
+                            X.hn_at(rn, 0, 0, lane + 1) =
+                                (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 0)[o] + coefH * curl_diff<U>(gA2[o], gA2[o + BX], gA1[o], gB1[o], idh);
+                    }
+                    else if (wid == 5 && lane < 2 * TY)
+                    {
+                        const int v = lane < TY ? lane : lane - TY;
+                        const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
+                        if (lane < TY)
+                            X.hn_at(rn, 2, v + 1, 0) =
+                                (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh);
+                        else
+                            X.hn_at(rn, 1, v + 1, 0) =
+                                (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 1)[o] + coefH * curl_diff<U>(gA0[o], gB0[o], gA2[o], gA2[o + 1], idh);
+                    }
+                };
+                if constexpr (sizeof(T) == 8)
                 {
-                    const int o = lane + XOFF;  // row y0 - 1 of the boxes
-                    if (wid == 7)
-                        X.hn_at(rn, 2, 0, lane + 1) =
-                            (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
-                    else
-                        X.hn_at(rn, 0, 0, lane + 1) =
-                            (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 0)[o] + coefH * ((gA2[o] - gA2[o + BX]) * idh - (gA1[o] - gB1[o]) * idh);
+                    if (unit_dx) fast_h_halo(std::true_type{});
+                    else fast_h_halo(std::false_type{});
                 }
-                else if (wid == 5 && lane < 2 * TY)
-                {
-                    const int v = lane < TY ? lane : lane - TY;
-                    const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
-                    if (lane < TY)
-                        X.hn_at(rn, 2, v + 1, 0) =
-                            (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 2)[o] + coefH * ((gA1[o] - gA1[o + 1]) * idh - (gA0[o] - gA0[o + BX]) * idh);
-                    else
-                        X.hn_at(rn, 1, v + 1, 0) =
-                            (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 1)[o] + coefH * ((gA0[o] - gB0[o]) * idh - (gA2[o] - gA2[o + 1]) * idh);
-                }
+                else
+                    fast_h_halo(std::false_type{});
             }
             else
             {
@@ -1016,10 +1028,17 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 int hx, hy, comp, row, col;
                 if (halo_point(X, wid, lane, hx, hy, comp, row, col))
                 {
+                    auto halo = [&](auto unit) {
+                        constexpr bool U = decltype(unit)::value;
+                        if (comp == 0) return fused_h_halo<T, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        if (comp == 1) return fused_h_halo<T, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        return fused_h_halo<T, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                    };
                     T v;
-                    if (comp == 0) v = fused_h_halo<T, 3>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                    else if (comp == 1) v = fused_h_halo<T, 4>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                    else v = fused_h_halo<T, 5>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                    if constexpr (sizeof(T) == 8)
+                        v = unit_dx ? halo(std::true_type{}) : halo(std::false_type{});
+                    else
+                        v = halo(std::false_type{});
                     X.hn_at(rn, comp, row, col) = v;
                 }
             }
