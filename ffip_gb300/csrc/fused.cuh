@@ -97,8 +97,16 @@ struct FusedShape;
 #ifndef FFIP_FUSED_F64_MINB
 #define FFIP_FUSED_F64_MINB 2
 #endif
+// most z planes per CTA (KCH), and the shorter chunk the fp32 pass takes on
+// grids that give fewer than 20 waves of CTAs at KCH planes (KCH_SHORT):
+// there the shorter jobs balance the geometry-heavy ones better, on large
+// grids the longer ones carry less per-job overhead; the fp64 pass (bound by
+// the fp64 pipe) keeps the longer chunks
 #ifndef FFIP_FUSED_KCH
 #define FFIP_FUSED_KCH 16
+#endif
+#ifndef FFIP_FUSED_F32_KCH_SHORT
+#define FFIP_FUSED_F32_KCH_SHORT 12
 #endif
 #ifndef FFIP_FUSED_F32_MINB_INTERIOR
 #define FFIP_FUSED_F32_MINB_INTERIOR 3
@@ -110,14 +118,15 @@ template <>
 struct FusedShape<float>
 {
     static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 1, BX = 36, SE = FFIP_FUSED_F32_SE,
-                         SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F32_MINB,
+                         SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT,
+                         MINB = FFIP_FUSED_F32_MINB,
                          MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR, STAGE_PSI = 1;
 };
 template <>
 struct FusedShape<double>
 {
     static constexpr int TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 1, BX = 34, SE = FFIP_FUSED_F64_SE,
-                         SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB,
+                         SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, KCH_SHORT = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB,
                          MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR, STAGE_PSI = 0;
 };
 

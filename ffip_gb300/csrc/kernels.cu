@@ -316,13 +316,16 @@ public:
         L.kbeg = kbeg;
         L.kend = std::max(kend, kbeg + 1);
         dim3 block(32, 8);  // 8 warps; each thread owns SH::RPT rows of the tile
-        // z chunk length: at most KCH planes, fewer when the grid has too few
-        // tiles to fill the GPU (each chunk recomputes one H plane, so at
-        // least 4 planes)
+        // z chunk length: KCH planes, KCH_SHORT when that gives fewer than 20
+        // waves of CTAs, fewer still when the grid has too few tiles to fill
+        // the GPU twice (each chunk recomputes one H plane, so at least 4)
         if (!nsm_) check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
         const int64_t tiles = (int64_t)std::max(nbx, 1) * std::max(nby, 1);
-        const int64_t want = 2LL * nsm_ * SH::MINB;  // CTAs for two waves
-        const int kch = (int)std::max<int64_t>(4, std::min<int64_t>(SH::KCH, ((int64_t)(L.kend - L.kbeg) * tiles + want - 1) / want));
+        const int64_t slots = (int64_t)nsm_ * SH::MINB;  // CTAs resident at once
+        const int64_t want = 2 * slots;                  // CTAs for two waves
+        const int64_t zlen = L.kend - L.kbeg;
+        const int kmax = zlen * tiles < 20 * slots * SH::KCH ? SH::KCH_SHORT : SH::KCH;
+        const int kch = (int)std::max<int64_t>(4, std::min<int64_t>(kmax, (zlen * tiles + want - 1) / want));
         const Jobs &J = jobs_for(p, L, nbx, nby, SH::TX, SH::TY, kch);
         int n = 0;
         const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
