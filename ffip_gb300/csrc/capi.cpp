@@ -296,7 +296,7 @@ int ffip_check_inside(const double *req_pts, uint64_t n, const double *poly_pts,
 {
     return guard([&]() -> int {
         if ((n && (!req_pts || !out)) || (m && !poly_pts)) return fail(FFIP_ERR_INVALID, "null argument");
-        if (n > (uint64_t(1) << 40) || m > (uint64_t(1) << 40)) return fail(FFIP_ERR_INVALID, "array too large");
+        if (n > (uint64_t(1) << 31) || m > (uint64_t(1) << 31)) return fail(FFIP_ERR_INVALID, "array too large");
         return ffipg::check_inside(req_pts, n, poly_pts, m, out);
     });
 }
