@@ -159,8 +159,8 @@ int ffip_to_convolve(const double *in1, uint64_t n0, uint64_t n1, const double *
  * vertices (poly_pts[2j], poly_pts[2j+1]) -- CGAL's Polygon_2::bounded_side
  * == ON_BOUNDED_SIDE -- and 0 on an edge, on a vertex or outside.  The polygon
  * is simple; its first vertex may be repeated at the end (a closed ring).
- * Orientation tests are exact.  Host buffers; computed on the current CUDA
- * device. */
+ * Orientation tests are exact.  At most 2^31 points and 2^31 vertices.  Host
+ * buffers; computed on the current CUDA device. */
 int ffip_check_inside(const double *req_pts, uint64_t n, const double *poly_pts, uint64_t m, uint8_t *out);
 
 /* ffip_transpose without any device allocation.  No counterpart in the
