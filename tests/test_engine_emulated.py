@@ -91,3 +91,20 @@ def test_set_source_data_equals_fresh_run(lib):
             s.set_source_data({"inhom source amplitude 0": amp[:-1]})
     for k in fresh:
         assert np.array_equal(fresh[k], again[k]), k
+
+
+def test_large_design_workload_builds_and_steps(lib):
+    """The large design workload's configuration (Drude backplane, Lorentz /
+    vacuum density box, three DFT planes at many frequencies), scaled down,
+    builds and steps on the emulated engine with slots from both media."""
+    from ffip_gb300 import native, workloads
+    cfg, ds = workloads.large_design(n=48, nz=40, pml=6, design=(24, 6), nfreq=4, steps=10, precision="fp32")
+    with native.NativeSim(cfg, ds, lib=lib) as s:
+        s.run()
+        out = s.outputs()
+        st = s.stats()
+    assert st["time_step"] == 10 and st["yee_cells"] == 48 * 48 * 40
+    groups = [g for g in out if g.startswith("volume fields dft")]
+    assert len(groups) == 3
+    for g in groups:
+        assert out[g]["real"].shape[0] == 4
