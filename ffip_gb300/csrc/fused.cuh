@@ -85,6 +85,9 @@ struct FusedShape;
 #ifndef FFIP_FUSED_F32_MINB
 #define FFIP_FUSED_F32_MINB 3
 #endif
+#ifndef FFIP_FUSED_F32_STAGE_PSI
+#define FFIP_FUSED_F32_STAGE_PSI 1
+#endif
 #ifndef FFIP_FUSED_F64_RPT
 #define FFIP_FUSED_F64_RPT 1
 #endif
@@ -120,7 +123,7 @@ struct FusedShape<float>
     static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 1, BX = 36, SE = FFIP_FUSED_F32_SE,
                          SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT,
                          MINB = FFIP_FUSED_F32_MINB,
-                         MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR, STAGE_PSI = 1;
+                         MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR, STAGE_PSI = FFIP_FUSED_F32_STAGE_PSI;
 };
 template <>
 struct FusedShape<double>
