@@ -120,6 +120,28 @@ int ffip_step_timed(ffip_sim *sim, int64_t n, double *ms)
     });
 }
 
+int ffip_step_timed_pass(ffip_sim *sim, int64_t n, double *ms, double *pass_ms)
+{
+    return guard([&]() -> int {
+        if (!sim || !ms || !pass_ms) return fail(FFIP_ERR_INVALID, "null argument");
+        if (n < 0) return fail(FFIP_ERR_INVALID, "negative step count");
+        sim->be->pass_ms();  // drop passes timed earlier
+        sim->be->time_passes(true);
+        try
+        {
+            *ms = sim->be->timed([&]() { sim->eng->step(n); });
+        }
+        catch (...)
+        {
+            sim->be->time_passes(false);
+            throw;
+        }
+        sim->be->time_passes(false);
+        *pass_ms = sim->be->pass_ms();
+        return FFIP_OK;
+    });
+}
+
 int ffip_run(ffip_sim *sim, const char *stop_json)
 {
     return guard([&]() -> int {
@@ -227,6 +249,7 @@ int ffip_get_stats(ffip_sim *sim, ffip_stats *st)
         st->dt = p.dt;
         st->dx = p.dx;
         st->bytes_per_step = sim->eng->bytes_per_step();
+        st->pass_bytes_per_step = sim->eng->pass_bytes_per_step();
         st->kernel_launches = sim->eng->launches();
         st->fused = sim->eng->fused() ? 1 : 0;
         st->fp32 = p.precision_fp32 ? 1 : 0;

@@ -61,6 +61,7 @@ public:
     void set_density(const std::string &dataset, const double *rho, uint64_t n) override;
     void set_source_data(const std::map<std::string, std::vector<double>> &data) override;
     double bytes_per_step() const override { return bytes_per_step_; }
+    double pass_bytes_per_step() const override { return pass_bytes_per_step_; }
 
 private:
     Plan P_;
@@ -88,6 +89,7 @@ private:
     double *scratch_{nullptr};
     int64_t scratch_n_{0};
     double bytes_per_step_{0};
+    double pass_bytes_per_step_{0};
 
     // allocation lifetimes: with the engine, until the media change, until
     // the sources change
@@ -578,6 +580,7 @@ void Engine<T>::compute_bytes()
             if (np) b += s * 4 * np;
         }
     }
+    pass_bytes_per_step_ = b;
     for (auto &U : P_.units) b += 32.0 * (double)U.npoints() * (double)U.freqs.size();
     bytes_per_step_ = b;
 }

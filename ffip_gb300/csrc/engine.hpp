@@ -56,6 +56,14 @@ struct Backend
     virtual const char *name() const = 0;
     // device time of f() between events on the backend's stream (ms)
     virtual double timed(const std::function<void()> &f) = 0;
+    // while on, every fused pass is bracketed by timing events on the
+    // backend's stream (from the launch of the first k_fused instance to the
+    // point where both instances, and the face-layer kernels beside them,
+    // have finished); pass_ms() waits for them and returns the summed
+    // device time (ms) of the passes since the last call, 0 where the
+    // backend does not time passes
+    virtual void time_passes(bool on) { (void)on; }
+    virtual double pass_ms() { return 0.0; }
     uint64_t h2d_bytes{0}, d2h_bytes{0};
 };
 
@@ -84,6 +92,8 @@ public:
     virtual int64_t launches() const = 0;  // kernel launches issued so far
     // algorithmic bytes of one full time step, and the number of Yee cells
     virtual double bytes_per_step() const = 0;
+    // bytes_per_step without the DFT sums (the field pass's share)
+    virtual double pass_bytes_per_step() const = 0;
 };
 
 std::unique_ptr<EngineBase> make_engine(Plan &&plan, Backend *be);

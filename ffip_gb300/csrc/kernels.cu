@@ -156,6 +156,11 @@ public:
         if (fork_) cudaEventDestroy(fork_);
         if (join_) cudaEventDestroy(join_);
         if (face_h_) cudaEventDestroy(face_h_);
+        for (auto &ev : pass_ev_)
+        {
+            cudaEventDestroy(ev.first);
+            cudaEventDestroy(ev.second);
+        }
         if (dft_)
         {
             cudaEventDestroy(dft_ready_);
@@ -345,6 +350,23 @@ public:
             check(cudaEventRecord(fork_, stream_), "cudaEventRecord");
             check(cudaStreamWaitEvent(side_, fork_, 0), "cudaStreamWaitEvent");
         }
+        cudaEvent_t pass_end = nullptr;
+        if (time_pass_)
+        {
+            if (pass_n_ == pass_ev_.size())
+            {
+                cudaEvent_t a, b;
+                check(cudaEventCreate(&a), "cudaEventCreate");
+                if (cudaEventCreate(&b) != cudaSuccess)
+                {
+                    cudaEventDestroy(a);
+                    throw std::runtime_error("cudaEventCreate failed");
+                }
+                pass_ev_.emplace_back(a, b);
+            }
+            check(cudaEventRecord(pass_ev_[pass_n_].first, stream_), "cudaEventRecord");
+            pass_end = pass_ev_[pass_n_++].second;
+        }
         // the H half of k_face reads only step-n fields: first on the side
         // stream, ahead of the interior instance
         if (nface > 0)
@@ -384,6 +406,7 @@ public:
             check(cudaEventRecord(join_, side_), "cudaEventRecord");
             check(cudaStreamWaitEvent(stream_, join_, 0), "cudaStreamWaitEvent");
         }
+        if (pass_end) check(cudaEventRecord(pass_end, stream_), "cudaEventRecord");
         if (nface > 0 && !early_face)
         {
             k_face<T, true><<<face_blocks, 256, 0, stream_>>>(L);
@@ -631,6 +654,21 @@ public:
         cudaEventDestroy(b);
         return ms;
     }
+    void time_passes(bool on) override { time_pass_ = on; }
+    double pass_ms() override
+    {
+        use();
+        double ms = 0;
+        for (size_t i = 0; i < pass_n_; ++i)
+        {
+            float t = 0;
+            check(cudaEventSynchronize(pass_ev_[i].second), "cudaEventSynchronize");
+            check(cudaEventElapsedTime(&t, pass_ev_[i].first, pass_ev_[i].second), "cudaEventElapsedTime");
+            ms += t;
+        }
+        pass_n_ = 0;
+        return ms;
+    }
     // the handle's stream, ordered after the DFT sums already issued
     cudaStream_t stream()
     {
@@ -654,6 +692,11 @@ private:
     cudaEvent_t dft_ready_{nullptr}, dft_join_{nullptr}, dft_done_[2]{nullptr, nullptr};
     bool dft_valid_[2]{false, false}, dft_pending_{false};
     int64_t passes_{0};
+    // timing events of the fused passes (time_passes / pass_ms): pairs in
+    // use and the pool, reused across calls
+    bool time_pass_{false};
+    size_t pass_n_{0};
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pass_ev_;
 };
 } // namespace
 

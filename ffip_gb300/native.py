@@ -11,7 +11,7 @@ from __future__ import annotations
 import ctypes
 import json
 import os
-from typing import Dict, Optional
+from typing import Dict, Optional, Tuple
 
 import numpy as np
 
@@ -30,12 +30,12 @@ class Stats(ctypes.Structure):
     _fields_ = [("time_step", ctypes.c_int64), ("yee_cells", ctypes.c_int64), ("array_cells", ctypes.c_int64),
                 ("dt", ctypes.c_double), ("dx", ctypes.c_double), ("bytes_per_step", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("fused", ctypes.c_int32), ("fp32", ctypes.c_int32),
-                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64), ("pass_bytes_per_step", ctypes.c_double)]
 
 
-EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_run", "ffip_output_count", "ffip_output_group", "ffip_output_array",
-           "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync", "ffip_stream", "ffip_destroy",
-           "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc",
+EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_step_timed_pass", "ffip_run", "ffip_output_count",
+           "ffip_output_group", "ffip_output_array", "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync",
+           "ffip_stream", "ffip_destroy", "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc",
            "ffip_set_source_data", "ffip_to_convolve", "ffip_check_inside"]
 
 
@@ -44,6 +44,7 @@ def _declare(lib):
     lib.ffip_create.argtypes = [ctypes.c_char_p, ctypes.POINTER(Dataset), U64, ctypes.POINTER(P)]
     lib.ffip_step.argtypes = [P, I64]
     lib.ffip_step_timed.argtypes = [P, I64, ctypes.POINTER(ctypes.c_double)]
+    lib.ffip_step_timed_pass.argtypes = [P, I64, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     lib.ffip_run.argtypes = [P, ctypes.c_char_p]
     lib.ffip_output_count.argtypes = [P, ctypes.POINTER(ctypes.c_int)]
     lib.ffip_output_group.argtypes = [P, ctypes.c_int, ctypes.c_char_p, U64]
@@ -124,6 +125,14 @@ class NativeSim:
         ms = ctypes.c_double()
         self._check(self.lib.ffip_step_timed(self.h, int(n), ctypes.byref(ms)))
         return ms.value
+
+    def step_timed_pass(self, n: int) -> Tuple[float, float]:
+        """Runs n steps; returns (device time of the n steps, summed device
+        time of their fused field passes), both in ms; the second is 0 for
+        the separate H and E passes."""
+        ms, pms = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.ffip_step_timed_pass(self.h, int(n), ctypes.byref(ms), ctypes.byref(pms)))
+        return ms.value, pms.value
 
     def run(self, stop: Optional[dict] = None):
         self._check(self.lib.ffip_run(self.h, json.dumps(stop).encode() if stop is not None else None))

@@ -59,6 +59,7 @@ typedef struct ffip_stats {
     int32_t fp32;            /* 1 = fp32 field state, 0 = fp64 */
     uint64_t h2d_bytes;      /* host->device bytes copied so far */
     uint64_t d2h_bytes;      /* device->host bytes copied so far */
+    double pass_bytes_per_step; /* bytes_per_step without the DFT sums: the field pass's share */
 } ffip_stats;
 
 /* Simulation::init(config) (src/simulation.cpp:127-188): parses the config
@@ -77,6 +78,13 @@ int ffip_step(ffip_sim *sim, int64_t n_steps);
  * before and after the n steps; *ms receives the elapsed device time.
  * Blocks until the steps have finished. */
 int ffip_step_timed(ffip_sim *sim, int64_t n_steps, double *ms);
+
+/* ffip_step_timed that also times the field pass of every step: CUDA events
+ * on the handle's stream from the launch of the first k_fused instance to
+ * the point where both instances (and the face-layer kernels that run beside
+ * them) have finished, summed over the n steps into *pass_ms.  *pass_ms is 0
+ * for the separate H and E passes ("engine": "unfused"). */
+int ffip_step_timed_pass(ffip_sim *sim, int64_t n_steps, double *ms, double *pass_ms);
 
 /* Simulation::run(stop_cond) (src/simulation.cpp:903-958): "time", "decay"
  * or DFT steady-state stop conditions.  stop_json == NULL uses the config's

@@ -227,3 +227,31 @@ def test_fused_asymmetric_cpml_and_odd_sizes_match_separate_passes():
     for prec in ("fp64", "fp32"):
         for k in outs["unfused", prec]:
             assert np.array_equal(outs["unfused", prec][k], outs["fused", prec][k]), (prec, k)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_pass_timing_leaves_results_unchanged(precision):
+    """ffip_step_timed_pass brackets every fused pass with timing events: the
+    DFT sums equal those of plain ffip_step, and the summed pass time lies
+    inside the steps' device time."""
+    from ffip_gb300 import native
+    cfg, ds, _ = load("dispersive")
+    cfg = copy.deepcopy(cfg)
+    cfg["precision"] = precision
+    steps = int(round(cfg["stop condition"]["time"] / (cfg["courant number"] / cfg["resolution"])))
+    outs = []
+    for timed in (False, True):
+        s = native.NativeSim(cfg, ds)
+        try:
+            assert s.stats()["fused"] == 1
+            if timed:
+                ms, pms = s.step_timed_pass(steps)
+                assert 0 < pms <= ms
+                assert 0 < s.stats()["pass_bytes_per_step"] < s.stats()["bytes_per_step"]
+            else:
+                s.step(steps)
+            outs.append(flatten(s.outputs()))
+        finally:
+            s.close()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
