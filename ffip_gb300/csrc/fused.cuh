@@ -133,11 +133,25 @@ struct FusedShape<double>
                          MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR, STAGE_PSI = 0;
 };
 
-// CPML coefficients of one position along one axis: b, c, 1/k
+// CPML coefficients of one position along one axis: b, c, 1/k, and in the
+// fourth slot the bit pattern of the integer 1 where c != 0 (0 elsewhere):
+// the CPML paths test c != 0 on the integer pipe (a floating-point compare
+// issues on the fp64 pipe, which bounds the fp64 pass)
 template <typename T>
 struct alignas(4 * sizeof(T)) PmlCoef
 {
-    T b, c, ik, pad;
+    T b, c, ik, nzbits;
+    __device__ __forceinline__ bool nz() const
+    {
+        if constexpr (sizeof(T) == 8) return __double2loint(nzbits) != 0;
+        else return __float_as_uint(nzbits) != 0u;
+    }
+    __device__ __forceinline__ void set_nz()
+    {
+        const bool on = c != T(0);
+        if constexpr (sizeof(T) == 8) nzbits = __hiloint2double(0, on ? 1 : 0);
+        else nzbits = __uint_as_float(on ? 1u : 0u);
+    }
 };
 
 template <typename T>
@@ -343,11 +357,10 @@ struct FusedCtx
         return a == 0 ? base + q * LY::NX : a == 1 ? base + 2 * LY::NX + q * LY::NY : base + 2 * (LY::NX + LY::NY) + q * LY::NZ;
     }
     template <int A>
-    __device__ __forceinline__ T pml_val(int q, int v, int pos) const
+    __device__ __forceinline__ const PmlCoef<T> &pml_at(int q, int pos) const
     {
         const int o = A == 0 ? pos - (x0 - 1) : A == 1 ? pos - (y0 - 1) : pos - (k0 - 1);
-        const PmlCoef<T> &e = tab(A, q)[o];
-        return v == 0 ? e.b : v == 1 ? e.c : e.ik;
+        return tab(A, q)[o];
     }
 };
 
@@ -359,12 +372,11 @@ __device__ __forceinline__ T fused_term(const FusedCtx<T> &X, bool pml_plane, in
 {
     using C = CompT<GC>;
     if (!pml_plane) return curl1 - curl2;
-    const int p1 = pick<C::a1>(x, y, k), p2 = pick<C::a2>(x, y, k);
-    const T cv1 = X.template pml_val<C::a1>(C::q1, 1, p1), cv2 = X.template pml_val<C::a2>(C::q2, 1, p2);
-    if (cv1 == T(0) && cv2 == T(0)) return curl1 - curl2;
-    return pml_combine(cv1, cv2, X.template pml_val<C::a1>(C::q1, 0, p1), X.template pml_val<C::a2>(C::q2, 0, p2),
-                       X.template pml_val<C::a1>(C::q1, 2, p1), X.template pml_val<C::a2>(C::q2, 2, p2), curl1, curl2, pin1,
-                       pin2, pout1, pout2, idx);
+    const PmlCoef<T> A1 = X.template pml_at<C::a1>(C::q1, pick<C::a1>(x, y, k));
+    const PmlCoef<T> A2 = X.template pml_at<C::a2>(C::q2, pick<C::a2>(x, y, k));
+    const bool n1 = A1.nz(), n2 = A2.nz();
+    if (!n1 && !n2) return curl1 - curl2;
+    return pml_combine_nz(n1, n2, A1.c, A2.c, A1.b, A2.b, A1.ik, A2.ik, curl1, curl2, pin1, pin2, pout1, pout2, idx);
 }
 
 // (a - b) / dx - (c - d) / dx of the plain curl update, 1/dx given; UNIT:
@@ -383,8 +395,9 @@ template <typename T>
 __device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &A2, T curl1, T curl2, T psi1, T psi2, T *ps1,
                                         T *ps2)
 {
-    if (A1.c == T(0) && A2.c == T(0)) return curl1 - curl2;
-    return pml_term(A1.c, A2.c, A1.b, A2.b, A1.ik, A2.ik, curl1, curl2, psi1, psi2, ps1, ps2);
+    const bool n1 = A1.nz(), n2 = A2.nz();
+    if (!n1 && !n2) return curl1 - curl2;
+    return pml_term_nz(n1, n2, A1.c, A2.c, A1.b, A2.b, A1.ik, A2.ik, curl1, curl2, psi1, psi2, ps1, ps2);
 }
 
 // H at the new level of a halo point (not owned: nothing is written),
@@ -512,8 +525,8 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
         if (owned && val)
         {
             F.hout[c][idx] = v;
-            if (hc[a1].c != T(0)) F.psih_out[c][0][idx] = ps1;
-            if (hc[a2].c != T(0)) F.psih_out[c][1][idx] = ps2;
+            if (hc[a1].nz()) F.psih_out[c][0][idx] = ps1;
+            if (hc[a2].nz()) F.psih_out[c][1][idx] = ps2;
         }
     }
 }
@@ -558,8 +571,8 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
             }
             else
             {
-                if (ve && ec[a1].c != T(0)) pe[c][0] = PE.psi[c][0][idx];
-                if (ve && ec[a2].c != T(0)) pe[c][1] = PE.psi[c][1][idx];
+                if (ve && ec[a1].nz()) pe[c][0] = PE.psi[c][0][idx];
+                if (ve && ec[a2].nz()) pe[c][1] = PE.psi[c][1][idx];
             }
         }
     }
@@ -596,8 +609,8 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
         if ((vb >> c) & 1u)
         {
             F.eout[c][idx] = v;
-            if (ec[a1].c != T(0)) PE.psi[c][0][idx] = ps1;
-            if (ec[a2].c != T(0)) PE.psi[c][1][idx] = ps2;
+            if (ec[a1].nz()) PE.psi[c][0][idx] = ps1;
+            if (ec[a2].nz()) PE.psi[c][1][idx] = ps2;
         }
     }
 }
@@ -692,9 +705,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 e.b = in ? ld_keep(PE.pb[a][q] + pos, keep) : T(0);
                 e.c = in ? ld_keep(PE.pc[a][q] + pos, keep) : T(0);
                 e.ik = in ? ld_keep(PE.pik[a][q] + pos, keep) : T(1);
-                e.pad = T(0);
+                e.set_nz();
                 X.tab(a, q)[o] = e;
-                if (a < 2 && e.c != T(0)) tile_pml = true;
+                if (a < 2 && e.nz()) tile_pml = true;
             }
         }
     }
@@ -833,19 +846,19 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             for (int c = 0; c < 3; ++c) ph[r][c][0] = ph[r][c][1] = T(0);
         if (do_h && pml_h)
         {
-            const T cx = X.tab(0, 1)[lane + 1].c, cz = X.tab(2, 1)[q].c;  // H side (parity 1)
+            const bool cx = X.tab(0, 1)[lane + 1].nz(), cz = X.tab(2, 1)[q].nz();  // H side (parity 1): c != 0
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
             {
-                const T ch[3] = {cx, X.tab(1, 1)[r0 + r + 1].c, cz};
+                const bool ch[3] = {cx, X.tab(1, 1)[r0 + r + 1].nz(), cz};
                 const unsigned vb = vxy[r] & (wh >> kInfoZValidShift);
 #pragma unroll
                 for (int c = 0; c < 3; ++c)
                 {
                     const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
                     const bool vh = (vb >> (3 + c)) & 1u;
-                    if (vh && ch[a1] != T(0)) ph[r][c][0] = F.psih_in[c][0][idx + r * sy];
-                    if (vh && ch[a2] != T(0)) ph[r][c][1] = F.psih_in[c][1][idx + r * sy];
+                    if (vh && ch[a1]) ph[r][c][0] = F.psih_in[c][0][idx + r * sy];
+                    if (vh && ch[a2]) ph[r][c][1] = F.psih_in[c][1][idx + r * sy];
                 }
             }
         }
@@ -855,11 +868,11 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         // place by this thread only), copied during the waits and the H update
         if (STG && do_e && pml_e)
         {
-            const T cx = X.tab(0, 0)[lane + 1].c, cz = X.tab(2, 0)[q - 1].c;  // E side (parity 0)
+            const bool cx = X.tab(0, 0)[lane + 1].nz(), cz = X.tab(2, 0)[q - 1].nz();  // E side (parity 0): c != 0
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
             {
-                const T ce[3] = {cx, X.tab(1, 0)[r0 + r + 1].c, cz};
+                const bool ce[3] = {cx, X.tab(1, 0)[r0 + r + 1].nz(), cz};
                 const unsigned vb = vxy[r] & (we >> kInfoZValidShift);
 #pragma unroll
                 for (int c = 0; c < 3; ++c)
@@ -867,8 +880,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
                     const bool ve = (vb >> c) & 1u;
                     T *dst = pstage + (LY::PSI_E + (r * 3 + c) * 2) * NTH;
-                    if (ve && ce[a1] != T(0)) cp_async_elem(dst, PE.psi[c][0] + idx_e + r * sy);
-                    if (ve && ce[a2] != T(0)) cp_async_elem(dst + NTH, PE.psi[c][1] + idx_e + r * sy);
+                    if (ve && ce[a1]) cp_async_elem(dst, PE.psi[c][0] + idx_e + r * sy);
+                    if (ve && ce[a2]) cp_async_elem(dst + NTH, PE.psi[c][1] + idx_e + r * sy);
                 }
             }
         }

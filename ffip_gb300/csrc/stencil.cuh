@@ -139,28 +139,60 @@ FFIP_HD int pick(int i, int j, int k)
 // CPML combination at a point where c1 or c2 is non-zero (PML_Stepping::step,
 // src/fields.cpp:98-107), from psi values already loaded (psi1/psi2 are not
 // used where the matching c is 0).  *ps1/*ps2 receive the new psi.
+// fused multiply-add with one rounding, the same on the host and the device
+FFIP_HD float fma_rn(float a, float b, float c) { return fmaf(a, b, c); }
+FFIP_HD double fma_rn(double a, double b, double c) { return fma(a, b, c); }
+
+// the two halves of the CPML update, roundings fixed (explicit fma) so that
+// every code path that forms them gives the same bits: the new psi
+// b psi + c curl, and the increment psi1 - psi2 + curl1 / k1 - curl2 / k2
+template <typename T>
+FFIP_HD T pml_psi(T b, T psi, T cv, T curl)
+{
+    return fma_rn(cv, curl, b * psi);
+}
+template <typename T>
+FFIP_HD T pml_sum(T p1, T p2, T ik1, T ik2, T curl1, T curl2)
+{
+    return fma_rn(-curl2, ik2, fma_rn(curl1, ik1, p1 - p2));
+}
+
+// n1 / n2: cv1 / cv2 are non-zero (callers that hold these as integer flags
+// pass them, and no floating-point compare is issued)
+template <typename T>
+FFIP_HD T pml_term_nz(bool n1, bool n2, T cv1, T cv2, T b1, T b2, T ik1, T ik2, T curl1, T curl2, T psi1, T psi2, T *ps1,
+                      T *ps2)
+{
+    const T p1 = n1 ? pml_psi(b1, psi1, cv1, curl1) : T(0);
+    const T p2 = n2 ? pml_psi(b2, psi2, cv2, curl2) : T(0);
+    *ps1 = p1;
+    *ps2 = p2;
+    return pml_sum(p1, p2, ik1, ik2, curl1, curl2);
+}
 template <typename T>
 FFIP_HD T pml_term(T cv1, T cv2, T b1, T b2, T ik1, T ik2, T curl1, T curl2, T psi1, T psi2, T *ps1, T *ps2)
 {
-    const T p1 = cv1 != T(0) ? b1 * psi1 + cv1 * curl1 : T(0);
-    const T p2 = cv2 != T(0) ? b2 * psi2 + cv2 * curl2 : T(0);
-    *ps1 = p1;
-    *ps2 = p2;
-    return p1 - p2 + curl1 * ik1 - curl2 * ik2;
+    return pml_term_nz(cv1 != T(0), cv2 != T(0), cv1, cv2, b1, b2, ik1, ik2, curl1, curl2, psi1, psi2, ps1, ps2);
 }
 
 // The same with psi read from pin and, when pout is not null, written to pout.
 template <typename T>
+FFIP_HD T pml_combine_nz(bool n1, bool n2, T cv1, T cv2, T b1, T b2, T ik1, T ik2, T curl1, T curl2, const T *pin1,
+                         const T *pin2, T *pout1, T *pout2, int64_t idx)
+{
+    const T psi1 = n1 ? pin1[idx] : T(0);
+    const T psi2 = n2 ? pin2[idx] : T(0);
+    T ps1, ps2;
+    const T t = pml_term_nz(n1, n2, cv1, cv2, b1, b2, ik1, ik2, curl1, curl2, psi1, psi2, &ps1, &ps2);
+    if (n1 && pout1) pout1[idx] = ps1;
+    if (n2 && pout2) pout2[idx] = ps2;
+    return t;
+}
+template <typename T>
 FFIP_HD T pml_combine(T cv1, T cv2, T b1, T b2, T ik1, T ik2, T curl1, T curl2, const T *pin1, const T *pin2, T *pout1,
                       T *pout2, int64_t idx)
 {
-    const T psi1 = cv1 != T(0) ? pin1[idx] : T(0);
-    const T psi2 = cv2 != T(0) ? pin2[idx] : T(0);
-    T ps1, ps2;
-    const T t = pml_term(cv1, cv2, b1, b2, ik1, ik2, curl1, curl2, psi1, psi2, &ps1, &ps2);
-    if (cv1 != T(0) && pout1) pout1[idx] = ps1;
-    if (cv2 != T(0) && pout2) pout2[idx] = ps2;
-    return t;
+    return pml_combine_nz(cv1 != T(0), cv2 != T(0), cv1, cv2, b1, b2, ik1, ik2, curl1, curl2, pin1, pin2, pout1, pout2, idx);
 }
 
 // curl increment of accdb at a point, CPML tables read from global memory
@@ -185,10 +217,6 @@ FFIP_HD int slot_of(const SlotView<T> &S, int My, int i, int j, int k, int64_t i
     const RowRange r = S.rows[j + (int64_t)k * My];
     return (i >= r.lo && i <= r.hi) ? S.map[idx] : -1;
 }
-
-// fused multiply-add with one rounding, the same on the host and the device
-FFIP_HD float fma_rn(float a, float b, float c) { return fmaf(a, b, c); }
-FFIP_HD double fma_rn(double a, double b, double c) { return fma(a, b, c); }
 
 // one pole of the (P, J) update: J_new = d1 P + d2 J + amp c3 E_old, with
 // its roundings fixed (explicit fma), so that every kernel that updates a
