@@ -353,6 +353,9 @@ public:
         cudaEvent_t pass_end = nullptr;
         if (time_pass_)
         {
+            // at most kPassEvents pairs: fold the elapsed times of a full pool
+            // into the running sum (waits for the passes already issued)
+            if (pass_n_ == kPassEvents) pass_acc_ += drain_passes();
             if (pass_n_ == pass_ev_.size())
             {
                 cudaEvent_t a, b;
@@ -658,6 +661,13 @@ public:
     double pass_ms() override
     {
         use();
+        const double ms = pass_acc_ + drain_passes();
+        pass_acc_ = 0;
+        return ms;
+    }
+    // summed elapsed time of the event pairs in use; frees them
+    double drain_passes()
+    {
         double ms = 0;
         for (size_t i = 0; i < pass_n_; ++i)
         {
@@ -694,8 +704,10 @@ private:
     int64_t passes_{0};
     // timing events of the fused passes (time_passes / pass_ms): pairs in
     // use and the pool, reused across calls
+    static constexpr size_t kPassEvents = 1024;
     bool time_pass_{false};
     size_t pass_n_{0};
+    double pass_acc_{0};
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pass_ev_;
 };
 } // namespace

@@ -83,7 +83,8 @@ int ffip_step_timed(ffip_sim *sim, int64_t n_steps, double *ms);
  * on the handle's stream from the launch of the first k_fused instance to
  * the point where both instances (and the face-layer kernels that run beside
  * them) have finished, summed over the n steps into *pass_ms.  *pass_ms is 0
- * for the separate H and E passes ("engine": "unfused"). */
+ * for the separate H and E passes ("engine": "unfused").  Every 1024 passes
+ * the host waits for the passes issued so far (the events are reused). */
 int ffip_step_timed_pass(ffip_sim *sim, int64_t n_steps, double *ms, double *pass_ms);
 
 /* Simulation::run(stop_cond) (src/simulation.cpp:903-958): "time", "decay"

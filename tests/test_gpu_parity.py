@@ -230,15 +230,18 @@ def test_fused_asymmetric_cpml_and_odd_sizes_match_separate_passes():
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_pass_timing_leaves_results_unchanged(precision):
-    """ffip_step_timed_pass brackets every fused pass with timing events: the
-    DFT sums equal those of plain ffip_step, and the summed pass time lies
-    inside the steps' device time."""
+@pytest.mark.parametrize("case,steps", [("dispersive", None), ("vacuum_pml", 2100)])
+def test_pass_timing_leaves_results_unchanged(precision, case, steps):
+    """ffip_step_timed_pass brackets every fused pass with timing events (a
+    pool of 1024 pairs, folded into a running sum when full: 2100 steps fold
+    twice): the DFT sums equal those of plain ffip_step, and the summed pass
+    time lies inside the steps' device time."""
     from ffip_gb300 import native
-    cfg, ds, _ = load("dispersive")
+    cfg, ds, _ = load(case)
     cfg = copy.deepcopy(cfg)
     cfg["precision"] = precision
-    steps = int(round(cfg["stop condition"]["time"] / (cfg["courant number"] / cfg["resolution"])))
+    if steps is None:
+        steps = int(round(cfg["stop condition"]["time"] / (cfg["courant number"] / cfg["resolution"])))
     outs = []
     for timed in (False, True):
         s = native.NativeSim(cfg, ds)
