@@ -134,23 +134,42 @@ struct FusedShape<double>
 };
 
 // CPML coefficients of one position along one axis: b, c, 1/k, and in the
-// fourth slot the bit pattern of the integer 1 where c != 0 (0 elsewhere):
-// the CPML paths test c != 0 on the integer pipe (a floating-point compare
-// issues on the fp64 pipe, which bounds the fp64 pass)
+// fourth slot the bit pattern of an integer flag word, bit 0 = (c != 0) and
+// (fp64) bit 1 = (c != 0 or 1/k != 1): the CPML paths test these on the
+// integer pipe (a floating-point compare issues on the fp64 pipe, which
+// bounds the fp64 pass).  none(): a position without CPML (c = 0, 1/k = 1).
 template <typename T>
 struct alignas(4 * sizeof(T)) PmlCoef
 {
-    T b, c, ik, nzbits;
+    T b, c, ik, flagbits;
+    __device__ __forceinline__ unsigned flags() const
+    {
+        if constexpr (sizeof(T) == 8) return (unsigned)__double2loint(flagbits);
+        else return __float_as_uint(flagbits);
+    }
     __device__ __forceinline__ bool nz() const
     {
-        if constexpr (sizeof(T) == 8) return __double2loint(nzbits) != 0;
-        else return __float_as_uint(nzbits) != 0u;
+        if constexpr (sizeof(T) == 8) return flags() & 1u;
+        else return flags() != 0u;  // fp32 keeps bit 0 only
     }
-    __device__ __forceinline__ void set_nz()
+    __device__ __forceinline__ bool active() const
     {
-        const bool on = c != T(0);
-        if constexpr (sizeof(T) == 8) nzbits = __hiloint2double(0, on ? 1 : 0);
-        else nzbits = __uint_as_float(on ? 1u : 0u);
+        static_assert(sizeof(T) == 8, "the fp32 flag word holds bit 0 only");
+        return flags() & 2u;
+    }
+    __device__ __forceinline__ void set_flags()
+    {
+        if constexpr (sizeof(T) == 8)
+            flagbits = __hiloint2double(0, (c != T(0) ? 3 : 0) | (ik != T(1) ? 2 : 0));
+        else
+            flagbits = __uint_as_float(c != T(0) ? 1u : 0u);
+    }
+    __device__ __forceinline__ static PmlCoef none()
+    {
+        PmlCoef e;
+        e.b = e.c = e.flagbits = T(0);
+        e.ik = T(1);
+        return e;
     }
 };
 
@@ -173,7 +192,7 @@ struct FusedLayout
     // CPML instance with STAGE_PSI: E-side psi of the own points staged by
     // cp.async, one slot of 256 elements (one per thread) per
     // [row][component][axis]
-    static constexpr int PSI_OFF = (INFO_OFF + NZ * 4 + 15) / 16 * 16;
+    static constexpr int PSI_OFF = (INFO_OFF + (NZ + 1) * 4 + 15) / 16 * 16;  // NZ plane words + the tile's axis word
     static constexpr int PSI_E = 0;
     static constexpr int PSI_SLOTS = SH::STAGE_PSI ? 6 * SH::RPT : 0;
     static constexpr int SMEM = PSI_OFF;  // the instance without CPML code
@@ -392,10 +411,9 @@ __device__ __forceinline__ T curl_diff(T a, T b, T c, T d, T inv)
 // curl term of one component from its two curls with the CPML coefficients
 // of its two curl axes (cv == 0 on both: plain curl, as Curl_Stepping)
 template <typename T>
-__device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &A2, T curl1, T curl2, T psi1, T psi2, T *ps1,
-                                        T *ps2)
+__device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &A2, bool n1, bool n2, T curl1, T curl2, T psi1,
+                                        T psi2, T *ps1, T *ps2)
 {
-    const bool n1 = A1.nz(), n2 = A2.nz();
     if (!n1 && !n2) return curl1 - curl2;
     return pml_term_nz(n1, n2, A1.c, A2.c, A1.b, A2.b, A1.ik, A2.ik, curl1, curl2, psi1, psi2, ps1, ps2);
 }
@@ -463,8 +481,10 @@ __device__ __forceinline__ bool halo_point(const FusedCtx<T> &X, int wid, int la
 
 // General H(k) at this thread's own point of tile row `row`: validity bits,
 // CPML from the staged tables (psi values ph loaded by the caller), material
-// slots, DFT.
-template <typename T, bool FULL = true, bool UNIT = false>
+// slots, DFT.  AX: the axes (bit a) along which the tile plane may have CPML
+// at its own points; the others are known to have none (c = 0, 1/k = 1) and
+// their terms are left out of the code (the same bits).
+template <typename T, bool FULL = true, bool UNIT = false, int AX = 7>
 __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int row, int eA, int eB, int hA, int slot_new,
                                               unsigned vb, bool owned, bool pml, bool slots, bool dft, int idx,
                                               const T (&ph)[3][2])
@@ -500,17 +520,18 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
     PmlCoef<T> hc[3] = {};  // per axis, parity 1
     if (pml)
     {
-        hc[0] = X.tab(0, 1)[tx + 1];
-        hc[1] = X.tab(1, 1)[row + 1];
-        hc[2] = X.tab(2, 1)[q];
+        hc[0] = (AX & 1) ? X.tab(0, 1)[tx + 1] : PmlCoef<T>::none();
+        hc[1] = (AX & 2) ? X.tab(1, 1)[row + 1] : PmlCoef<T>::none();
+        hc[2] = (AX & 4) ? X.tab(2, 1)[q] : PmlCoef<T>::none();
     }
+    auto hn = [&](int a) { return ((AX >> a) & 1) && hc[a].nz(); };
     const int x = X.x0 + tx, y = X.y0 + row, k = X.k0 - 1 + q;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
         const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
         T ps1 = T(0), ps2 = T(0);
-        const T term = plane_term(hc[a1], hc[a2], curl1[c], curl2[c], ph[c][0], ph[c][1], &ps1, &ps2);
+        const T term = plane_term(hc[a1], hc[a2], hn(a1), hn(a2), curl1[c], curl2[c], ph[c][0], ph[c][1], &ps1, &ps2);
         const T old = X.h_tile(hA, c)[offE];
         T v, vd;
         if (!slots)
@@ -525,8 +546,8 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
         if (owned && val)
         {
             F.hout[c][idx] = v;
-            if (hc[a1].nz()) F.psih_out[c][0][idx] = ps1;
-            if (hc[a2].nz()) F.psih_out[c][1][idx] = ps2;
+            if (hn(a1)) F.psih_out[c][0][idx] = ps1;
+            if (hn(a2)) F.psih_out[c][1][idx] = ps2;
         }
     }
 }
@@ -536,7 +557,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
 // psi is read from the global arrays, or (STAGED) taken from the values ps
 // the caller read from its staging slots, and written back in place here;
 // sl: material slot indices.
-template <typename T, bool FULL = true, bool STAGED = false, bool UNIT = false>
+template <typename T, bool FULL = true, bool STAGED = false, bool UNIT = false, int AX = 7>
 __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int eS, int rn, int rp, unsigned vb,
                                               bool pml, bool slots, int idx, const int (&sl)[3], const T (&ps)[3][2])
 {
@@ -554,11 +575,12 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     const int offN = (row + 1) * (TX + 1) + tx + 1;
     PmlCoef<T> ec[3] = {};  // per axis, parity 0
     T pe[3][2] = {};
+    auto en = [&](int a) { return ((AX >> a) & 1) && ec[a].nz(); };
     if (pml)
     {
-        ec[0] = X.tab(0, 0)[tx + 1];
-        ec[1] = X.tab(1, 0)[row + 1];
-        ec[2] = X.tab(2, 0)[qe];
+        ec[0] = (AX & 1) ? X.tab(0, 0)[tx + 1] : PmlCoef<T>::none();
+        ec[1] = (AX & 2) ? X.tab(1, 0)[row + 1] : PmlCoef<T>::none();
+        ec[2] = (AX & 4) ? X.tab(2, 0)[qe] : PmlCoef<T>::none();
 #pragma unroll
         for (int c = 0; c < 3; ++c)
         {
@@ -571,8 +593,8 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
             }
             else
             {
-                if (ve && ec[a1].nz()) pe[c][0] = PE.psi[c][0][idx];
-                if (ve && ec[a2].nz()) pe[c][1] = PE.psi[c][1][idx];
+                if (ve && en(a1)) pe[c][0] = PE.psi[c][0][idx];
+                if (ve && en(a2)) pe[c][1] = PE.psi[c][1][idx];
             }
         }
     }
@@ -596,7 +618,7 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     {
         const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
         T ps1 = T(0), ps2 = T(0);
-        const T term = plane_term(ec[a1], ec[a2], curl1[c], curl2[c], pe[c][0], pe[c][1], &ps1, &ps2);
+        const T term = plane_term(ec[a1], ec[a2], en(a1), en(a2), curl1[c], curl2[c], pe[c][0], pe[c][1], &ps1, &ps2);
         const T old = X.e_tile(eS, c)[offE];
         T v, vd;
         if (!slots || sl[c] < 0)
@@ -609,8 +631,8 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
         if ((vb >> c) & 1u)
         {
             F.eout[c][idx] = v;
-            if (ec[a1].nz()) PE.psi[c][0][idx] = ps1;
-            if (ec[a2].nz()) PE.psi[c][1][idx] = ps2;
+            if (en(a1)) PE.psi[c][0][idx] = ps1;
+            if (en(a2)) PE.psi[c][1][idx] = ps2;
         }
     }
 }
@@ -651,6 +673,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         for (int s = 0; s < SHS; ++s) mbar_init(&hbar[s], 1);
         for (int s = 0; s < 4; ++s) mbar_init(&hd[s], NTH);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if constexpr (sizeof(T) == 8) reinterpret_cast<unsigned *>(smem + LY::INFO_OFF)[LY::NZ] = 0u;  // the tile's axis word
     }
     __syncthreads();
     auto issue_e = [&](int p) {
@@ -705,9 +728,13 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 e.b = in ? ld_keep(PE.pb[a][q] + pos, keep) : T(0);
                 e.c = in ? ld_keep(PE.pc[a][q] + pos, keep) : T(0);
                 e.ik = in ? ld_keep(PE.pik[a][q] + pos, keep) : T(1);
-                e.set_nz();
+                e.set_flags();
                 X.tab(a, q)[o] = e;
                 if (a < 2 && e.nz()) tile_pml = true;
+                // fp64: axis word, bit 2 q + a: CPML (c != 0 or 1/k != 1) along
+                // x / y at an own position of the tile
+                if constexpr (sizeof(T) == 8)
+                    if (a < 2 && o >= 1 && o <= (a == 0 ? TX : TY) && e.active()) atomicOr(&info[LY::NZ], 1u << (2 * q + a));
             }
         }
     }
@@ -805,6 +832,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     // (the pass is bound by the fp64 pipe there)
     const bool unit_dx = sizeof(T) == 8 && idh == T(1) && ide == T(1);
     const unsigned rowmask = ((1u << RPT) - 1u) << r0;
+    // fp64: axes x / y (bits 0 / 1) with CPML at the tile's own points, per side
+    const unsigned axw = sizeof(T) == 8 && PML ? info[LY::NZ] : 0u;
+    const int ax_e = (int)(axw & 3u), ax_h = (int)((axw >> 2) & 3u);
 
     // material slot indices of the E plane of the next iteration, loaded one
     // iteration ahead (rows flagged in the plane word only)
@@ -1030,10 +1060,25 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     constexpr bool U = decltype(unit)::value;
                     if (lean_h)
                     {
+                        auto lean = [&](auto ax) {
+                            constexpr int A = decltype(ax)::value;
 #pragma unroll
-                        for (int r = 0; r < RPT; ++r)
-                            h_own_general<T, false, U>(X, q, r0 + r, eA, eB, hA, rn, 63u, q >= 1, true, false, false, idx + r * sy,
-                                                       ph[r]);
+                            for (int r = 0; r < RPT; ++r)
+                                h_own_general<T, false, U, A>(X, q, r0 + r, eA, eB, hA, rn, 63u, q >= 1, true, false, false,
+                                                              idx + r * sy, ph[r]);
+                        };
+                        // fp64: a tile plane with CPML along one axis only
+                        // takes a copy without the other axes' terms
+                        if constexpr (sizeof(T) == 8)
+                        {
+                            const int ax = ax_h | (X.tab(2, 1)[q].active() ? 4 : 0);
+                            if (ax == 1) lean(std::integral_constant<int, 1>{});
+                            else if (ax == 2) lean(std::integral_constant<int, 2>{});
+                            else if (ax == 4) lean(std::integral_constant<int, 4>{});
+                            else lean(std::integral_constant<int, 7>{});
+                        }
+                        else
+                            lean(std::integral_constant<int, 7>{});
                     }
                     else
                     {
@@ -1129,8 +1174,23 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     auto general_e_own = [&](auto unit) {
                         constexpr bool U = decltype(unit)::value;
                         if (lean_e)
-                            e_own_general<T, false, STG, U>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false, idx_e + r * sy,
-                                                            sl_e[r], pe);
+                        {
+                            auto lean = [&](auto ax) {
+                                constexpr int A = decltype(ax)::value;
+                                e_own_general<T, false, STG, U, A>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false,
+                                                                   idx_e + r * sy, sl_e[r], pe);
+                            };
+                            if constexpr (sizeof(T) == 8)
+                            {
+                                const int ax = ax_e | (X.tab(2, 0)[q - 1].active() ? 4 : 0);
+                                if (ax == 1) lean(std::integral_constant<int, 1>{});
+                                else if (ax == 2) lean(std::integral_constant<int, 2>{});
+                                else if (ax == 4) lean(std::integral_constant<int, 4>{});
+                                else lean(std::integral_constant<int, 7>{});
+                            }
+                            else
+                                lean(std::integral_constant<int, 7>{});
+                        }
                         else
                             e_own_general<T, true, STG, U>(X, q - 1, r0 + r, eS, rp, rpp, vxy[r] & (we >> kInfoZValidShift),
                                                            pml_e, e_slots, idx_e + r * sy, sl_e[r], pe);
