@@ -229,6 +229,34 @@ def test_fused_asymmetric_cpml_and_odd_sizes_match_separate_passes():
             assert np.array_equal(outs["unfused", prec][k], outs["fused", prec][k]), (prec, k)
 
 
+def test_fused_cpml_kappa_and_resolution_match_separate_passes():
+    """CPML with k max > 1, one layer with sigma max = 0 (c = 0 but 1/k != 1:
+    the reference leaves those points to the plain curl update), resolution 2
+    (1/dx != 1): tile planes with CPML along one axis take the per-axis copy
+    of the lean path in fp64; fused and separate passes give the same bits."""
+    from ffip_gb300 import native
+    cfg = random_config(11, n=20, steps=60)
+    cfg["resolution"] = 2.0
+    cfg["size"] = [21.0, 18.0, 22.0]
+    cfg["PML"] = [{"thickness": 2.0, "direction": "y", "k max": 2.0, "sigma max": 0.0, "order": 3},
+                  {"thickness": 3.0, "direction": "x", "side": "positive", "k max": 3.0, "sigma max": 2.5, "order": 2},
+                  {"thickness": 2.5, "direction": "z", "k max": 1.0, "sigma max": 3.0, "order": 3}]
+    outs = {}
+    for eng in ("unfused", "fused"):
+        for prec in ("fp64", "fp32"):
+            c = dict(cfg)
+            c["engine"] = eng
+            c["precision"] = prec
+            with native.NativeSim(c) as s:
+                assert s.stats()["fused"] == (1 if eng == "fused" else 0)
+                s.run(c["stop condition"])
+                outs[eng, prec] = flatten(s.outputs())
+    for prec in ("fp64", "fp32"):
+        for k in outs["unfused", prec]:
+            assert np.array_equal(outs["unfused", prec][k], outs["fused", prec][k]), (prec, k)
+        assert max(np.abs(v).max() for k, v in outs["fused", prec].items() if k.endswith("/real")) > 0
+
+
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 @pytest.mark.parametrize("case,steps", [("dispersive", None), ("vacuum_pml", 2100)])
 def test_pass_timing_leaves_results_unchanged(precision, case, steps):
