@@ -133,11 +133,21 @@ struct FusedShape<double>
                          MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR, STAGE_PSI = 0;
 };
 
+// the lean CPML path is compiled per axis for tile planes with CPML along
+// one axis only (fp64: bound by the fp64 pipe, every instruction left out
+// counts; fp32 keeps one generic copy)
+#ifndef FFIP_FUSED_F32_AXIS_SPEC
+#define FFIP_FUSED_F32_AXIS_SPEC 0
+#endif
+template <typename T>
+constexpr bool kAxisSpec = sizeof(T) == 8 || FFIP_FUSED_F32_AXIS_SPEC;
+
 // CPML coefficients of one position along one axis: b, c, 1/k, and in the
 // fourth slot the bit pattern of an integer flag word, bit 0 = (c != 0) and
-// (fp64) bit 1 = (c != 0 or 1/k != 1): the CPML paths test these on the
-// integer pipe (a floating-point compare issues on the fp64 pipe, which
-// bounds the fp64 pass).  none(): a position without CPML (c = 0, 1/k = 1).
+// (with the per-axis copies) bit 1 = (c != 0 or 1/k != 1): the CPML paths
+// test these on the integer pipe (a floating-point compare issues on the
+// fp64 pipe, which bounds the fp64 pass).  none(): a position without CPML
+// (c = 0, 1/k = 1).
 template <typename T>
 struct alignas(4 * sizeof(T)) PmlCoef
 {
@@ -149,20 +159,19 @@ struct alignas(4 * sizeof(T)) PmlCoef
     }
     __device__ __forceinline__ bool nz() const
     {
-        if constexpr (sizeof(T) == 8) return flags() & 1u;
-        else return flags() != 0u;  // fp32 keeps bit 0 only
+        if constexpr (kAxisSpec<T>) return flags() & 1u;
+        else return flags() != 0u;  // bit 0 only
     }
     __device__ __forceinline__ bool active() const
     {
-        static_assert(sizeof(T) == 8, "the fp32 flag word holds bit 0 only");
+        static_assert(kAxisSpec<T>, "without the per-axis copies the flag word holds bit 0 only");
         return flags() & 2u;
     }
     __device__ __forceinline__ void set_flags()
     {
-        if constexpr (sizeof(T) == 8)
-            flagbits = __hiloint2double(0, (c != T(0) ? 3 : 0) | (ik != T(1) ? 2 : 0));
-        else
-            flagbits = __uint_as_float(c != T(0) ? 1u : 0u);
+        const unsigned f = kAxisSpec<T> ? (c != T(0) ? 3u : 0u) | (ik != T(1) ? 2u : 0u) : (c != T(0) ? 1u : 0u);
+        if constexpr (sizeof(T) == 8) flagbits = __hiloint2double(0, (int)f);
+        else flagbits = __uint_as_float(f);
     }
     __device__ __forceinline__ static PmlCoef none()
     {
@@ -673,7 +682,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         for (int s = 0; s < SHS; ++s) mbar_init(&hbar[s], 1);
         for (int s = 0; s < 4; ++s) mbar_init(&hd[s], NTH);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        if constexpr (sizeof(T) == 8) reinterpret_cast<unsigned *>(smem + LY::INFO_OFF)[LY::NZ] = 0u;  // the tile's axis word
+        if constexpr (kAxisSpec<T>) reinterpret_cast<unsigned *>(smem + LY::INFO_OFF)[LY::NZ] = 0u;  // the tile's axis word
     }
     __syncthreads();
     auto issue_e = [&](int p) {
@@ -733,7 +742,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 if (a < 2 && e.nz()) tile_pml = true;
                 // fp64: axis word, bit 2 q + a: CPML (c != 0 or 1/k != 1) along
                 // x / y at an own position of the tile
-                if constexpr (sizeof(T) == 8)
+                if constexpr (kAxisSpec<T>)
                     if (a < 2 && o >= 1 && o <= (a == 0 ? TX : TY) && e.active()) atomicOr(&info[LY::NZ], 1u << (2 * q + a));
             }
         }
@@ -833,7 +842,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     const bool unit_dx = sizeof(T) == 8 && idh == T(1) && ide == T(1);
     const unsigned rowmask = ((1u << RPT) - 1u) << r0;
     // fp64: axes x / y (bits 0 / 1) with CPML at the tile's own points, per side
-    const unsigned axw = sizeof(T) == 8 && PML ? info[LY::NZ] : 0u;
+    const unsigned axw = kAxisSpec<T> && PML ? info[LY::NZ] : 0u;
     const int ax_e = (int)(axw & 3u), ax_h = (int)((axw >> 2) & 3u);
 
     // material slot indices of the E plane of the next iteration, loaded one
@@ -1069,7 +1078,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                         };
                         // fp64: a tile plane with CPML along one axis only
                         // takes a copy without the other axes' terms
-                        if constexpr (sizeof(T) == 8)
+                        if constexpr (kAxisSpec<T>)
                         {
                             const int ax = ax_h | (X.tab(2, 1)[q].active() ? 4 : 0);
                             if (ax == 1) lean(std::integral_constant<int, 1>{});
@@ -1180,7 +1189,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                                 e_own_general<T, false, STG, U, A>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false,
                                                                    idx_e + r * sy, sl_e[r], pe);
                             };
-                            if constexpr (sizeof(T) == 8)
+                            if constexpr (kAxisSpec<T>)
                             {
                                 const int ax = ax_e | (X.tab(2, 0)[q - 1].active() ? 4 : 0);
                                 if (ax == 1) lean(std::integral_constant<int, 1>{});
