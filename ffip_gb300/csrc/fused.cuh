@@ -141,6 +141,11 @@ struct FusedShape<double>
 #endif
 template <typename T>
 constexpr bool kAxisSpec = sizeof(T) == 8 || FFIP_FUSED_F32_AXIS_SPEC;
+// fp64 copies for the tile planes with CPML along two axes (slab edges) as
+// well as one
+#ifndef FFIP_FUSED_F64_AXIS_PAIRS
+#define FFIP_FUSED_F64_AXIS_PAIRS 1
+#endif
 
 // CPML coefficients of one position along one axis: b, c, 1/k, and in the
 // fourth slot the bit pattern of an integer flag word, bit 0 = (c != 0) and
@@ -1084,6 +1089,11 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                             if (ax == 1) lean(std::integral_constant<int, 1>{});
                             else if (ax == 2) lean(std::integral_constant<int, 2>{});
                             else if (ax == 4) lean(std::integral_constant<int, 4>{});
+#if FFIP_FUSED_F64_AXIS_PAIRS
+                            else if (ax == 3) lean(std::integral_constant<int, 3>{});
+                            else if (ax == 5) lean(std::integral_constant<int, 5>{});
+                            else if (ax == 6) lean(std::integral_constant<int, 6>{});
+#endif
                             else lean(std::integral_constant<int, 7>{});
                         }
                         else
@@ -1195,6 +1205,11 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                                 if (ax == 1) lean(std::integral_constant<int, 1>{});
                                 else if (ax == 2) lean(std::integral_constant<int, 2>{});
                                 else if (ax == 4) lean(std::integral_constant<int, 4>{});
+#if FFIP_FUSED_F64_AXIS_PAIRS
+                                else if (ax == 3) lean(std::integral_constant<int, 3>{});
+                                else if (ax == 5) lean(std::integral_constant<int, 5>{});
+                                else if (ax == 6) lean(std::integral_constant<int, 6>{});
+#endif
                                 else lean(std::integral_constant<int, 7>{});
                             }
                             else
