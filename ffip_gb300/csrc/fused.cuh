@@ -35,8 +35,10 @@
 // shared memory (E components use only parity-0 positions along their curl
 // axes and H components only parity-1 positions, so one (b, c, 1/k) triple
 // per axis and side) and handles material slots and DFT sums; its psi values
-// are loaded at the top of the iteration, before the TMA wait.  The choice
-// is CTA-uniform (warp-uniform for E material slots) and comes from flags
+// are loaded at the top of the iteration, before the TMA wait.  A lean copy
+// of it serves CPML tile planes whose points are all valid and hold no slot
+// (in fp64 one copy per set of axes with CPML at the plane).  The choice is
+// CTA-uniform (warp-uniform for E material slots) and comes from flags
 // precomputed once per CTA.
 //
 // When the valid x (y) extent exceeds a whole number of tiles by one or two
