@@ -108,3 +108,35 @@ def test_large_design_workload_builds_and_steps(lib):
     assert len(groups) == 3
     for g in groups:
         assert out[g]["real"].shape[0] == 4
+
+
+def test_step_timed_pass_steps_like_step(lib):
+    """ffip_step_timed_pass through the C ABI: the same steps as ffip_step
+    (same outputs, same time step), and a pass time of 0 where the backend
+    does not time fused passes (the host emulation runs separate passes)."""
+    from ffip_gb300 import native
+    cfg, ds, _ = load("vacuum_pml")
+    steps = 37
+    outs = []
+    for timed in (False, True):
+        s = native.NativeSim(cfg, ds, lib=lib)
+        try:
+            if timed:
+                ms, pms = s.step_timed_pass(steps)
+                assert ms >= 0 and pms == 0
+            else:
+                s.step(steps)
+            st = s.stats()
+            assert st["time_step"] == steps
+            assert 0 < st["pass_bytes_per_step"] <= st["bytes_per_step"]
+            outs.append(flatten(s.outputs()))
+        finally:
+            s.close()
+    for k in outs[0]:
+        assert np.array_equal(outs[0][k], outs[1][k]), k
+    with pytest.raises(native.FfipError):
+        s = native.NativeSim(cfg, ds, lib=lib)
+        try:
+            s.step_timed_pass(-1)
+        finally:
+            s.close()
