@@ -35,26 +35,33 @@ def _deps_mtime() -> float:
     return m
 
 
-def build(force: bool = False, verbose: bool = False) -> str:
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
-        return LIB
-    os.makedirs(BUILD, exist_ok=True)
-    os.makedirs(LIBDIR, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, defines=(), libdir: str | None = None) -> str:
+    """Builds the library (and the run_sim_json driver beside it).  defines /
+    libdir: a tuning build with extra -D macros for the CUDA sources (the
+    FFIP_FUSED_* switches of fused.cuh), placed in its own directory."""
+    lib = LIB if libdir is None else os.path.join(libdir, "libffip_gb300.so")
+    cli = CLI if libdir is None else os.path.join(libdir, "run_sim_json")
+    bdir = BUILD if libdir is None else os.path.join(libdir, "_build")
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= _deps_mtime():
+        return lib
+    os.makedirs(bdir, exist_ok=True)
+    os.makedirs(os.path.dirname(lib), exist_ok=True)
     nvcc = _nvcc()
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
+    dflags = ["-D" + d for d in defines]
     jobs = []
     objs = []
     for s in CUDA_SOURCES:
-        o = os.path.join(BUILD, s + ".o")
+        o = os.path.join(bdir, s + ".o")
         objs.append(o)
         jobs.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-                     "-Xptxas", "-warn-spills", *inc, "-c", os.path.join(CSRC, s), "-o", o])
+                     "-Xptxas", "-warn-spills", *dflags, *inc, "-c", os.path.join(CSRC, s), "-o", o])
     for s in CXX_SOURCES:
-        o = os.path.join(BUILD, s + ".o")
+        o = os.path.join(bdir, s + ".o")
         objs.append(o)
         jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", *inc,
                      "-I", "/usr/local/cuda/include", "-c", os.path.join(CSRC, s), "-o", o])
-    cli_obj = os.path.join(BUILD, "run_sim_json.cpp.o")
+    cli_obj = os.path.join(bdir, "run_sim_json.cpp.o")
     jobs.append(["g++", "-O2", "-std=c++17", "-Wall", *inc, "-c", os.path.join(CSRC, "run_sim_json.cpp"), "-o", cli_obj])
     procs = [(j, subprocess.Popen(j, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)) for j in jobs]
     failed = []
@@ -67,18 +74,18 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if failed:
         msg = "\n\n".join(" ".join(j) + "\n" + out for j, out in failed)
         raise RuntimeError("native build failed:\n" + msg)
-    tmp = LIB + ".tmp%d" % os.getpid()
+    tmp = lib + ".tmp%d" % os.getpid()
     link = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("native link failed:\n" + r.stdout.decode(errors="replace"))
-    os.replace(tmp, LIB)
+    os.replace(tmp, lib)
     # the run_sim_json command-line driver, next to the library it loads
-    r = subprocess.run(["g++", "-o", CLI, cli_obj, "-L", LIBDIR, "-lffip_gb300", "-Wl,-rpath,$ORIGIN"],
+    r = subprocess.run(["g++", "-o", cli, cli_obj, "-L", os.path.dirname(lib), "-lffip_gb300", "-Wl,-rpath,$ORIGIN"],
                        stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("run_sim_json link failed:\n" + r.stdout.decode(errors="replace"))
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":

@@ -189,19 +189,15 @@ namespace
 constexpr uint64_t kTransposeScratchDoubles = uint64_t(1) << 20; // 8 MiB
 __device__ __align__(256) double g_transpose_scratch[kTransposeScratchDoubles];
 
-// address of g_transpose_scratch on each device, looked up once per device
-double *scratch_address(int device)
+// address of g_transpose_scratch on the current device, looked up on every
+// call: a host-side lookup that follows the module wherever the current
+// context loaded it (a cached address would outlive a cudaDeviceReset), and
+// no state is shared between calling threads
+double *scratch_address()
 {
-    constexpr int kMaxDevices = 64;
-    static double *addr[kMaxDevices] = {};
-    if (device < 0 || device >= kMaxDevices) throw std::runtime_error("device ordinal out of range");
-    if (!addr[device])
-    {
-        void *p = nullptr;
-        check(cudaGetSymbolAddress(&p, g_transpose_scratch), "cudaGetSymbolAddress");
-        addr[device] = static_cast<double *>(p);
-    }
-    return addr[device];
+    void *p = nullptr;
+    check(cudaGetSymbolAddress(&p, g_transpose_scratch), "cudaGetSymbolAddress");
+    return static_cast<double *>(p);
 }
 } // namespace
 
@@ -215,9 +211,7 @@ int adjoint_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, u
         throw std::length_error("ffip_transpose_noalloc: 4 * npts + nx * ny * nz = " + std::to_string(4 * npts + nout) +
                                 " doubles exceeds the fixed scratch of " + std::to_string(kTransposeScratchDoubles) +
                                 " doubles; use ffip_transpose");
-    int device = 0;
-    check(cudaGetDevice(&device), "cudaGetDevice");
-    double *base = scratch_address(device);
+    double *base = scratch_address();
     double *dpt = base, *dout = base + 4 * npts;
     Grid3 g = make_grid(gx, nx, gy, ny, gz, nz);
     if (npts) check(cudaMemcpy(dpt, pt, 4 * npts * sizeof(double), cudaMemcpyHostToDevice), "cudaMemcpy H2D");

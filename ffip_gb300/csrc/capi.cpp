@@ -65,6 +65,14 @@ int guard(F &&f)
     {
         return fail(FFIP_ERR_INTERNAL, "host out of memory");
     }
+    catch (const ffipg::Diverged &e)
+    {
+        return fail(FFIP_ERR_DIVERGED, e.what());
+    }
+    catch (const ffipg::DeviceTimeout &e)
+    {
+        return fail(FFIP_ERR_CUDA, e.what());
+    }
     catch (const std::exception &e)
     {
         return fail(code_for(e), e.what());
@@ -308,7 +316,7 @@ int ffip_to_convolve(const double *in1, uint64_t n0, uint64_t n1, const double *
                      int transpose)
 {
     return guard([&]() -> int {
-        if (!out || (n0 * n1 && !in1) || !in2) return fail(FFIP_ERR_INVALID, "null argument");
+        if (!out || (n0 && n1 && !in1) || !in2) return fail(FFIP_ERR_INVALID, "null argument");
         if (n0 > (1u << 30) || n1 > (1u << 30) || m0 > (1u << 30) || m1 > (1u << 30))
             return fail(FFIP_ERR_INVALID, "array too large");
         return ffipg::to_convolve(in1, (int)n0, (int)n1, in2, (int)m0, (int)m1, out, transpose);

@@ -128,6 +128,7 @@ private:
     void compute_bytes();
     void set_phases(int side, double t, double (*phase)[2]);
     void one_step();
+    void check_finite();
     void ensure_scratch(int64_t n)
     {
         if (n <= scratch_n_) return;
@@ -637,6 +638,8 @@ void Engine<T>::one_step()
                 fp.psih_out[c][s] = even ? b : a;
             }
         }
+        fp.wait_ns = P_.fused_wait_ns;
+        fp.stall_test = P_.fused_stall_test ? 1 : 0;
         nlaunch_ += be_->fused(fp);
         cur_ = nx;
         for (int c = 0; c < 3; ++c)
@@ -670,6 +673,20 @@ void Engine<T>::one_step()
     }
     if (gp_.nfaces) { be_->ghosts(gp_); ++nlaunch_; }
     ++ts_;
+    if (P_.divergence_check > 0 && ts_ % P_.divergence_check == 0) check_finite();
+}
+
+template <typename T>
+void Engine<T>::check_finite()
+{
+    // the reference has no such check: a diverging run there carries NaN /
+    // infinite values into its outputs; here the run stops with an error
+    const T *f[6];
+    for (int c = 0; c < 6; ++c) f[c] = buf_[cur_][c];
+    ++nlaunch_;
+    if (be_->any_nonfinite(f, 6, P_.cells()))
+        throw Diverged("the simulation diverged: non-finite field values at time step " + std::to_string(ts_) +
+                       " (checked every " + std::to_string(P_.divergence_check) + " steps)");
 }
 
 template <typename T>
@@ -908,6 +925,7 @@ void Engine<T>::reset()
     }
     cur_ = 0;
     ts_ = 0;
+    be_->clear_error();
     bind_params();
 }
 

@@ -7,6 +7,7 @@
 #include <functional>
 #include <map>
 #include <memory>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -27,6 +28,25 @@ struct FusedParams
     T *eout[3], *hout[3]; // outputs
     const T *psih_in[3][2];
     T *psih_out[3][2];
+    // the pass's waits on its TMA rings and on the threads of its CTA give
+    // up after wait_ns (global timer) and report a timeout; stall_test != 0
+    // makes every CTA first wait on a barrier that nothing completes (the
+    // timeout path, exercised by a test)
+    uint64_t wait_ns;
+    int stall_test;
+};
+
+// A bounded wait inside a kernel gave up: the results of the steps since
+// the last check are invalid.
+struct DeviceTimeout : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
+};
+
+// The divergence check found non-finite field values.
+struct Diverged : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
 };
 
 struct Backend
@@ -53,6 +73,12 @@ struct Backend
     virtual void probe(const float *f, const int64_t *lin, const double *w, int n, double *out) = 0;
     // sum over i of re[i]^2 + im[i]^2 -> out[0]
     virtual void dft_norm(const double *re, const double *im, int64_t n, double *out) = 0;
+    // whether any of the first n values of any of the nf arrays is NaN or
+    // infinite (waits for the result)
+    virtual bool any_nonfinite(const double *const *f, int nf, int64_t n) = 0;
+    virtual bool any_nonfinite(const float *const *f, int nf, int64_t n) = 0;
+    // forgets a reported kernel timeout (after the state was reset)
+    virtual void clear_error() {}
     virtual const char *name() const = 0;
     // device time of f() between events on the backend's stream (ms)
     virtual double timed(const std::function<void()> &f) = 0;

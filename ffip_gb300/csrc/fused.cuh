@@ -213,7 +213,7 @@ struct FusedLayout
     static constexpr int PSI_SLOTS = SH::STAGE_PSI ? 6 * SH::RPT : 0;
     static constexpr int SMEM = PSI_OFF;  // the instance without CPML code
     static constexpr int SMEM_PML = PSI_OFF + PSI_SLOTS * 256 * (int)sizeof(T);
-    static_assert((SH::SE + SH::SH + 4) * 8 <= 120, "mbarriers do not fit");
+    static_assert((SH::SE + SH::SH + 5) * 8 <= 120, "mbarriers do not fit");
     static_assert(SH::SE >= 5, "E planes q-2 .. q+1 are in use while one more loads");
     static_assert(SH::BX >= SH::XOFF + SH::TX + 1, "TMA box too narrow");
     static_assert((SH::XOFF - 1) * (int)sizeof(T) % 16 == 0, "TMA box start off a 16-byte boundary");
@@ -247,7 +247,27 @@ struct FusedLaunch
     const int4 *jobs;     // per CTA: x0, y0, k0, k1 (tile origin and owned z planes)
 };
 
-constexpr int kFusedWaitLimit = 1 << 22;
+// Bound of the waits that drain a CTA's outstanding TMA copies before it
+// leaves after an error (ns); the march waits take FusedParams::wait_ns.
+constexpr uint64_t kFusedDrainWaitNs = 2000000000ull;
+// Suspend-time hint of one mbarrier poll (ns): a waiting thread sleeps until
+// the phase completes or this time passes, instead of re-polling at once
+#ifndef FFIP_FUSED_WAIT_HINT_NS
+#define FFIP_FUSED_WAIT_HINT_NS 0
+#endif
+// Field and psi stores of the fused pass with the streaming (evict-first)
+// cache hint, so that the step's output does not push the halo rows that
+// neighbouring tiles still read out of L2
+#ifndef FFIP_FUSED_STORE_CS
+#define FFIP_FUSED_STORE_CS 0
+#endif
+
+template <typename T>
+__device__ __forceinline__ void st_out(T *p, T v)
+{
+    if constexpr (FFIP_FUSED_STORE_CS) __stcs(p, v);
+    else *p = v;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -269,21 +289,43 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
 {
     uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
+    if constexpr (FFIP_FUSED_WAIT_HINT_NS > 0)
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity), "r"((uint32_t)FFIP_FUSED_WAIT_HINT_NS)
+            : "memory");
+    else
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
     return ok != 0;
 }
 
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ uint64_t global_ns()
 {
-    for (int i = 0; i < kFusedWaitLimit; ++i)
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Waits for the phase of `parity` to complete; gives up (returns false) once
+// limit_ns have passed on the global timer since the first poll failed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint64_t limit_ns)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (;;)
+    {
         if (mbar_try_wait(bar, parity)) return true;
-    return false;
+        if (global_ns() - t0 > limit_ns) return false;
+    }
 }
 
 __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
@@ -561,9 +603,9 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
         X.hn_at(slot_new, c, row + 1, tx + 1) = val ? v : T(0);
         if (owned && val)
         {
-            F.hout[c][idx] = v;
-            if (hn(a1)) F.psih_out[c][0][idx] = ps1;
-            if (hn(a2)) F.psih_out[c][1][idx] = ps2;
+            st_out(&F.hout[c][idx], v);
+            if (hn(a1)) st_out(&F.psih_out[c][0][idx], ps1);
+            if (hn(a2)) st_out(&F.psih_out[c][1][idx], ps2);
         }
     }
 }
@@ -646,9 +688,9 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
             v = material_rec(PE, PE.slot[c], sl[c], old, term, &vd);
         if ((vb >> c) & 1u)
         {
-            F.eout[c][idx] = v;
-            if (en(a1)) PE.psi[c][0][idx] = ps1;
-            if (en(a2)) PE.psi[c][1][idx] = ps2;
+            st_out(&F.eout[c][idx], v);
+            if (en(a1)) st_out(&PE.psi[c][0][idx], ps1);
+            if (en(a2)) st_out(&PE.psi[c][1][idx], ps2);
         }
     }
 }
@@ -682,12 +724,14 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     uint64_t *ebar = reinterpret_cast<uint64_t *>(smem);
     uint64_t *hbar = ebar + SE;
     uint64_t *hd = hbar + SHS;  // per H ring plane: every thread has written its H there
+    uint64_t *stall = hd + 4;   // completed by nothing (the timeout path under test)
 
     if (tid == 0)
     {
         for (int s = 0; s < SE; ++s) mbar_init(&ebar[s], 1);
         for (int s = 0; s < SHS; ++s) mbar_init(&hbar[s], 1);
         for (int s = 0; s < 4; ++s) mbar_init(&hd[s], NTH);
+        mbar_init(stall, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if constexpr (kAxisSpec<T>) reinterpret_cast<unsigned *>(smem + LY::INFO_OFF)[LY::NZ] = 0u;  // the tile's axis word
     }
@@ -946,7 +990,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         // every thread has written H(q-1): the ring plane of H(q-2) is read
         // and the one of H(k-3) free, the E stage of plane q-3 and the H
         // stage of plane q-1 are no longer read by anyone
-        bool ok = q == 0 || mbar_wait_bounded(&hd[(q - 1) & 3], ((q - 1) >> 2) & 1);
+        bool ok = q == 0 || mbar_wait_bounded(&hd[(q - 1) & 3], ((q - 1) >> 2) & 1, F.wait_ns);
+        // the timeout path under test: a barrier that nothing completes
+        if (q == 0 && F.stall_test) ok = mbar_wait_bounded(stall, 0, F.wait_ns);
         if (tid == 0 && ok)
         {
             bool fence = false;
@@ -964,9 +1010,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 h_issued = q + SHS;
             }
         }
-        if (ok && q == 0) ok = mbar_wait_bounded(&ebar[0], 0);
-        if (ok && q + 1 < NP) ok = mbar_wait_bounded(&ebar[(q + 1) % SE], ((q + 1) / SE) & 1);
-        if (ok && do_h) ok = mbar_wait_bounded(&hbar[q % SHS], (q / SHS) & 1);
+        if (ok && q == 0) ok = mbar_wait_bounded(&ebar[0], 0, F.wait_ns);
+        if (ok && q + 1 < NP) ok = mbar_wait_bounded(&ebar[(q + 1) % SE], ((q + 1) / SE) & 1, F.wait_ns);
+        if (ok && do_h) ok = mbar_wait_bounded(&hbar[q % SHS], (q / SHS) & 1, F.wait_ns);
         if (!ok)
         {
             // a wait gave up: record it, let thread 0 wait (bounded) for its
@@ -976,8 +1022,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
             cp_async_wait_all();
             if (tid == 0)
             {
-                for (int p = 0; p < e_issued; ++p) mbar_wait_bounded(&ebar[p % SE], (p / SE) & 1);
-                for (int p = 0; p < h_issued; ++p) mbar_wait_bounded(&hbar[p % SHS], (p / SHS) & 1);
+                for (int p = 0; p < e_issued; ++p) mbar_wait_bounded(&ebar[p % SE], (p / SE) & 1, kFusedDrainWaitNs);
+                for (int p = 0; p < h_issued; ++p) mbar_wait_bounded(&hbar[p % SHS], (p / SHS) & 1, kFusedDrainWaitNs);
             }
             return;
         }
@@ -1023,9 +1069,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
 #pragma unroll
                         for (int r = 0; r < RPT; ++r)
                         {
-                            F.hout[0][idx + r * sy] = hn0[r];
-                            F.hout[1][idx + r * sy] = hn1[r];
-                            F.hout[2][idx + r * sy] = hn2[r];
+                            st_out(&F.hout[0][idx + r * sy], hn0[r]);
+                            st_out(&F.hout[1][idx + r * sy], hn1[r]);
+                            st_out(&F.hout[2][idx + r * sy], hn2[r]);
                         }
                     }
                 };
@@ -1161,9 +1207,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                         const T ex = eS0[r * BX] + coefE * curl_diff<U>(hz[r + 1], hz[r], hyr, hyp, ide);
                         const T ey = eS1[r * BX] + coefE * curl_diff<U>(hx[r + 1], hxp, hz[r + 1], hzx, ide);
                         const T ez = eS2[r * BX] + coefE * curl_diff<U>(hyr, hyx, hx[r + 1], hx[r], ide);
-                        F.eout[0][idx_e + r * sy] = ex;
-                        F.eout[1][idx_e + r * sy] = ey;
-                        F.eout[2][idx_e + r * sy] = ez;
+                        st_out(&F.eout[0][idx_e + r * sy], ex);
+                        st_out(&F.eout[1][idx_e + r * sy], ey);
+                        st_out(&F.eout[2][idx_e + r * sy], ez);
                     }
                 };
                 if constexpr (sizeof(T) == 8)

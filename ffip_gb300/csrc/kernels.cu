@@ -16,7 +16,9 @@
 #include <cstdio>
 #include <vector>
 #include <map>
+#include <memory>
 #include <mutex>
+#include <type_traits>
 #include <stdexcept>
 #include <string>
 
@@ -92,6 +94,50 @@ __global__ void k_dft_norm(const double *re, const double *im, int64_t n, double
     if (threadIdx.x == 0) *out = s[0];
 }
 
+// Divergence check: any NaN or infinity among the first n values of nf
+// arrays -> *flag = 1 (vector loads; n is a multiple of the 32-element row)
+template <typename T>
+struct NonfiniteArgs
+{
+    const T *f[6];
+    int nf;
+    int64_t n;
+};
+template <typename T>
+__global__ void __launch_bounds__(256) k_nonfinite(const __grid_constant__ NonfiniteArgs<T> a, int *flag)
+{
+    using V = typename std::conditional<sizeof(T) == 4, float4, double2>::type;
+    constexpr int W = sizeof(V) / sizeof(T);
+    const int64_t nv = a.n / W;
+    bool bad = false;
+    for (int i = 0; i < a.nf; ++i)
+    {
+        const V *p = reinterpret_cast<const V *>(a.f[i]);
+        for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nv; t += (int64_t)gridDim.x * blockDim.x)
+        {
+            const V v = __ldcs(p + t);
+            if constexpr (W == 4) bad = bad || !isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z) || !isfinite(v.w);
+            else bad = bad || !isfinite(v.x) || !isfinite(v.y);
+        }
+        for (int64_t t = nv * W + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < a.n; t += (int64_t)gridDim.x * blockDim.x)
+            bad = bad || !isfinite(a.f[i][t]);
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+// one flag per device and field type: the fused kernels' attributes
+// (dynamic shared memory, carveout) are set once on each device
+template <typename T>
+std::once_flag &fused_attr_once(int dev)
+{
+    static std::mutex m;
+    static std::map<int, std::unique_ptr<std::once_flag>> flags;
+    std::lock_guard<std::mutex> g(m);
+    auto &f = flags[dev];
+    if (!f) f.reset(new std::once_flag);
+    return *f;
+}
+
 // cuTensorMapEncodeTiled from the driver, without linking libcuda
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
@@ -151,6 +197,7 @@ public:
         if (dft_) cudaStreamSynchronize(dft_);
         cudaStreamSynchronize(stream_);
         if (err_) cudaFree(err_);
+        if (flag_) cudaFree(flag_);
         for (auto &kv : jobs_) cudaFree(kv.second.dev);
         if (side_) cudaStreamDestroy(side_);
         if (fork_) cudaEventDestroy(fork_);
@@ -253,11 +300,10 @@ public:
             check(cudaMalloc(&err_, sizeof(int)), "cudaMalloc");
             check(cudaMemsetAsync(err_, 0, sizeof(int), stream_), "cudaMemsetAsync");
         }
-        // kernel attributes, set once per process (std::call_once: the first
-        // handle sets them before any launch; no handle changes them while
-        // another one's kernels run)
-        static std::once_flag attr_once;
-        std::call_once(attr_once, [&] {
+        // kernel attributes are per device: set once on each device, by the
+        // first handle that launches there, before its first launch (no
+        // handle changes them while another one's kernels run)
+        std::call_once(fused_attr_once<T>(dev_), [&] {
             // shared memory for the CTAs per SM each instance is built for
             // (plus the 1 KB the system reserves per CTA), the same carveout
             // for both so that they share SMs; the rest of the unified
@@ -576,8 +622,39 @@ public:
         int e = 0;
         check(cudaMemcpyAsync(&e, err_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "cudaMemcpy err flag");
         check(cudaStreamSynchronize(stream_), "sync");
-        if (e) throw std::runtime_error("fused kernel: a TMA wait timed out (results of this step are invalid)");
+        if (e)
+            throw DeviceTimeout("fused kernel: a wait on its TMA rings or on its CTA's threads timed out; the field "
+                                "state is invalid until ffip_reset");
     }
+    void clear_error() override
+    {
+        if (!err_) return;
+        use();
+        join_dft();
+        check(cudaMemsetAsync(err_, 0, sizeof(int), stream_), "cudaMemsetAsync");
+    }
+
+    template <typename T>
+    bool any_nonfinite_t(const T *const *f, int nf, int64_t n)
+    {
+        use();
+        join_dft();
+        if (!flag_) check(cudaMalloc(&flag_, sizeof(int)), "cudaMalloc");
+        check(cudaMemsetAsync(flag_, 0, sizeof(int), stream_), "cudaMemsetAsync");
+        if (!nsm_) check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
+        NonfiniteArgs<T> a{};
+        for (int i = 0; i < nf && i < 6; ++i) a.f[i] = f[i];
+        a.nf = std::min(nf, 6);
+        a.n = n;
+        k_nonfinite<T><<<nsm_ * 4, 256, 0, stream_>>>(a, flag_);
+        check(cudaGetLastError(), "k_nonfinite launch");
+        int h = 0;
+        check(cudaMemcpyAsync(&h, flag_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "cudaMemcpy D2H");
+        check(cudaStreamSynchronize(stream_), "sync");
+        return h != 0;
+    }
+    bool any_nonfinite(const double *const *f, int nf, int64_t n) override { return any_nonfinite_t(f, nf, n); }
+    bool any_nonfinite(const float *const *f, int nf, int64_t n) override { return any_nonfinite_t(f, nf, n); }
 
     template <typename T>
     void sources_t(const SourceParams<T> &p)
@@ -691,6 +768,7 @@ private:
     cudaStream_t stream_{nullptr};
     int dev_{0};
     int *err_{nullptr};
+    int *flag_{nullptr};  // result word of the divergence check
     std::map<std::pair<const void *, int>, CUtensorMap> maps_;
     std::map<std::string, Jobs> jobs_;
     cudaStream_t side_{nullptr};

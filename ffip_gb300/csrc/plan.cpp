@@ -857,6 +857,17 @@ void build_plan(const Json &cfg, const std::map<std::string, Dataset> &ds, Plan 
     if (prec != "fp64" && prec != "fp32") throw std::runtime_error("precision must be \"fp64\" or \"fp32\"");
     p.precision_fp32 = prec == "fp32";
     p.engine = cfg.str("engine", "auto");
+    // divergence check every N steps (0: off)
+    const double every = cfg.num("divergence check interval", 4096);
+    if (!(every >= 0) || every > 1e15 || every != std::floor(every))
+        throw std::runtime_error("divergence check interval must be a non-negative whole number of steps");
+    p.divergence_check = (int64_t)every;
+    // bound of the fused pass's device-side waits, and the test of its
+    // timeout path
+    const double wait_s = cfg.num("fused wait timeout", 2.0);
+    if (!(wait_s > 0) || wait_s > 60) throw std::runtime_error("fused wait timeout must be in (0, 60] seconds");
+    p.fused_wait_ns = (uint64_t)(wait_s * 1e9);
+    p.fused_stall_test = cfg.num("fused wait test", 0) != 0;
     // set_size, src/simulation.cpp:570-581
     for (int a = 0; a < 3; ++a)
     {

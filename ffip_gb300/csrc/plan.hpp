@@ -155,6 +155,9 @@ struct Plan
     int vlo[6][3], vhi[6][3];  // valid index range per component per axis
     bool precision_fp32{false};
     std::string engine{"auto"};
+    int64_t divergence_check{4096};  // steps between checks for non-finite fields (0: never)
+    uint64_t fused_wait_ns{2000000000ull};
+    bool fused_stall_test{false};
     // CPML tables per axis and parity over array index (length M[a])
     std::vector<double> pml_k[3][2], pml_b[3][2], pml_c[3][2];
     bool any_pml{false};

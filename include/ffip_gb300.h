@@ -36,6 +36,7 @@ extern "C" {
 #define FFIP_ERR_CUDA (-2)      /* CUDA runtime failure (no device, out of memory, ...) */
 #define FFIP_ERR_NOT_FOUND (-3) /* unknown output group / array / dataset */
 #define FFIP_ERR_INTERNAL (-4)
+#define FFIP_ERR_DIVERGED (-5)  /* the divergence check found NaN / infinite field values */
 
 typedef struct ffip_sim ffip_sim;
 
@@ -66,8 +67,15 @@ typedef struct ffip_stats {
  * JSON, builds the grid, CPML, media, sources and DFT monitors, and uploads
  * them to a CUDA device.  Rebuild-only keys: "precision" ("fp64" default,
  * "fp32" = fp32 field state with fp64 DFT sums), "engine" ("auto", "fused",
- * "unfused") and "device" (CUDA device index; default: the device current
- * in the calling thread). */
+ * "unfused"), "device" (CUDA device index; default: the device current in
+ * the calling thread), "divergence check interval" (every that many steps
+ * the fields are checked for NaN / infinite values and stepping stops with
+ * FFIP_ERR_DIVERGED; default 4096, 0 = never; the reference has no such
+ * check), "fused wait timeout" (seconds after which a wait inside the fused
+ * pass gives up; the next synchronising call then returns FFIP_ERR_CUDA and
+ * the fields stay invalid until ffip_reset; default 2) and "fused wait test"
+ * (true: every CTA of the fused pass first waits on a barrier that nothing
+ * completes, so that the timeout path can be tested). */
 int ffip_create(const char *config_json, const ffip_dataset *datasets, uint64_t n_datasets, ffip_sim **out);
 
 /* n iterations of the time loop body of Simulation::run_until_time
@@ -185,9 +193,11 @@ int ffip_check_inside(const double *req_pts, uint64_t n, const double *poly_pts,
  * FFIP_ERR_INVALID with a message, use ffip_transpose for them.
  * The output part of the buffer is zeroed by every call.  The buffer is
  * shared by all calls on a device: calls that overlap on one device (from
- * several threads) race and must be serialised by the caller.  The first
- * call on each device looks the buffer's address up with
- * cudaGetSymbolAddress; make that first call outside any stream capture. */
+ * several threads) race and must be serialised by the caller.  Every call
+ * looks the buffer's address up with cudaGetSymbolAddress on the current
+ * device (nothing is cached between calls); the first call on a device
+ * also loads the library's device code there, so make that first call
+ * outside any stream capture. */
 int ffip_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
                            const double *pt, uint64_t npts, double *out);
 

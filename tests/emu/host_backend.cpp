@@ -7,6 +7,7 @@
 // tests/emu/build_emu.py into tests/_build/libffip_emu.so, which exports the
 // same ffip_* C functions as the product library.  The fused pass is not
 // emulated (it is a CUDA-only tiling of the same rules).
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <stdexcept>
@@ -94,6 +95,16 @@ public:
     }
     void probe(const double *f, const int64_t *l, const double *w, int n, double *o) override { probe_t(f, l, w, n, o); }
     void probe(const float *f, const int64_t *l, const double *w, int n, double *o) override { probe_t(f, l, w, n, o); }
+    template <typename T>
+    bool any_nonfinite_t(const T *const *f, int nf, int64_t n)
+    {
+        for (int i = 0; i < nf; ++i)
+            for (int64_t t = 0; t < n; ++t)
+                if (!std::isfinite(f[i][t])) return true;
+        return false;
+    }
+    bool any_nonfinite(const double *const *f, int nf, int64_t n) override { return any_nonfinite_t(f, nf, n); }
+    bool any_nonfinite(const float *const *f, int nf, int64_t n) override { return any_nonfinite_t(f, nf, n); }
     void dft_norm(const double *re, const double *im, int64_t n, double *out) override
     {
         double s = 0;

@@ -140,3 +140,39 @@ def test_step_timed_pass_steps_like_step(lib):
             s.step_timed_pass(-1)
         finally:
             s.close()
+
+
+@pytest.mark.parametrize("precision,steps", [("fp32", 200), ("fp64", 1300)])
+def test_divergence_check_stops_the_unstable_debye_run(lib, precision, steps):
+    """The reference's Debye pole is unconditionally unstable: run long, the
+    fields overflow, and a check every 100 steps stops the run with
+    FFIP_ERR_DIVERGED at the first check that sees non-finite values; with
+    the check off the run goes on and its outputs carry them."""
+    from ffip_gb300 import native
+    cfg, ds, _ = load("debye_short")
+    cfg = copy.deepcopy(cfg)
+    cfg["precision"] = precision
+    cfg["divergence check interval"] = 100
+    with native.NativeSim(cfg, ds, lib=lib) as s:
+        with pytest.raises(native.FfipError, match=r"error -5: the simulation diverged.*time step %d " % steps):
+            s.step(3000)
+        assert s.stats()["time_step"] == steps
+    cfg["divergence check interval"] = 0
+    with native.NativeSim(cfg, ds, lib=lib) as s:
+        s.step(steps + 100)
+        out = flatten(s.outputs())
+        assert not all(np.isfinite(v).all() for k, v in out.items() if k.endswith("/real"))
+
+
+def test_divergence_check_interval_is_validated(lib):
+    from ffip_gb300 import native
+    cfg, ds, _ = load("vacuum_pml")
+    for bad in (-1, 2.5):
+        c = copy.deepcopy(cfg)
+        c["divergence check interval"] = bad
+        with pytest.raises(native.FfipError, match="divergence check interval"):
+            native.NativeSim(c, ds, lib=lib)
+    c = copy.deepcopy(cfg)
+    c["fused wait timeout"] = 0
+    with pytest.raises(native.FfipError, match="fused wait timeout"):
+        native.NativeSim(c, ds, lib=lib)

@@ -59,3 +59,17 @@ def test_noalloc_rejects_inputs_beyond_the_scratch():
     gx, gy, gz, pt = _case(6, 262100, 8, 8, 8)     # 4 * 262100 + 512 > 2**20
     with pytest.raises(native.FfipError, match="exceeds the fixed scratch"):
         native.transpose_noalloc(gx, gy, gz, pt, lib=lib)
+
+
+def test_noalloc_rejects_a_point_count_whose_scratch_size_overflows():
+    # npts = 2**62: 4 * npts wraps to 0 in 64 bits, so only the separate
+    # npts bound stops it; the call must fail before it reads the points
+    import ctypes
+    lib = native.load()
+    g = np.array([0.0])
+    pt = np.zeros((1, 4))
+    out = np.zeros(1)
+    D = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    rc = lib.ffip_transpose_noalloc(D(g), 1, D(g), 1, D(g), 1, D(pt), 1 << 62, D(out))
+    assert rc == -1
+    assert "exceeds the fixed scratch" in lib.ffip_last_error().decode()
