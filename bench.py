@@ -124,13 +124,23 @@ class ClockSampler:
         except (ValueError, IndexError):
             return None
 
-    def summary(self):
+    def summary(self, timed=None):
+        """Samples inside [start, stop]: the whole fp32 leg (warm-up, the K
+        timed steps and the full-length fp32 run, all the same kernels at the
+        same load), so that a short timed region (20 steps last about 9 ms,
+        shorter than the 50 ms sampling period) still has a clock record;
+        timed: (t0, t1) of the K timed steps, whose own samples are counted
+        apart."""
         rows = [r for r in self.rows if len(r) >= 10]
         inside = rows
         if self.t0 is not None and self.t1 is not None:
             inside = [r for r in rows if (w := self._when(r)) is not None and self.t0 <= w <= self.t1]
+        n_timed = None
+        if timed is not None:
+            n_timed = sum(1 for r in rows if (w := self._when(r)) is not None and timed[0] <= w <= timed[1])
         if not inside:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0, "samples_total": len(rows)}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0, "samples_total": len(rows),
+                    "samples_timed_steps": n_timed}
         num = lambda v: float(v) if v.replace(".", "").isdigit() else None  # noqa: E731
         sm = [x for x in (num(r[2]) for r in inside) if x is not None]
         mx = [x for x in (num(r[3]) for r in inside) if x is not None]
@@ -142,8 +152,29 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(inside), "samples_total": len(rows),
+                "samples_timed_steps": n_timed,
                 "window_s": (self.t1 - self.t0).total_seconds() if self.t0 else None,
-                "sampling": "nvidia-smi every 50 ms; samples timestamped inside the timed region"}
+                "sampling": "nvidia-smi every 50 ms; samples timestamped inside the fp32 leg (warm-up, the timed "
+                            "steps and the full-length fp32 run)"}
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
 
 
 def peaks():
@@ -314,7 +345,7 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps,
                 "warmup": warm, "ms_per_step": dt / a.steps * 1e3, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg_meta,
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "cpu_model": cpu_model(), "kind": "port",
                                  "sample": "%d time steps of the full workload after %d warm-up steps (set-up %.1f s untimed)"
                                            % (a.steps, warm, setup)},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -331,27 +362,40 @@ def main():
         cfg["device"] = dev
         return cfg
 
+    def full_run(prec):
+        """One full-length run through the C ABI: config in, set-up, stepping,
+        DFT arrays out (wall clock, max over ranks)."""
+        barrier(world)
+        t0 = time.perf_counter()
+        s = native.NativeSim(make(prec))
+        s.run()
+        o = s.outputs()
+        dt = time.perf_counter() - t0
+        st = s.stats()
+        s.close()
+        return o, allmax(world, dt), st
+
     # ---- device-resident throughput, fp32 and fp64
     res = {}
     clocks = None
+    full = {}
+    e2e = None
     for prec in (("fp32",) if a.fp32_only else ("fp32", "fp64")):
         s = native.NativeSim(make(prec))
-        # the clock sampler runs from before the warm-up (nvidia-smi takes a
-        # moment to start) and keeps the samples inside the timed region
+        # the clock sampler runs over the whole fp32 leg: from before the
+        # warm-up (nvidia-smi takes a moment to start) through the timed
+        # steps and the full-length fp32 run
         cs = ClockSampler(dev).__enter__() if prec == "fp32" else None
         if cs:
             time.sleep(0.3)
+            cs.start()
         s.step(warm)
         s.sync()
         st0 = s.stats()
         barrier(world)
-        if cs:
-            cs.start()
+        ta = datetime.datetime.now()
         ms, pass_ms = s.step_timed_pass(a.steps)
-        if cs:
-            cs.stop()
-            cs.__exit__(None, None, None)
-            clocks = cs.summary()
+        tb = datetime.datetime.now()
         barrier(world)
         st1 = s.stats()
         ms = allmax(world, ms)
@@ -360,6 +404,19 @@ def main():
                      "bytes_per_step": st1["bytes_per_step"], "pass_bytes_per_step": st1["pass_bytes_per_step"],
                      "fused": st1["fused"]}
         s.close()
+        if prec == "fp32" and not a.skip_full_run:
+            o, dt, st = full_run("fp32")
+            full["fp32"] = o
+            steps_run = st["time_step"]
+            e2e = {"value": world * cells * steps_run / dt / 1e9, "unit": UNIT,
+                   "h2d_bytes_per_step": st["h2d_bytes"] / steps_run, "d2h_bytes_per_step": st["d2h_bytes"] / steps_run,
+                   "unit_of_work": "one full %d-step run through ffip_create/ffip_run/ffip_output_* "
+                                   "(config JSON in from the host, set-up, stepping, DFT arrays out)" % steps_run,
+                   "seconds": dt}
+        if cs:
+            cs.stop()
+            cs.__exit__(None, None, None)
+            clocks = cs.summary((ta, tb))
     if a.fp32_only:
         res["fp64"] = res["fp32"]
     t32 = res["fp32"]["ms"] / a.steps
@@ -402,30 +459,13 @@ def main():
                     "pass_ms": res["fp64"]["pass_ms"] / a.steps},
            "clocks": clocks}
 
-    # ---- full runs: fp32-vs-fp64 DFT error and end-to-end through the C ABI
+    # ---- full runs: end to end through the C ABI (fp32, run above inside the
+    #      clock window) and the fp32-vs-fp64 DFT error
     if not a.skip_full_run:
-        full = {}
-        e2e = None
-        for prec in ("fp32", "fp64"):
-            barrier(world)
-            t0 = time.perf_counter()
-            s = native.NativeSim(make(prec))
-            s.run()
-            o = s.outputs()
-            dt = time.perf_counter() - t0
-            st = s.stats()
-            s.close()
-            dt = allmax(world, dt)
-            full[prec] = o
-            if prec == "fp32":
-                steps_run = st["time_step"]
-                e2e = {"value": world * cells * steps_run / dt / 1e9, "unit": UNIT,
-                       "h2d_bytes_per_step": st["h2d_bytes"] / steps_run, "d2h_bytes_per_step": st["d2h_bytes"] / steps_run,
-                       "unit_of_work": "one full %d-step run through ffip_create/ffip_run/ffip_output_* "
-                                       "(config JSON in from the host, set-up, stepping, DFT arrays out)" % steps_run,
-                       "seconds": dt}
         out["e2e"] = e2e
-        out["dft_rel_err_fp32_vs_fp64"] = dft_rel_err(full["fp32"], full["fp64"])
+        if not a.fp32_only:
+            full["fp64"] = full_run("fp64")[0]
+            out["dft_rel_err_fp32_vs_fp64"] = dft_rel_err(full["fp32"], full["fp64"])
 
     # ---- the plain fp64 vacuum box, GPU beside the CPU restatement
     if not a.fp32_only:
@@ -446,7 +486,8 @@ def main():
         threads = os.cpu_count() or 1
         try:
             dt, setup = cpu_leg(workloads.dispersive_spheres(n, precision="fp64"), a.cpu_steps, 2, threads)
-            out["cpu_baseline"] = {"value": cells * a.cpu_steps / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            out["cpu_baseline"] = {"value": cells * a.cpu_steps / dt / 1e9, "unit": UNIT, "cores": threads,
+                                   "cpu_model": cpu_model(), "kind": "port",
                                    "sample": "%d time steps of the full workload after 2 warm-up steps, set-up (%.1f s) untimed"
                                              % (a.cpu_steps, setup)}
         except Exception as e:  # the baseline is reported, not required

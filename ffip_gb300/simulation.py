@@ -526,9 +526,20 @@ class Adjoint_Source:
             return
         self.forward_dfts[component] = self.forward_simulation.add_dft_fields(
             center=self.center, size=self.size, frequency=[self.frequency], field_component=component)
+        # the reference names the datasets "<component> adjoint"
+        # (ffip/simulation.py:711-721), so two Adjoint_Source objects of one
+        # adjoint simulation would write the same datasets and every one of
+        # them would run with the last one's amplitudes; a later source here
+        # gets a numbered suffix instead (the first keeps the reference's name)
+        suffix = component + " adjoint"
+        used = {getattr(src, "amplitude_dataset_name", None) for src in getattr(self.adjoint_simulation, "sources", ())}
+        n = 1
+        while "inhom source amplitude %s" % suffix in used:
+            suffix = "%s adjoint %d" % (component, n)
+            n += 1
         self.adjoint_sources[component] = Inhom_Source(function=self.function, frequency=self.frequency, amplitude=None,
                                                        center=self.center, size=self.size, dim=self.dim,
-                                                       field_component=component, suffix=component + " adjoint")
+                                                       field_component=component, suffix=suffix)
         self.adjoint_simulation.add_source(self.adjoint_sources[component])
 
     @property
@@ -653,7 +664,10 @@ class Adjoint_Volume:
                                               density=density, epsilon_fun=epsilon_fun, e_sus=e_sus, suffix="adjoint")
         shared = geometry is not None and any(g is geometry for g in forward_simulation.geometry)
         self.geom = geometry
-        adjoint_simulation.add_geometry(self.geom)
+        # a shared adjoint simulation (one broadband adjoint run for several
+        # frequencies' volumes) holds the design box once, too
+        if not any(g is geometry for g in adjoint_simulation.geometry):
+            adjoint_simulation.add_geometry(self.geom)
         if not shared:
             forward_simulation.add_geometry(self.geom)
         comps = ["Ex", "Ey", "Ez"]

@@ -152,7 +152,7 @@ def filtered_noise(shape, sigma, seed):
 
 
 def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0.11), steps=5000, nprobe=4,
-                   seed=2024, precision="fp32", exact=True):
+                   seed=2024, precision="fp32", exact=True, broadband=True):
     """The adjoint-gradient workload: a size[0] x size[0] x size[1] cell box
     (dx = 1, Courant 0.5) with a `pml`-cell CPML; a design box of
     design[0] x design[0] x design[1] cells centred at the origin whose
@@ -161,8 +161,10 @@ def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0
     medium2 vacuum); an Ex current sheet (Gaussian1, f = 0.1) half-way
     between the lower CPML and the design box; objective F = sum over
     `nprobe` seeded probe cells above the design box and over `freqs` of
-    |Ex|^2.  One forward run and one adjoint run per frequency, `steps` time
-    steps each.  Returns (AdjointProblem, rho0)."""
+    |Ex|^2.  One forward run and, with broadband=True, one adjoint run for
+    all frequencies (design.BroadbandAdjoint), else one adjoint run per
+    frequency as the reference's scripts do; `steps` time steps each.
+    Returns (AdjointProblem, rho0)."""
     from . import design as D
     from .geom import Medium, Vector3
     from .simulation import Adjoint_Source, Adjoint_Volume, Simulation, field_match_objective, run_until_time
@@ -183,6 +185,19 @@ def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0
                float(rng.integers(dz // 2 + 8, nz / 2 - pml - 8))) for _ in range(nprobe)]
     rho0 = filtered_noise((dz + 1, dn + 1, dn + 1), 3.0, seed)
     dt = 0.5
+    if broadband:
+        adj = Simulation(size=V(n, n, nz), resolution=1, pmls=pmls, precision=precision)
+        bb = D.BroadbandAdjoint(adj, fwd, Gaussian1(0.1, cutoff=4, start_time=0.0), freqs, dt)
+        geom = None
+        for f in freqs:
+            for p in probes:
+                bb.source(f, center=V(*p), size=V(0, 0, 0), dim=V(1, 1, 1),
+                          udfs=[field_match_objective(np.zeros((1, 1, 1)), "Ex", weight=1.0)])
+            vol = Adjoint_Volume(adj, fwd, frequency=f, center=V(0, 0, 0), size=V(dn, dn, dz), dim=V(dn + 1, dn + 1, dz + 1),
+                                 density=rho0, medium1=Medium(epsilon=12), medium2=Medium(), norm=bb.norm(f), geometry=geom)
+            geom = vol.geom
+            bb.add_volume(vol)
+        return D.AdjointProblem(fwd, [bb], run_until_time(steps * dt), exact=exact), rho0
     terms, geom = [], None
     for f in freqs:
         adj = Simulation(size=V(n, n, nz), resolution=1, pmls=pmls, precision=precision)

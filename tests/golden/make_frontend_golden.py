@@ -67,7 +67,8 @@ def build_cases(ffip):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("FFIP_REFERENCE"), required="FFIP_REFERENCE" not in os.environ,
+                    help="reference checkout (default: $FFIP_REFERENCE)")
     a = ap.parse_args()
     for name in ("h5py", "shapely", "shapely.geometry", "ffip._ffip"):
         mod = types.ModuleType(name)

@@ -220,7 +220,8 @@ def run_case(binary, cfg, ds, workdir):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("FFIP_REFERENCE"), required="FFIP_REFERENCE" not in os.environ,
+                    help="reference checkout (default: $FFIP_REFERENCE)")
     a = ap.parse_args()
     subprocess.check_call(["make", "-s", "-f", os.path.join(ROOT, "oracle", "Makefile.ref"), "REF=" + a.ref])
     binary = os.path.join(ROOT, "oracle", "_ref", "run_sim_json")
