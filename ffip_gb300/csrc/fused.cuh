@@ -64,28 +64,35 @@ namespace ffipg
 {
 template <typename T>
 struct FusedShape;
-// TY tile rows, RPT adjacent rows per thread (8 warps of 32 lanes, warp w
-// owns rows RPT w .. RPT w + RPT - 1); SE / SH: TMA stages of the E / H
-// plane rings; KCH: most z planes per CTA; MINB: CTAs per SM the register
-// budget is sized for (tuning builds may override the defaults); STAGE_PSI:
-// the CPML instance stages psi in shared memory by cp.async, ahead of use
-// (fp32 only: the fp64 pass is bound by fp64 arithmetic, and there the copy
-// instructions cost more than the latency they hide).  Tiles start
-// at x0 = 1 + TX * bx, so the TMA box starts at x0 - XOFF = TX * bx, a
-// 128-byte boundary (a box row then spans the fewest 32-byte sectors), and
-// spans BX >= XOFF + TX + 1 elements (x0 - 1 .. x0 + TX), rounded up to
-// 16 bytes.
+// NPT adjacent x points per thread (vector loads and stores), TX = 32 NPT
+// tile columns; TY tile rows, RPT adjacent rows per thread (8 warps of 32
+// lanes, warp w owns rows RPT w .. RPT w + RPT - 1); SE / SH: TMA stages of
+// the E / H plane rings; KCH: most z planes per CTA; MINB: CTAs per SM the
+// register budget is sized for (tuning builds may override the defaults);
+// STAGE_PSI: the CPML instance stages psi in shared memory by cp.async,
+// ahead of use (fp32 only: the fp64 pass is bound by fp64 arithmetic, and
+// there the copy instructions cost more than the latency they hide).  Tiles
+// start at x0 = kXFirst + TX * bx (the first index that holds grid points);
+// the TMA box starts XOFF elements to the left, at a 16-byte boundary
+// (TX * bx), and spans BX >= XOFF + TX + 1 elements (x0 - XOFF .. x0 + TX),
+// rounded up to 16 bytes; a thread's own points sit XOFF + NPT lane + p into
+// a box row (8-byte aligned pairs in fp32).  The H ring planes hold rows of
+// RW = XOFF + TX elements: the low-x halo column at XOFF - 1, the tile's own
+// points from XOFF on.
+#ifndef FFIP_FUSED_F32_NPT
+#define FFIP_FUSED_F32_NPT 2
+#endif
 #ifndef FFIP_FUSED_F32_RPT
 #define FFIP_FUSED_F32_RPT 1
 #endif
 #ifndef FFIP_FUSED_F32_SE
-#define FFIP_FUSED_F32_SE 6
+#define FFIP_FUSED_F32_SE 5
 #endif
 #ifndef FFIP_FUSED_F32_SH
 #define FFIP_FUSED_F32_SH 3
 #endif
 #ifndef FFIP_FUSED_F32_MINB
-#define FFIP_FUSED_F32_MINB 3
+#define FFIP_FUSED_F32_MINB 2
 #endif
 #ifndef FFIP_FUSED_F32_STAGE_PSI
 #define FFIP_FUSED_F32_STAGE_PSI 1
@@ -114,26 +121,67 @@ struct FusedShape;
 #define FFIP_FUSED_F32_KCH_SHORT 12
 #endif
 #ifndef FFIP_FUSED_F32_MINB_INTERIOR
-#define FFIP_FUSED_F32_MINB_INTERIOR 3
+#define FFIP_FUSED_F32_MINB_INTERIOR 2
 #endif
 #ifndef FFIP_FUSED_F64_MINB_INTERIOR
 #define FFIP_FUSED_F64_MINB_INTERIOR 2
 #endif
+constexpr int fused_box_width(int xoff, int tx, int elems16) { return (xoff + tx + 1 + elems16 - 1) / elems16 * elems16; }
 template <>
 struct FusedShape<float>
 {
-    static constexpr int TX = 32, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 1, BX = 36, SE = FFIP_FUSED_F32_SE,
-                         SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH, KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT,
-                         MINB = FFIP_FUSED_F32_MINB,
+    static constexpr int NPT = FFIP_FUSED_F32_NPT, TX = 32 * NPT, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 4,
+                         BX = fused_box_width(XOFF, TX, 4), RW = XOFF + TX, SE = FFIP_FUSED_F32_SE, SH = FFIP_FUSED_F32_SH,
+                         KCH = FFIP_FUSED_KCH, KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT, MINB = FFIP_FUSED_F32_MINB,
                          MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR, STAGE_PSI = FFIP_FUSED_F32_STAGE_PSI;
 };
 template <>
 struct FusedShape<double>
 {
-    static constexpr int TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 1, BX = 34, SE = FFIP_FUSED_F64_SE,
-                         SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH, KCH_SHORT = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB,
-                         MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR, STAGE_PSI = 0;
+    static constexpr int NPT = 1, TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 2, BX = fused_box_width(XOFF, TX, 2),
+                         RW = XOFF + TX, SE = FFIP_FUSED_F64_SE, SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH,
+                         KCH_SHORT = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB, MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR,
+                         STAGE_PSI = 0;
 };
+
+// NPT consecutive values of one row: an aligned vector load / store (float2
+// for two fp32 values), elementwise otherwise
+template <typename T, int N>
+struct Vals
+{
+    T v[N];
+    __device__ __forceinline__ T &operator[](int i) { return v[i]; }
+    __device__ __forceinline__ const T &operator[](int i) const { return v[i]; }
+};
+template <int N, typename T>
+__device__ __forceinline__ Vals<T, N> ldv(const T *p)
+{
+    Vals<T, N> r;
+    if constexpr (N == 2 && sizeof(T) == 4)
+    {
+        const float2 f = *reinterpret_cast<const float2 *>(p);
+        r.v[0] = f.x;
+        r.v[1] = f.y;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < N; ++i) r.v[i] = p[i];
+    }
+    return r;
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
+{
+    if constexpr (N == 2 && sizeof(T) == 4)
+        *reinterpret_cast<float2 *>(p) = make_float2(v.v[0], v.v[1]);
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < N; ++i) p[i] = v.v[i];
+    }
+}
 
 // the lean CPML path is compiled per axis for tile planes with CPML along
 // one axis only (fp64: bound by the fp64 pipe, every instruction left out
@@ -200,25 +248,28 @@ struct FusedLayout
     static constexpr int E_OFF = 128;  // [0, 128): mbarriers
     static constexpr int H_OFF = E_OFF + SH::SE * 3 * E_TILE;
     static constexpr int HN_OFF = H_OFF + SH::SH * 3 * H_TILE;
-    static constexpr int HN_PLANE = 3 * (SH::TY + 1) * (SH::TX + 1);  // elements of one H ring plane
+    static constexpr int HN_PLANE = 3 * (SH::TY + 1) * SH::RW;  // elements of one H ring plane
     static constexpr int NX = SH::TX + 1, NY = SH::TY + 1, NZ = SH::KCH + 2;  // CPML table lengths
     static constexpr int PML_OFF = (HN_OFF + 4 * HN_PLANE * (int)sizeof(T) + 31) / 32 * 32;
     static constexpr int PML_BYTES = 2 * (NX + NY + NZ) * (int)sizeof(PmlCoef<T>);  // [axis][parity][n]
     static constexpr int INFO_OFF = PML_OFF + PML_BYTES;
     // CPML instance with STAGE_PSI: E-side psi of the own points staged by
     // cp.async, one slot of 256 elements (one per thread) per
-    // [row][component][axis]
+    // [row][point][component][axis]
     static constexpr int PSI_OFF = (INFO_OFF + (NZ + 1) * 4 + 15) / 16 * 16;  // NZ plane words + the tile's axis word
     static constexpr int PSI_E = 0;
-    static constexpr int PSI_SLOTS = SH::STAGE_PSI ? 6 * SH::RPT : 0;
+    static constexpr int PSI_SLOTS = SH::STAGE_PSI ? 6 * SH::RPT * SH::NPT : 0;
     static constexpr int SMEM = PSI_OFF;  // the instance without CPML code
     static constexpr int SMEM_PML = PSI_OFF + PSI_SLOTS * 256 * (int)sizeof(T);
     static_assert((SH::SE + SH::SH + 5) * 8 <= 120, "mbarriers do not fit");
     static_assert(SH::SE >= 5, "E planes q-2 .. q+1 are in use while one more loads");
     static_assert(SH::BX >= SH::XOFF + SH::TX + 1, "TMA box too narrow");
-    static_assert((SH::XOFF - 1) * (int)sizeof(T) % 16 == 0, "TMA box start off a 16-byte boundary");
+    static_assert((kXFirst - SH::XOFF) * (int)sizeof(T) % 16 == 0 && SH::TX * (int)sizeof(T) % 16 == 0,
+                  "TMA box start (x0 - XOFF = kXFirst - XOFF + TX bx) off a 16-byte boundary");
     static_assert(SH::BX * (int)sizeof(T) % 16 == 0, "TMA box width not a multiple of 16 bytes");
-    static_assert(SH::TX == 32 && SH::TY == 8 * SH::RPT && 2 * SH::TY <= 32, "8 warps of 32 lanes, halo in one warp");
+    static_assert(SH::XOFF * (int)sizeof(T) % (SH::NPT * (int)sizeof(T)) == 0 && SH::RW * (int)sizeof(T) % 16 == 0,
+                  "own points of a box row / ring row not aligned for NPT-wide vector access");
+    static_assert(SH::TX == 32 * SH::NPT && SH::TY == 8 * SH::RPT && 2 * SH::TY <= 32, "8 warps of 32 lanes, halo in one warp");
 };
 
 // per-plane flag word (one per plane of the chunk, shared memory); bits
@@ -267,6 +318,21 @@ __device__ __forceinline__ void st_out(T *p, T v)
 {
     if constexpr (FFIP_FUSED_STORE_CS) __stcs(p, v);
     else *p = v;
+}
+template <typename T, int N>
+__device__ __forceinline__ void st_outv(T *p, const Vals<T, N> &v)
+{
+    if constexpr (N == 2 && sizeof(T) == 4)
+    {
+        const float2 f = make_float2(v.v[0], v.v[1]);
+        if constexpr (FFIP_FUSED_STORE_CS) __stcs(reinterpret_cast<float2 *>(p), f);
+        else *reinterpret_cast<float2 *>(p) = f;
+    }
+    else
+    {
+#pragma unroll
+        for (int i = 0; i < N; ++i) st_out(p + i, v.v[i]);
+    }
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -420,12 +486,13 @@ struct FusedCtx
     {
         return reinterpret_cast<const T *>(smem + LY::H_OFF + (st * 3 + c) * LY::H_TILE);
     }
-    // new H, ring plane r (0..2), rows y0-1 .. y0+TY-1, columns x0-1 .. x0+TX-1
+    // new H, ring plane r (0..3), rows y0-1 .. y0+TY-1; column XOFF - 1 is
+    // x0 - 1, column XOFF + j is x0 + j
     __device__ __forceinline__ T *hn_plane(int r, int c) const
     {
-        return reinterpret_cast<T *>(smem + LY::HN_OFF) + r * LY::HN_PLANE + c * (SH::TY + 1) * (SH::TX + 1);
+        return reinterpret_cast<T *>(smem + LY::HN_OFF) + r * LY::HN_PLANE + c * (SH::TY + 1) * SH::RW;
     }
-    __device__ __forceinline__ T &hn_at(int r, int c, int row, int col) const { return hn_plane(r, c)[row * (SH::TX + 1) + col]; }
+    __device__ __forceinline__ T &hn_at(int r, int c, int row, int col) const { return hn_plane(r, c)[row * SH::RW + col]; }
     // CPML table of axis a, parity q: entry o is position first_a + o, with
     // first = x0 - 1, y0 - 1, k0 - 1
     __device__ __forceinline__ PmlCoef<T> *tab(int a, int q) const
@@ -521,30 +588,33 @@ __device__ __forceinline__ T fused_h_halo(const FusedCtx<T> &X, int x, int y, in
     return material_at(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
 }
 
-// The halo H point of this thread, if any: Hz / Hx of the low-y row (warps
-// 7 / 6), Hz / Hy of the low-x column (warp 5, lanes < TY / < 2 TY), with
-// its place (row, col) in an H ring plane
+// Halo H point p (0 .. NPT-1) of this thread, if any: Hz / Hx of the low-y
+// row (warps 7 / 6, NPT points per lane), Hz / Hy of the low-x column (warp
+// 5, lanes < TY / < 2 TY, p = 0 only), with its place (row, col) in an H
+// ring plane
 template <typename T>
-__device__ __forceinline__ bool halo_point(const FusedCtx<T> &X, int wid, int lane, int &hx, int &hy, int &comp, int &row,
-                                           int &col)
+__device__ __forceinline__ bool halo_point(const FusedCtx<T> &X, int wid, int lane, int p, int &hx, int &hy, int &comp,
+                                           int &row, int &col)
 {
-    constexpr int TY = FusedShape<T>::TY;
-    if (wid == 7) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 2; row = 0; col = lane + 1; }
-    else if (wid == 6) { hx = X.x0 + lane; hy = X.y0 - 1; comp = 0; row = 0; col = lane + 1; }
-    else if (wid == 5 && lane < TY) { hx = X.x0 - 1; hy = X.y0 + lane; comp = 2; row = lane + 1; col = 0; }
-    else if (wid == 5 && lane < 2 * TY) { hx = X.x0 - 1; hy = X.y0 + lane - TY; comp = 1; row = lane - TY + 1; col = 0; }
+    using SH = FusedShape<T>;
+    constexpr int TY = SH::TY, NPT = SH::NPT, XOFF = SH::XOFF;
+    const int j = lane * NPT + p;
+    if (wid == 7) { hx = X.x0 + j; hy = X.y0 - 1; comp = 2; row = 0; col = XOFF + j; }
+    else if (wid == 6) { hx = X.x0 + j; hy = X.y0 - 1; comp = 0; row = 0; col = XOFF + j; }
+    else if (p == 0 && wid == 5 && lane < TY) { hx = X.x0 - 1; hy = X.y0 + lane; comp = 2; row = lane + 1; col = XOFF - 1; }
+    else if (p == 0 && wid == 5 && lane < 2 * TY) { hx = X.x0 - 1; hy = X.y0 + lane - TY; comp = 1; row = lane - TY + 1; col = XOFF - 1; }
     else return false;
     return true;
 }
 
-// General H(k) at this thread's own point of tile row `row`: validity bits,
-// CPML from the staged tables (psi values ph loaded by the caller), material
-// slots, DFT.  AX: the axes (bit a) along which the tile plane may have CPML
-// at its own points; the others are known to have none (c = 0, 1/k = 1) and
-// their terms are left out of the code (the same bits).
+// General H(k) at this thread's own point x0 + xi of tile row `row`:
+// validity bits, CPML from the staged tables (psi values ph loaded by the
+// caller), material slots, DFT.  AX: the axes (bit a) along which the tile
+// plane may have CPML at its own points; the others are known to have none
+// (c = 0, 1/k = 1) and their terms are left out of the code (the same bits).
 template <typename T, bool FULL = true, bool UNIT = false, int AX = 7>
-__device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int row, int eA, int eB, int hA, int slot_new,
-                                              unsigned vb, bool owned, bool pml, bool slots, bool dft, int idx,
+__device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int row, int xi, int eA, int eB, int hA,
+                                              int slot_new, unsigned vb, bool owned, bool pml, bool slots, bool dft, int idx,
                                               const T (&ph)[3][2])
 {
     // FULL = false: the lean instance for CPML tile planes whose points are
@@ -558,8 +628,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
     constexpr int BX = SH::BX;
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PH = F.h;
-    const int tx = threadIdx.x;
-    const int offE = (row + 1) * BX + tx + SH::XOFF;
+    const int offE = (row + 1) * BX + xi + SH::XOFF;
     const T idh = PH.inv_dx;
     const T *eA0 = X.e_tile(eA, 0), *eA1 = X.e_tile(eA, 1), *eA2 = X.e_tile(eA, 2);
     const T *eB0 = X.e_tile(eB, 0), *eB1 = X.e_tile(eB, 1);
@@ -578,12 +647,12 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
     PmlCoef<T> hc[3] = {};  // per axis, parity 1
     if (pml)
     {
-        hc[0] = (AX & 1) ? X.tab(0, 1)[tx + 1] : PmlCoef<T>::none();
+        hc[0] = (AX & 1) ? X.tab(0, 1)[xi + 1] : PmlCoef<T>::none();
         hc[1] = (AX & 2) ? X.tab(1, 1)[row + 1] : PmlCoef<T>::none();
         hc[2] = (AX & 4) ? X.tab(2, 1)[q] : PmlCoef<T>::none();
     }
     auto hn = [&](int a) { return ((AX >> a) & 1) && hc[a].nz(); };
-    const int x = X.x0 + tx, y = X.y0 + row, k = X.k0 - 1 + q;
+    const int x = X.x0 + xi, y = X.y0 + row, k = X.k0 - 1 + q;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
@@ -600,7 +669,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
         else
             v = material_at(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
         const bool val = (vb >> (3 + c)) & 1u;
-        X.hn_at(slot_new, c, row + 1, tx + 1) = val ? v : T(0);
+        X.hn_at(slot_new, c, row + 1, SH::XOFF + xi) = val ? v : T(0);
         if (owned && val)
         {
             st_out(&F.hout[c][idx], v);
@@ -616,11 +685,12 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
 // the caller read from its staging slots, and written back in place here;
 // sl: material slot indices.
 template <typename T, bool FULL = true, bool STAGED = false, bool UNIT = false, int AX = 7>
-__device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int eS, int rn, int rp, unsigned vb,
-                                              bool pml, bool slots, int idx, const int (&sl)[3], const T (&ps)[3][2])
+__device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int xi, int eS, int rn, int rp,
+                                              unsigned vb, bool pml, bool slots, int idx, const int (&sl)[3],
+                                              const T (&ps)[3][2])
 {
     using SH = FusedShape<T>;
-    constexpr int BX = SH::BX, TX = SH::TX;
+    constexpr int BX = SH::BX, RW = SH::RW;
     if (!FULL)
     {
         vb = 63u;
@@ -628,15 +698,14 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     }
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PE = F.e;
-    const int tx = threadIdx.x;
-    const int offE = (row + 1) * BX + tx + SH::XOFF;
-    const int offN = (row + 1) * (TX + 1) + tx + 1;
+    const int offE = (row + 1) * BX + xi + SH::XOFF;
+    const int offN = (row + 1) * RW + xi + SH::XOFF;
     PmlCoef<T> ec[3] = {};  // per axis, parity 0
     T pe[3][2] = {};
     auto en = [&](int a) { return ((AX >> a) & 1) && ec[a].nz(); };
     if (pml)
     {
-        ec[0] = (AX & 1) ? X.tab(0, 0)[tx + 1] : PmlCoef<T>::none();
+        ec[0] = (AX & 1) ? X.tab(0, 0)[xi + 1] : PmlCoef<T>::none();
         ec[1] = (AX & 2) ? X.tab(1, 0)[row + 1] : PmlCoef<T>::none();
         ec[2] = (AX & 4) ? X.tab(2, 0)[qe] : PmlCoef<T>::none();
 #pragma unroll
@@ -659,9 +728,9 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     const T ide = PE.inv_dx;
     const T *n0 = X.hn_plane(rn, 0), *n1 = X.hn_plane(rn, 1), *n2 = X.hn_plane(rn, 2);
     const T *p0 = X.hn_plane(rp, 0), *p1 = X.hn_plane(rp, 1);
-    const T hzr = n2[offN], hzy = n2[offN - (TX + 1)], hzx = n2[offN - 1];
+    const T hzr = n2[offN], hzy = n2[offN - RW], hzx = n2[offN - 1];
     const T hyr = n1[offN], hyp = p1[offN], hyx = n1[offN - 1];
-    const T hxr = n0[offN], hxp = p0[offN], hxy = n0[offN - (TX + 1)];
+    const T hxr = n0[offN], hxp = p0[offN], hxy = n0[offN - RW];
     T curl1[3], curl2[3];
     const T m = UNIT ? T(1) : ide;
     curl1[0] = UNIT ? hzr - hzy : (hzr - hzy) * m;  // Ex: dHz/dy - dHy/dz
@@ -670,7 +739,7 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
     curl2[1] = UNIT ? hzr - hzx : (hzr - hzx) * m;
     curl1[2] = UNIT ? hyr - hyx : (hyr - hyx) * m;  // Ez: dHy/dx - dHx/dy
     curl2[2] = UNIT ? hxr - hxy : (hxr - hxy) * m;
-    const int x = X.x0 + tx, y = X.y0 + row, k = X.k0 - 1 + qe;
+    const int x = X.x0 + xi, y = X.y0 + row, k = X.k0 - 1 + qe;
 #pragma unroll
     for (int c = 0; c < 3; ++c)
     {
@@ -703,7 +772,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
 {
     using SH = FusedShape<T>;
     using LY = FusedLayout<T>;
-    constexpr int TX = SH::TX, TY = SH::TY, RPT = SH::RPT, XOFF = SH::XOFF, SE = SH::SE, SHS = SH::SH, BX = SH::BX;
+    constexpr int TX = SH::TX, TY = SH::TY, RPT = SH::RPT, NPT = SH::NPT, XOFF = SH::XOFF, SE = SH::SE, SHS = SH::SH,
+                  BX = SH::BX, RW = SH::RW;
     constexpr int NTH = 256;
     extern __shared__ __align__(128) unsigned char smem[];
     const FusedParams<T> &F = L.fp;
@@ -867,26 +937,30 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     }
     }
 
-    const int x = X.x0 + lane;
-    // per own row: components with a grid point at (x, y) that this pass owns
-    unsigned vxy[RPT];
+    const int x = X.x0 + lane * NPT;  // first own point of this thread
+    // per own row and point: components with a grid point at (x + p, y) that
+    // this pass owns
+    unsigned vxy[RPT][NPT];
 #pragma unroll
     for (int r = 0; r < RPT; ++r)
-    {
-        const int y = X.y0 + r0 + r;
-        vxy[r] = 0;
-        if (x < L.xlim && y < L.ylim)
-            for (int c = 0; c < 3; ++c)
-            {
-                if (x >= PE.vlo[c][0] && x <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1]) vxy[r] |= 1u << c;
-                if (x >= PH.vlo[c][0] && x <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1]) vxy[r] |= 1u << (3 + c);
-            }
-    }
+#pragma unroll
+        for (int p = 0; p < NPT; ++p)
+        {
+            const int y = X.y0 + r0 + r, xp = x + p;
+            vxy[r][p] = 0;
+            if (xp < L.xlim && y < L.ylim)
+                for (int c = 0; c < 3; ++c)
+                {
+                    if (xp >= PE.vlo[c][0] && xp <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1]) vxy[r][p] |= 1u << c;
+                    if (xp >= PH.vlo[c][0] && xp <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1])
+                        vxy[r][p] |= 1u << (3 + c);
+                }
+        }
     __syncthreads();
     const int sz = (int)PE.sz, sy = (int)PE.sy;
-    const int own0 = x + (X.y0 + r0) * sy;  // own point of row r0 at z = 0
-    const int offE = (r0 + 1) * BX + lane + XOFF;    // own point of row r0 in an E or H box
-    const int offN = (r0 + 1) * (TX + 1) + lane + 1;  // own point of row r0 in an H ring plane
+    const int own0 = x + (X.y0 + r0) * sy;              // first own point of row r0 at z = 0
+    const int offE = (r0 + 1) * BX + XOFF + lane * NPT;  // first own point of row r0 in an E or H box
+    const int offN = (r0 + 1) * RW + XOFF + lane * NPT;  // first own point of row r0 in an H ring plane
     const T coefH = PH.coef_def, coefE = PE.coef_def, idh = PH.inv_dx, ide = PE.inv_dx;
     // fp64: the plain path without the 1/dx multiplications when 1/dx is 1
     // (the pass is bound by the fp64 pipe there)
@@ -898,9 +972,11 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
 
     // material slot indices of the E plane of the next iteration, loaded one
     // iteration ahead (rows flagged in the plane word only)
-    int sl_next[RPT][3];
+    int sl_next[RPT][NPT][3];
 #pragma unroll
-    for (int r = 0; r < RPT; ++r) sl_next[r][0] = sl_next[r][1] = sl_next[r][2] = -1;
+    for (int r = 0; r < RPT; ++r)
+#pragma unroll
+        for (int p = 0; p < NPT; ++p) sl_next[r][p][0] = sl_next[r][p][1] = sl_next[r][p][2] = -1;
     // running ring positions: E stages of planes q-1, q, q+1; H stage of
     // plane q; H ring planes of H(k), H(k-1), H(k-2)
     int eS = SE - 1, eA = 0, eB = 1 % SE, hA = 0, rn = 0, rp = 3, rpp = 2;
@@ -910,13 +986,16 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     // iteration, during the waits and the H update
     constexpr bool STG = PML && SH::STAGE_PSI;
     T *pstage = reinterpret_cast<T *>(smem + LY::PSI_OFF) + tid;
+    auto stage_slot = [&](int r, int p, int c, int a) { return pstage + (LY::PSI_E + ((r * NPT + p) * 3 + c) * 2 + a) * NTH; };
     // iteration q: H at plane k = k0 - 1 + q (q <= NP - 2), E at plane k - 1 (q >= 2)
     for (int q = 0; q < NP; ++q, idx += sz)
     {
-        int sl_e[RPT][3];
+        int sl_e[RPT][NPT][3];
 #pragma unroll
         for (int r = 0; r < RPT; ++r)
-            for (int c = 0; c < 3; ++c) sl_e[r][c] = sl_next[r][c];
+#pragma unroll
+            for (int p = 0; p < NPT; ++p)
+                for (int c = 0; c < 3; ++c) sl_e[r][p][c] = sl_next[r][p][c];
         const bool do_h = q <= NP - 2, do_e = q >= 2;
         const int k = X.k0 - 1 + q;
         const int idx_e = idx - sz;
@@ -930,62 +1009,71 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         const bool pml_e = !fast_e && pml_tables && (we & kInfoZPml);
         const bool dft_h = wh & kInfoDftH;
         // CPML psi of this iteration's own H points, loaded before the TMA wait
-        T ph[RPT][3][2];
+        T ph[RPT][NPT][3][2];
 #pragma unroll
         for (int r = 0; r < RPT; ++r)
-            for (int c = 0; c < 3; ++c) ph[r][c][0] = ph[r][c][1] = T(0);
+#pragma unroll
+            for (int p = 0; p < NPT; ++p)
+                for (int c = 0; c < 3; ++c) ph[r][p][c][0] = ph[r][p][c][1] = T(0);
         if (do_h && pml_h)
         {
-            const bool cx = X.tab(0, 1)[lane + 1].nz(), cz = X.tab(2, 1)[q].nz();  // H side (parity 1): c != 0
+            const bool cz = X.tab(2, 1)[q].nz();  // H side (parity 1): c != 0
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
-            {
-                const bool ch[3] = {cx, X.tab(1, 1)[r0 + r + 1].nz(), cz};
-                const unsigned vb = vxy[r] & (wh >> kInfoZValidShift);
 #pragma unroll
-                for (int c = 0; c < 3; ++c)
+                for (int p = 0; p < NPT; ++p)
                 {
-                    const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-                    const bool vh = (vb >> (3 + c)) & 1u;
-                    if (vh && ch[a1]) ph[r][c][0] = F.psih_in[c][0][idx + r * sy];
-                    if (vh && ch[a2]) ph[r][c][1] = F.psih_in[c][1][idx + r * sy];
+                    const bool ch[3] = {X.tab(0, 1)[lane * NPT + p + 1].nz(), X.tab(1, 1)[r0 + r + 1].nz(), cz};
+                    const unsigned vb = vxy[r][p] & (wh >> kInfoZValidShift);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                    {
+                        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+                        const bool vh = (vb >> (3 + c)) & 1u;
+                        if (vh && ch[a1]) ph[r][p][c][0] = F.psih_in[c][0][idx + r * sy + p];
+                        if (vh && ch[a2]) ph[r][p][c][1] = F.psih_in[c][1][idx + r * sy + p];
+                    }
                 }
-            }
         }
 #pragma unroll
-        for (int r = 0; r < RPT; ++r) sl_next[r][0] = sl_next[r][1] = sl_next[r][2] = -1;
+        for (int r = 0; r < RPT; ++r)
+#pragma unroll
+            for (int p = 0; p < NPT; ++p) sl_next[r][p][0] = sl_next[r][p][1] = sl_next[r][p][2] = -1;
         // CPML psi of this iteration's own E points (plane k - 1; updated in
         // place by this thread only), copied during the waits and the H update
         if (STG && do_e && pml_e)
         {
-            const bool cx = X.tab(0, 0)[lane + 1].nz(), cz = X.tab(2, 0)[q - 1].nz();  // E side (parity 0): c != 0
+            const bool cz = X.tab(2, 0)[q - 1].nz();  // E side (parity 0): c != 0
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
-            {
-                const bool ce[3] = {cx, X.tab(1, 0)[r0 + r + 1].nz(), cz};
-                const unsigned vb = vxy[r] & (we >> kInfoZValidShift);
 #pragma unroll
-                for (int c = 0; c < 3; ++c)
+                for (int p = 0; p < NPT; ++p)
                 {
-                    const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
-                    const bool ve = (vb >> c) & 1u;
-                    T *dst = pstage + (LY::PSI_E + (r * 3 + c) * 2) * NTH;
-                    if (ve && ce[a1]) cp_async_elem(dst, PE.psi[c][0] + idx_e + r * sy);
-                    if (ve && ce[a2]) cp_async_elem(dst + NTH, PE.psi[c][1] + idx_e + r * sy);
+                    const bool ce[3] = {X.tab(0, 0)[lane * NPT + p + 1].nz(), X.tab(1, 0)[r0 + r + 1].nz(), cz};
+                    const unsigned vb = vxy[r][p] & (we >> kInfoZValidShift);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                    {
+                        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+                        const bool ve = (vb >> c) & 1u;
+                        if (ve && ce[a1]) cp_async_elem(stage_slot(r, p, c, 0), PE.psi[c][0] + idx_e + r * sy + p);
+                        if (ve && ce[a2]) cp_async_elem(stage_slot(r, p, c, 1), PE.psi[c][1] + idx_e + r * sy + p);
+                    }
                 }
-            }
         }
         if (STG) cp_async_commit();
         if (q >= 1 && q <= NP - 2 && (wh & rowmask))
         {
 #pragma unroll
             for (int r = 0; r < RPT; ++r)
-            {
-                const unsigned vb = vxy[r] & (wh >> kInfoZValidShift);
 #pragma unroll
-                for (int c = 0; c < 3; ++c)
-                    if (PE.slot[c].map && ((vb >> c) & 1u)) sl_next[r][c] = PE.slot[c].map[idx + r * sy];
-            }
+                for (int p = 0; p < NPT; ++p)
+                {
+                    const unsigned vb = vxy[r][p] & (wh >> kInfoZValidShift);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        if (PE.slot[c].map && ((vb >> c) & 1u)) sl_next[r][p][c] = PE.slot[c].map[idx + r * sy + p];
+                }
         }
         // every thread has written H(q-1): the ring plane of H(q-2) is read
         // and the one of H(k-3) free, the E stage of plane q-3 and the H
@@ -1039,39 +1127,46 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     const T *eA0 = X.e_tile(eA, 0) + offE, *eA1 = X.e_tile(eA, 1) + offE, *eA2 = X.e_tile(eA, 2) + offE;
                     const T *eB0 = X.e_tile(eB, 0) + offE, *eB1 = X.e_tile(eB, 1) + offE;
                     const T *hA0 = X.h_tile(hA, 0) + offE, *hA1 = X.h_tile(hA, 1) + offE, *hA2 = X.h_tile(hA, 2) + offE;
-                    T exa[RPT + 1], eza[RPT + 1];
+                    Vals<T, NPT> exa[RPT + 1], eza[RPT + 1];
 #pragma unroll
                     for (int r = 0; r <= RPT; ++r)
                     {
-                        exa[r] = eA0[r * BX];
-                        eza[r] = eA2[r * BX];
+                        exa[r] = ldv<NPT>(eA0 + r * BX);
+                        eza[r] = ldv<NPT>(eA2 + r * BX);
                     }
-                    T hn0[RPT], hn1[RPT], hn2[RPT];
+                    Vals<T, NPT> hn0[RPT], hn1[RPT], hn2[RPT];
 #pragma unroll
                     for (int r = 0; r < RPT; ++r)
                     {
-                        const T eya = eA1[r * BX], eyx = eA1[r * BX + 1], eyb = eB1[r * BX];
-                        const T exb = eB0[r * BX], ezx = eA2[r * BX + 1];
-                        hn0[r] = hA0[r * BX] + coefH * curl_diff<U>(eza[r], eza[r + 1], eya, eyb, idh);
-                        hn1[r] = hA1[r * BX] + coefH * curl_diff<U>(exa[r], exb, eza[r], ezx, idh);
-                        hn2[r] = hA2[r * BX] + coefH * curl_diff<U>(eya, eyx, exa[r], exa[r + 1], idh);
+                        const Vals<T, NPT> eya = ldv<NPT>(eA1 + r * BX), eyb = ldv<NPT>(eB1 + r * BX), exb = ldv<NPT>(eB0 + r * BX);
+                        const Vals<T, NPT> h0 = ldv<NPT>(hA0 + r * BX), h1 = ldv<NPT>(hA1 + r * BX), h2 = ldv<NPT>(hA2 + r * BX);
+                        // x + 1 neighbours: the next point of the pair, or the box column after it
+                        const T eyn = eA1[r * BX + NPT], ezn = eA2[r * BX + NPT];
+#pragma unroll
+                        for (int p = 0; p < NPT; ++p)
+                        {
+                            const T eyx = p + 1 < NPT ? eya[p + 1] : eyn, ezx = p + 1 < NPT ? eza[r][p + 1] : ezn;
+                            hn0[r][p] = h0[p] + coefH * curl_diff<U>(eza[r][p], eza[r + 1][p], eya[p], eyb[p], idh);
+                            hn1[r][p] = h1[p] + coefH * curl_diff<U>(exa[r][p], exb[p], eza[r][p], ezx, idh);
+                            hn2[r][p] = h2[p] + coefH * curl_diff<U>(eya[p], eyx, exa[r][p], exa[r + 1][p], idh);
+                        }
                     }
                     T *n0 = X.hn_plane(rn, 0) + offN, *n1 = X.hn_plane(rn, 1) + offN, *n2 = X.hn_plane(rn, 2) + offN;
 #pragma unroll
                     for (int r = 0; r < RPT; ++r)
                     {
-                        n0[r * (TX + 1)] = hn0[r];
-                        n1[r * (TX + 1)] = hn1[r];
-                        n2[r * (TX + 1)] = hn2[r];
+                        stv(n0 + r * RW, hn0[r]);
+                        stv(n1 + r * RW, hn1[r]);
+                        stv(n2 + r * RW, hn2[r]);
                     }
                     if (q >= 1)
                     {
 #pragma unroll
                         for (int r = 0; r < RPT; ++r)
                         {
-                            st_out(&F.hout[0][idx + r * sy], hn0[r]);
-                            st_out(&F.hout[1][idx + r * sy], hn1[r]);
-                            st_out(&F.hout[2][idx + r * sy], hn2[r]);
+                            st_outv(&F.hout[0][idx + r * sy], hn0[r]);
+                            st_outv(&F.hout[1][idx + r * sy], hn1[r]);
+                            st_outv(&F.hout[2][idx + r * sy], hn2[r]);
                         }
                     }
                 };
@@ -1088,23 +1183,27 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     constexpr bool U = decltype(unit)::value;
                     if (wid >= 6)
                     {
-                        const int o = lane + XOFF;  // row y0 - 1 of the boxes
-                        if (wid == 7)
-                            X.hn_at(rn, 2, 0, lane + 1) =
-                                (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh);
-                        else
-                            X.hn_at(rn, 0, 0, lane + 1) =
-                                (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 0)[o] + coefH * curl_diff<U>(gA2[o], gA2[o + BX], gA1[o], gB1[o], idh);
+#pragma unroll
+                        for (int p = 0; p < NPT; ++p)
+                        {
+                            const int o = XOFF + lane * NPT + p;  // row y0 - 1 of the boxes
+                            if (wid == 7)
+                                X.hn_at(rn, 2, 0, o) =
+                                    (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh);
+                            else
+                                X.hn_at(rn, 0, 0, o) =
+                                    (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 0)[o] + coefH * curl_diff<U>(gA2[o], gA2[o + BX], gA1[o], gB1[o], idh);
+                        }
                     }
                     else if (wid == 5 && lane < 2 * TY)
                     {
                         const int v = lane < TY ? lane : lane - TY;
                         const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
                         if (lane < TY)
-                            X.hn_at(rn, 2, v + 1, 0) =
+                            X.hn_at(rn, 2, v + 1, XOFF - 1) =
                                 (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh);
                         else
-                            X.hn_at(rn, 1, v + 1, 0) =
+                            X.hn_at(rn, 1, v + 1, XOFF - 1) =
                                 (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 1)[o] + coefH * curl_diff<U>(gA0[o], gB0[o], gA2[o], gA2[o + 1], idh);
                     }
                 };
@@ -1126,8 +1225,10 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                             constexpr int A = decltype(ax)::value;
 #pragma unroll
                             for (int r = 0; r < RPT; ++r)
-                                h_own_general<T, false, U, A>(X, q, r0 + r, eA, eB, hA, rn, 63u, q >= 1, true, false, false,
-                                                              idx + r * sy, ph[r]);
+#pragma unroll
+                                for (int p = 0; p < NPT; ++p)
+                                    h_own_general<T, false, U, A>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn, 63u, q >= 1, true,
+                                                                  false, false, idx + r * sy + p, ph[r][p]);
                         };
                         // fp64: a tile plane with CPML along one axis only
                         // takes a copy without the other axes' terms
@@ -1151,8 +1252,11 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     {
 #pragma unroll
                         for (int r = 0; r < RPT; ++r)
-                            h_own_general<T, true, U>(X, q, r0 + r, eA, eB, hA, rn, vxy[r] & (wh >> kInfoZValidShift), q >= 1,
-                                                      pml_h, h_slots, dft_h, idx + r * sy, ph[r]);
+#pragma unroll
+                            for (int p = 0; p < NPT; ++p)
+                                h_own_general<T, true, U>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn,
+                                                          vxy[r][p] & (wh >> kInfoZValidShift), q >= 1, pml_h, h_slots, dft_h,
+                                                          idx + r * sy + p, ph[r][p]);
                     }
                 };
                 if constexpr (sizeof(T) == 8)
@@ -1162,21 +1266,25 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 }
                 else
                     general_h_own(std::false_type{});
-                int hx, hy, comp, row, col;
-                if (halo_point(X, wid, lane, hx, hy, comp, row, col))
+#pragma unroll
+                for (int p = 0; p < NPT; ++p)
                 {
-                    auto halo = [&](auto unit) {
-                        constexpr bool U = decltype(unit)::value;
-                        if (comp == 0) return fused_h_halo<T, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                        if (comp == 1) return fused_h_halo<T, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                        return fused_h_halo<T, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                    };
-                    T v;
-                    if constexpr (sizeof(T) == 8)
-                        v = unit_dx ? halo(std::true_type{}) : halo(std::false_type{});
-                    else
-                        v = halo(std::false_type{});
-                    X.hn_at(rn, comp, row, col) = v;
+                    int hx, hy, comp, row, col;
+                    if (halo_point(X, wid, lane, p, hx, hy, comp, row, col))
+                    {
+                        auto halo = [&](auto unit) {
+                            constexpr bool U = decltype(unit)::value;
+                            if (comp == 0) return fused_h_halo<T, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                            if (comp == 1) return fused_h_halo<T, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                            return fused_h_halo<T, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        };
+                        T v;
+                        if constexpr (sizeof(T) == 8)
+                            v = unit_dx ? halo(std::true_type{}) : halo(std::false_type{});
+                        else
+                            v = halo(std::false_type{});
+                        X.hn_at(rn, comp, row, col) = v;
+                    }
                 }
             }
         }
@@ -1191,25 +1299,32 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     const T *eS0 = X.e_tile(eS, 0) + offE, *eS1 = X.e_tile(eS, 1) + offE, *eS2 = X.e_tile(eS, 2) + offE;
                     const T *n0 = X.hn_plane(rp, 0) + offN, *n1 = X.hn_plane(rp, 1) + offN, *n2 = X.hn_plane(rp, 2) + offN;
                     const T *p0 = X.hn_plane(rpp, 0) + offN, *p1 = X.hn_plane(rpp, 1) + offN;
-                    constexpr int RS = TX + 1;  // ring row stride
-                    T hz[RPT + 1], hx[RPT + 1];  // rows r0-1 .. r0+RPT-1
+                    Vals<T, NPT> hz[RPT + 1], hx[RPT + 1];  // rows r0-1 .. r0+RPT-1
 #pragma unroll
                     for (int r = 0; r <= RPT; ++r)
                     {
-                        hz[r] = n2[(r - 1) * RS];
-                        hx[r] = n0[(r - 1) * RS];
+                        hz[r] = ldv<NPT>(n2 + (r - 1) * RW);
+                        hx[r] = ldv<NPT>(n0 + (r - 1) * RW);
                     }
 #pragma unroll
                     for (int r = 0; r < RPT; ++r)
                     {
-                        const T hzx = n2[r * RS - 1], hyr = n1[r * RS], hyp = p1[r * RS], hyx = n1[r * RS - 1];
-                        const T hxp = p0[r * RS];
-                        const T ex = eS0[r * BX] + coefE * curl_diff<U>(hz[r + 1], hz[r], hyr, hyp, ide);
-                        const T ey = eS1[r * BX] + coefE * curl_diff<U>(hx[r + 1], hxp, hz[r + 1], hzx, ide);
-                        const T ez = eS2[r * BX] + coefE * curl_diff<U>(hyr, hyx, hx[r + 1], hx[r], ide);
-                        st_out(&F.eout[0][idx_e + r * sy], ex);
-                        st_out(&F.eout[1][idx_e + r * sy], ey);
-                        st_out(&F.eout[2][idx_e + r * sy], ez);
+                        const Vals<T, NPT> hyr = ldv<NPT>(n1 + r * RW), hyp = ldv<NPT>(p1 + r * RW), hxp = ldv<NPT>(p0 + r * RW);
+                        const Vals<T, NPT> e0 = ldv<NPT>(eS0 + r * BX), e1 = ldv<NPT>(eS1 + r * BX), e2 = ldv<NPT>(eS2 + r * BX);
+                        // x - 1 neighbours: the previous point of the pair, or the ring column before it
+                        const T hzw = n2[r * RW - 1], hyw = n1[r * RW - 1];
+                        Vals<T, NPT> ex, ey, ez;
+#pragma unroll
+                        for (int p = 0; p < NPT; ++p)
+                        {
+                            const T hzx = p > 0 ? hz[r + 1][p - 1] : hzw, hyx = p > 0 ? hyr[p - 1] : hyw;
+                            ex[p] = e0[p] + coefE * curl_diff<U>(hz[r + 1][p], hz[r][p], hyr[p], hyp[p], ide);
+                            ey[p] = e1[p] + coefE * curl_diff<U>(hx[r + 1][p], hxp[p], hz[r + 1][p], hzx, ide);
+                            ez[p] = e2[p] + coefE * curl_diff<U>(hyr[p], hyx, hx[r + 1][p], hx[r][p], ide);
+                        }
+                        st_outv(&F.eout[0][idx_e + r * sy], ex);
+                        st_outv(&F.eout[1][idx_e + r * sy], ey);
+                        st_outv(&F.eout[2][idx_e + r * sy], ez);
                     }
                 };
                 if constexpr (sizeof(T) == 8)
@@ -1225,56 +1340,60 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                 if (STG && pml_e) cp_async_wait_all();
 #pragma unroll
                 for (int r = 0; r < RPT; ++r)
-                {
-                    // staged psi of the own point (stale where the copy was
-                    // skipped, i.e. where it is not used)
-                    T pe[3][2] = {};
-                    if (STG && pml_e)
-                    {
 #pragma unroll
-                        for (int c = 0; c < 3; ++c)
+                    for (int p = 0; p < NPT; ++p)
+                    {
+                        // staged psi of the own point (stale where the copy was
+                        // skipped, i.e. where it is not used)
+                        T pe[3][2] = {};
+                        if (STG && pml_e)
                         {
-                            pe[c][0] = pstage[(LY::PSI_E + (r * 3 + c) * 2) * NTH];
-                            pe[c][1] = pstage[(LY::PSI_E + (r * 3 + c) * 2 + 1) * NTH];
-                        }
-                    }
-                    auto general_e_own = [&](auto unit) {
-                        constexpr bool U = decltype(unit)::value;
-                        if (lean_e)
-                        {
-                            auto lean = [&](auto ax) {
-                                constexpr int A = decltype(ax)::value;
-                                e_own_general<T, false, STG, U, A>(X, q - 1, r0 + r, eS, rp, rpp, 63u, true, false,
-                                                                   idx_e + r * sy, sl_e[r], pe);
-                            };
-                            if constexpr (kAxisSpec<T>)
+#pragma unroll
+                            for (int c = 0; c < 3; ++c)
                             {
-                                const int ax = ax_e | (X.tab(2, 0)[q - 1].active() ? 4 : 0);
-                                if (ax == 1) lean(std::integral_constant<int, 1>{});
-                                else if (ax == 2) lean(std::integral_constant<int, 2>{});
-                                else if (ax == 4) lean(std::integral_constant<int, 4>{});
+                                pe[c][0] = *stage_slot(r, p, c, 0);
+                                pe[c][1] = *stage_slot(r, p, c, 1);
+                            }
+                        }
+                        const int xi = lane * NPT + p;
+                        auto general_e_own = [&](auto unit) {
+                            constexpr bool U = decltype(unit)::value;
+                            if (lean_e)
+                            {
+                                auto lean = [&](auto ax) {
+                                    constexpr int A = decltype(ax)::value;
+                                    e_own_general<T, false, STG, U, A>(X, q - 1, r0 + r, xi, eS, rp, rpp, 63u, true, false,
+                                                                       idx_e + r * sy + p, sl_e[r][p], pe);
+                                };
+                                if constexpr (kAxisSpec<T>)
+                                {
+                                    const int ax = ax_e | (X.tab(2, 0)[q - 1].active() ? 4 : 0);
+                                    if (ax == 1) lean(std::integral_constant<int, 1>{});
+                                    else if (ax == 2) lean(std::integral_constant<int, 2>{});
+                                    else if (ax == 4) lean(std::integral_constant<int, 4>{});
 #if FFIP_FUSED_F64_AXIS_PAIRS
-                                else if (ax == 3) lean(std::integral_constant<int, 3>{});
-                                else if (ax == 5) lean(std::integral_constant<int, 5>{});
-                                else if (ax == 6) lean(std::integral_constant<int, 6>{});
+                                    else if (ax == 3) lean(std::integral_constant<int, 3>{});
+                                    else if (ax == 5) lean(std::integral_constant<int, 5>{});
+                                    else if (ax == 6) lean(std::integral_constant<int, 6>{});
 #endif
-                                else lean(std::integral_constant<int, 7>{});
+                                    else lean(std::integral_constant<int, 7>{});
+                                }
+                                else
+                                    lean(std::integral_constant<int, 7>{});
                             }
                             else
-                                lean(std::integral_constant<int, 7>{});
+                                e_own_general<T, true, STG, U>(X, q - 1, r0 + r, xi, eS, rp, rpp,
+                                                               vxy[r][p] & (we >> kInfoZValidShift), pml_e, e_slots,
+                                                               idx_e + r * sy + p, sl_e[r][p], pe);
+                        };
+                        if constexpr (sizeof(T) == 8)
+                        {
+                            if (unit_dx) general_e_own(std::true_type{});
+                            else general_e_own(std::false_type{});
                         }
                         else
-                            e_own_general<T, true, STG, U>(X, q - 1, r0 + r, eS, rp, rpp, vxy[r] & (we >> kInfoZValidShift),
-                                                           pml_e, e_slots, idx_e + r * sy, sl_e[r], pe);
-                    };
-                    if constexpr (sizeof(T) == 8)
-                    {
-                        if (unit_dx) general_e_own(std::true_type{});
-                        else general_e_own(std::false_type{});
+                            general_e_own(std::false_type{});
                     }
-                    else
-                        general_e_own(std::false_type{});
-                }
             }
         }
         eS = eA;

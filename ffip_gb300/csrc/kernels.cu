@@ -354,19 +354,20 @@ public:
                 kend = std::max(kend, P.vhi[c][2] + 1);
             }
         }
-        // tiles start at index 1; one or two layers beyond a whole number of
-        // tiles go to k_face
-        const int nxp = xend - 1, nyp = yend - 1;
+        // tiles start at the first index holding grid points (kXFirst along
+        // x, 1 along y); one or two layers beyond a whole number of tiles go
+        // to k_face
+        const int nxp = xend - kXFirst, nyp = yend - 1;
         const int rx = nxp % SH::TX, ry = nyp % SH::TY;
         const int nbx = (nxp >= SH::TX && rx <= 2) ? nxp / SH::TX : (nxp + SH::TX - 1) / SH::TX;
         const int nby = (nyp >= SH::TY && ry <= 2) ? nyp / SH::TY : (nyp + SH::TY - 1) / SH::TY;
-        L.xlim = std::min(xend, 1 + nbx * SH::TX);
+        L.xlim = std::min(xend, kXFirst + nbx * SH::TX);
         L.ylim = std::min(yend, 1 + nby * SH::TY);
         L.xend = xend;
         L.yend = yend;
         L.kbeg = kbeg;
         L.kend = std::max(kend, kbeg + 1);
-        dim3 block(32, 8);  // 8 warps; each thread owns SH::RPT rows of the tile
+        dim3 block(32, 8);  // 8 warps; each thread owns SH::RPT rows and SH::NPT columns of the tile
         // z chunk length: KCH planes, KCH_SHORT when that gives fewer than 20
         // waves of CTAs, fewer still when the grid has too few tiles to fill
         // the GPU twice (each chunk recomputes one H plane, so at least 4)
@@ -585,7 +586,7 @@ public:
                 const bool yin = !any(1, y0 - 1, y0 + TY - 1);
                 for (int bx = 0; bx < std::max(nbx, 1); ++bx)
                 {
-                    const int x0 = 1 + bx * TX;
+                    const int x0 = kXFirst + bx * TX;
                     const bool xin = !any(0, x0 - 1, x0 + TX - 1);
                     (zin && yin && xin ? in : b).push_back(make_int4(x0, y0, ch.first, ch.second));
                 }

@@ -6,8 +6,9 @@
 // 2*x/dx) in which all six components interleave (include/utility.hpp:48-64,
 // 907-1023).  Here every component gets its own dense array, all six with the
 // same shape (Mx_pad, My, Mz), x fastest.  Along an axis whose doubled range
-// is [lo, hi], let o = lo rounded down to even; array index i holds the
-// coordinate o + 2(i-1) (even-parity components) or o + 2(i-1) + 1 (odd).
+// is [lo, hi], let o = lo rounded down to even and f the axis's first index
+// (kXFirst = 4 along x, 1 along y and z); array index i holds the
+// coordinate o + 2(i-f) (even-parity components) or o + 2(i-f) + 1 (odd).
 // With that convention an even-parity point at index i has its odd neighbours
 // at i-1 and i, and an odd-parity point has its even neighbours at i and i+1,
 // whatever lo is.  Array positions that hold no grid point of a component
@@ -27,6 +28,11 @@ namespace ffipg
 {
 constexpr double kPi = 3.141592653589793e+00;  // src/utility.cpp:5
 constexpr int kMaxPoles = 8;                    // poles per grid point in one slot
+// first array index along x that holds grid points: rows start on a
+// 128-byte boundary and the fused pass's tiles start at index kXFirst, so
+// that every tile's TMA box (kXFirst elements to the left of the tile) and
+// the vector loads and stores of its own points are 16-byte aligned
+constexpr int kXFirst = 4;
 
 enum Comp { EX = 0, EY = 1, EZ = 2, HX = 3, HY = 4, HZ = 5 };
 enum BC { BC_PEC = 0, BC_PMC = 1, BC_NONE = 2, BC_SYNC = 3, BC_PERIOD = 4 };
@@ -187,8 +193,11 @@ struct Plan
     int64_t plane() const { return (int64_t)Mx_pad * M[1]; }
     int64_t cells() const { return (int64_t)Mx_pad * M[1] * M[2]; }
     int64_t lin(int i, int j, int k) const { return (int64_t)i + (int64_t)Mx_pad * ((int64_t)j + (int64_t)M[1] * k); }
-    int index_of(int a, int c) const { return (c - o[a] + 2) >> 1; }
-    int coord_of(int a, int i, int parity) const { return o[a] + 2 * (i - 1) + parity; }
+    // first array index that can hold a grid point along axis a (kXFirst
+    // along x, 1 along y and z; the indices before it are zero ghosts)
+    static int first_index(int a) { return a == 0 ? kXFirst : 1; }
+    int index_of(int a, int c) const { return ((c - o[a]) >> 1) + first_index(a); }
+    int coord_of(int a, int i, int parity) const { return o[a] + 2 * (i - first_index(a)) + parity; }
     bool valid(int c, int i, int j, int k) const
     {
         return i >= vlo[c][0] && i <= vhi[c][0] && j >= vlo[c][1] && j <= vhi[c][1] && k >= vlo[c][2] && k <= vhi[c][2];

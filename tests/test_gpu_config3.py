@@ -5,12 +5,15 @@ Workload (ffip_gb300.workloads.adjoint_design): 192 x 192 x 160 cells,
 16-cell CPML, a 96 x 96 x 24 design box (97 x 97 x 25 density nodes of
 seeded filtered noise, eps = 1 + 11 rho), an Ex current sheet below it,
 objective F = sum of |Ex|^2 at 4 seeded probe cells above it at 0.09, 0.1 and
-0.11; every run 5000 steps.  The gradient (one forward run, one adjoint run
-per frequency, the GPU correlation and transpose) is compared with central
+0.11; every run 5000 steps.  The gradient (one forward run, the adjoint
+run(s), the GPU correlation and transpose) is compared with central
 differences (h = 1e-3) of F at 16 seeded density nodes, the differences
 taken with fp64 state (fp32 state rounds F at about 1e-7 of its value, which
 h = 1e-3 turns into noise far above the gradient).  Bound: 1e-3 relative
-per node, for the fp64-state and the fp32-state gradient."""
+per node, for the fp64-state and the fp32-state gradient.  The gradient
+comes from one broadband adjoint run for the three frequencies
+(design.BroadbandAdjoint); with fp64 state it also equals the sum of three
+per-frequency adjoint runs (the reference's scheme) to 1e-3."""
 import numpy as np
 import pytest
 
@@ -55,8 +58,9 @@ def fd(nodes):
 def grads():
     from ffip_gb300 import workloads
     res = {}
-    for precision in ("fp64", "fp32"):
-        prob, rho0 = workloads.adjoint_design(precision=precision)
+    for precision, broadband in (("fp64", True), ("fp32", True), ("fp64 per frequency", False)):
+        prob, rho0 = workloads.adjoint_design(precision=precision.split()[0], broadband=broadband)
+        assert len(prob.terms) == (1 if broadband else 3)
         for s in [prob.forward_simulation] + [t.adjoint_simulation for t in prob.terms]:
             s.device = 0
         try:
@@ -73,3 +77,10 @@ def test_full_size_gradient_matches_central_differences(fd, grads, nodes, precis
     assert abs(F - F0) <= (1e-12 if precision == "fp64" else 1e-4) * abs(F0)
     errs = {n: abs(g[n] - d[n]) / abs(d[n]) for n in nodes}
     assert max(errs.values()) <= 1e-3, errs
+
+
+def test_broadband_adjoint_equals_the_per_frequency_runs(grads):
+    F1, g1 = grads["fp64"]
+    F3, g3 = grads["fp64 per frequency"]
+    assert F1 == F3
+    assert np.abs(g1 - g3).max() <= 1e-3 * np.abs(g3).max()
