@@ -62,8 +62,6 @@
 
 namespace ffipg
 {
-template <typename T>
-struct FusedShape;
 // NPT adjacent x points per thread (vector loads and stores), TX = 32 NPT
 // tile columns; TY tile rows, RPT adjacent rows per thread (8 warps of 32
 // lanes, warp w owns rows RPT w .. RPT w + RPT - 1); SE / SH: TMA stages of
@@ -82,17 +80,26 @@ struct FusedShape;
 #ifndef FFIP_FUSED_F32_NPT
 #define FFIP_FUSED_F32_NPT 2
 #endif
+#ifndef FFIP_FUSED_F32_NPT_PML
+#define FFIP_FUSED_F32_NPT_PML 1
+#endif
 #ifndef FFIP_FUSED_F32_RPT
 #define FFIP_FUSED_F32_RPT 1
 #endif
 #ifndef FFIP_FUSED_F32_SE
-#define FFIP_FUSED_F32_SE 5
+#define FFIP_FUSED_F32_SE 6
+#endif
+#ifndef FFIP_FUSED_F32_SE_X2
+#define FFIP_FUSED_F32_SE_X2 5
 #endif
 #ifndef FFIP_FUSED_F32_SH
 #define FFIP_FUSED_F32_SH 3
 #endif
 #ifndef FFIP_FUSED_F32_MINB
-#define FFIP_FUSED_F32_MINB 2
+#define FFIP_FUSED_F32_MINB 3
+#endif
+#ifndef FFIP_FUSED_F32_MINB_X2
+#define FFIP_FUSED_F32_MINB_X2 2
 #endif
 #ifndef FFIP_FUSED_F32_STAGE_PSI
 #define FFIP_FUSED_F32_STAGE_PSI 1
@@ -120,28 +127,28 @@ struct FusedShape;
 #ifndef FFIP_FUSED_F32_KCH_SHORT
 #define FFIP_FUSED_F32_KCH_SHORT 12
 #endif
-#ifndef FFIP_FUSED_F32_MINB_INTERIOR
-#define FFIP_FUSED_F32_MINB_INTERIOR 2
-#endif
-#ifndef FFIP_FUSED_F64_MINB_INTERIOR
-#define FFIP_FUSED_F64_MINB_INTERIOR 2
-#endif
 constexpr int fused_box_width(int xoff, int tx, int elems16) { return (xoff + tx + 1 + elems16 - 1) / elems16 * elems16; }
-template <>
-struct FusedShape<float>
+// The two instances (P = true: the CPML jobs, P = false: the interior jobs)
+// may take different tile widths: interior jobs are TX-wide tiles of the
+// interior instance's NPT; a column of that width that touches a CPML point
+// runs as TX / TX_P narrower jobs of the CPML instance.
+template <typename T, bool P>
+struct FusedShape;
+template <bool P>
+struct FusedShape<float, P>
 {
-    static constexpr int NPT = FFIP_FUSED_F32_NPT, TX = 32 * NPT, RPT = FFIP_FUSED_F32_RPT, TY = 8 * RPT, XOFF = 4,
-                         BX = fused_box_width(XOFF, TX, 4), RW = XOFF + TX, SE = FFIP_FUSED_F32_SE, SH = FFIP_FUSED_F32_SH,
-                         KCH = FFIP_FUSED_KCH, KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT, MINB = FFIP_FUSED_F32_MINB,
-                         MINB_INTERIOR = FFIP_FUSED_F32_MINB_INTERIOR, STAGE_PSI = FFIP_FUSED_F32_STAGE_PSI;
+    static constexpr int NPT = P ? FFIP_FUSED_F32_NPT_PML : FFIP_FUSED_F32_NPT, TX = 32 * NPT, RPT = FFIP_FUSED_F32_RPT,
+                         TY = 8 * RPT, XOFF = 4, BX = fused_box_width(XOFF, TX, 4), RW = XOFF + TX,
+                         SE = NPT == 1 ? FFIP_FUSED_F32_SE : FFIP_FUSED_F32_SE_X2, SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH,
+                         KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT, MINB = NPT == 1 ? FFIP_FUSED_F32_MINB : FFIP_FUSED_F32_MINB_X2,
+                         STAGE_PSI = FFIP_FUSED_F32_STAGE_PSI;
 };
-template <>
-struct FusedShape<double>
+template <bool P>
+struct FusedShape<double, P>
 {
     static constexpr int NPT = 1, TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 2, BX = fused_box_width(XOFF, TX, 2),
                          RW = XOFF + TX, SE = FFIP_FUSED_F64_SE, SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH,
-                         KCH_SHORT = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB, MINB_INTERIOR = FFIP_FUSED_F64_MINB_INTERIOR,
-                         STAGE_PSI = 0;
+                         KCH_SHORT = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB, STAGE_PSI = 0;
 };
 
 // NPT consecutive values of one row: an aligned vector load / store (float2
@@ -237,10 +244,10 @@ struct alignas(4 * sizeof(T)) PmlCoef
     }
 };
 
-template <typename T>
+template <typename T, bool P>
 struct FusedLayout
 {
-    using SH = FusedShape<T>;
+    using SH = FusedShape<T, P>;
     static constexpr int E_BYTES = (SH::TY + 2) * SH::BX * (int)sizeof(T);  // one E box
     static constexpr int H_BYTES = (SH::TY + 1) * SH::BX * (int)sizeof(T);  // one H box
     static constexpr int E_TILE = (E_BYTES + 127) / 128 * 128;
@@ -469,11 +476,11 @@ __device__ __forceinline__ bool bar_warps_1_7_or(bool v)
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Per-CTA context of the fused pass
-template <typename T>
+template <typename T, bool P>
 struct FusedCtx
 {
-    using SH = FusedShape<T>;
-    using LY = FusedLayout<T>;
+    using SH = FusedShape<T, P>;
+    using LY = FusedLayout<T, P>;
     unsigned char *smem;
     const FusedLaunch<T> *L;
     int x0, y0, k0;
@@ -510,8 +517,8 @@ struct FusedCtx
 
 // accdb increment at one point of component GC from its two curls, CPML
 // coefficients taken from the staged tables (halo points)
-template <typename T, int GC>
-__device__ __forceinline__ T fused_term(const FusedCtx<T> &X, bool pml_plane, int x, int y, int k, int64_t idx, T curl1,
+template <typename T, bool P, int GC>
+__device__ __forceinline__ T fused_term(const FusedCtx<T, P> &X, bool pml_plane, int x, int y, int k, int64_t idx, T curl1,
                                         T curl2, const T *pin1, const T *pin2, T *pout1, T *pout2)
 {
     using C = CompT<GC>;
@@ -546,11 +553,11 @@ __device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &
 // H at the new level of a halo point (not owned: nothing is written),
 // component GC (3..5), point (x, y) of plane k; E stages eA/eB hold planes
 // k/k+1, H stage hA plane k.  Returns 0 where the component has no grid point.
-template <typename T, int GC, bool UNIT = false>
-__device__ __forceinline__ T fused_h_halo(const FusedCtx<T> &X, int x, int y, int k, int eA, int eB, int hA, bool pml_plane,
+template <typename T, bool P, int GC, bool UNIT = false>
+__device__ __forceinline__ T fused_h_halo(const FusedCtx<T, P> &X, int x, int y, int k, int eA, int eB, int hA, bool pml_plane,
                                           bool slots)
 {
-    using SH = FusedShape<T>;
+    using SH = FusedShape<T, P>;
     constexpr int BX = SH::BX, XOFF = SH::XOFF, c = GC - 3;
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PH = F.h;
@@ -580,7 +587,7 @@ __device__ __forceinline__ T fused_h_halo(const FusedCtx<T> &X, int x, int y, in
         curl2 = scale(Ex[o] - Ex[o + BX]);
     }
     const int idx = x + y * (int)PH.sy + k * (int)PH.sz;
-    const T term = fused_term<T, GC>(X, pml_plane, x, y, k, idx, curl1, curl2, F.psih_in[c][0], F.psih_in[c][1], nullptr,
+    const T term = fused_term<T, P, GC>(X, pml_plane, x, y, k, idx, curl1, curl2, F.psih_in[c][0], F.psih_in[c][1], nullptr,
                                      nullptr);
     const T old = X.h_tile(hA, c)[o];
     T vd;
@@ -592,11 +599,11 @@ __device__ __forceinline__ T fused_h_halo(const FusedCtx<T> &X, int x, int y, in
 // row (warps 7 / 6, NPT points per lane), Hz / Hy of the low-x column (warp
 // 5, lanes < TY / < 2 TY, p = 0 only), with its place (row, col) in an H
 // ring plane
-template <typename T>
-__device__ __forceinline__ bool halo_point(const FusedCtx<T> &X, int wid, int lane, int p, int &hx, int &hy, int &comp,
+template <typename T, bool P>
+__device__ __forceinline__ bool halo_point(const FusedCtx<T, P> &X, int wid, int lane, int p, int &hx, int &hy, int &comp,
                                            int &row, int &col)
 {
-    using SH = FusedShape<T>;
+    using SH = FusedShape<T, P>;
     constexpr int TY = SH::TY, NPT = SH::NPT, XOFF = SH::XOFF;
     const int j = lane * NPT + p;
     if (wid == 7) { hx = X.x0 + j; hy = X.y0 - 1; comp = 2; row = 0; col = XOFF + j; }
@@ -612,8 +619,8 @@ __device__ __forceinline__ bool halo_point(const FusedCtx<T> &X, int wid, int la
 // caller), material slots, DFT.  AX: the axes (bit a) along which the tile
 // plane may have CPML at its own points; the others are known to have none
 // (c = 0, 1/k = 1) and their terms are left out of the code (the same bits).
-template <typename T, bool FULL = true, bool UNIT = false, int AX = 7>
-__device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int row, int xi, int eA, int eB, int hA,
+template <typename T, bool P, bool FULL = true, bool UNIT = false, int AX = 7>
+__device__ __forceinline__ void h_own_general(const FusedCtx<T, P> &X, int q, int row, int xi, int eA, int eB, int hA,
                                               int slot_new, unsigned vb, bool owned, bool pml, bool slots, bool dft, int idx,
                                               const T (&ph)[3][2])
 {
@@ -624,7 +631,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
         vb = 63u;
         slots = dft = false;
     }
-    using SH = FusedShape<T>;
+    using SH = FusedShape<T, P>;
     constexpr int BX = SH::BX;
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PH = F.h;
@@ -675,6 +682,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
             st_out(&F.hout[c][idx], v);
             if (hn(a1)) st_out(&F.psih_out[c][0][idx], ps1);
             if (hn(a2)) st_out(&F.psih_out[c][1][idx], ps2);
+            if (dft) dft_point<T>(PH.nunits, PH.units, PH.phase, 3 + c, x, y, k, (double)v, (double)vd);
         }
     }
 }
@@ -684,17 +692,17 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T> &X, int q, int r
 // psi is read from the global arrays, or (STAGED) taken from the values ps
 // the caller read from its staging slots, and written back in place here;
 // sl: material slot indices.
-template <typename T, bool FULL = true, bool STAGED = false, bool UNIT = false, int AX = 7>
-__device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int row, int xi, int eS, int rn, int rp,
-                                              unsigned vb, bool pml, bool slots, int idx, const int (&sl)[3],
+template <typename T, bool P, bool FULL = true, bool STAGED = false, bool UNIT = false, int AX = 7>
+__device__ __forceinline__ void e_own_general(const FusedCtx<T, P> &X, int qe, int row, int xi, int eS, int rn, int rp,
+                                              unsigned vb, bool pml, bool slots, bool dft, int idx, const int (&sl)[3],
                                               const T (&ps)[3][2])
 {
-    using SH = FusedShape<T>;
+    using SH = FusedShape<T, P>;
     constexpr int BX = SH::BX, RW = SH::RW;
     if (!FULL)
     {
         vb = 63u;
-        slots = false;
+        slots = dft = false;
     }
     const FusedParams<T> &F = X.L->fp;
     const SideParams<T> &PE = F.e;
@@ -760,6 +768,7 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
             st_out(&F.eout[c][idx], v);
             if (en(a1)) st_out(&PE.psi[c][0][idx], ps1);
             if (en(a2)) st_out(&PE.psi[c][1][idx], ps2);
+            if (dft) dft_point<T>(PE.nunits, PE.units, PE.phase, c, x, y, k, (double)v, (double)vd);
         }
     }
 }
@@ -767,11 +776,10 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T> &X, int qe, int 
 // PML = false: the instance for jobs whose tiles, halos and planes hold no
 // CPML point (the host sorts the jobs); it carries no CPML code.
 template <typename T, bool PML>
-__global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>::MINB_INTERIOR)
-    k_fused(const __grid_constant__ FusedLaunch<T> L)
+__global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const __grid_constant__ FusedLaunch<T> L)
 {
-    using SH = FusedShape<T>;
-    using LY = FusedLayout<T>;
+    using SH = FusedShape<T, PML>;
+    using LY = FusedLayout<T, PML>;
     constexpr int TX = SH::TX, TY = SH::TY, RPT = SH::RPT, NPT = SH::NPT, XOFF = SH::XOFF, SE = SH::SE, SHS = SH::SH,
                   BX = SH::BX, RW = SH::RW;
     constexpr int NTH = 256;
@@ -781,7 +789,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     const SideParams<T> &PH = F.h;
     const int lane = threadIdx.x, wid = threadIdx.y, tid = wid * 32 + lane;
     const int r0 = wid * RPT;  // first tile row of this thread
-    FusedCtx<T> X;
+    FusedCtx<T, PML> X;
     X.smem = smem;
     X.L = &L;
     const uint64_t keep = l2_keep_policy();
@@ -930,10 +938,14 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
     {
         const unsigned w = info[o];
         const bool zpml = pml_tables && (tile_pml || (w & kInfoZPml));
-        const bool hok = inside && !h_slots && !(w & kInfoDftH) && ((w >> (kInfoZValidShift + 3)) & 7u) == 7u;
-        const bool eok = inside && !(w & kInfoDftE) && ((w >> kInfoZValidShift) & 7u) == 7u;
-        info[o] = w | (zpml ? kInfoZPml : 0u) | (hok ? (zpml ? kInfoLeanH : kInfoFastH) : 0u) |
-                  (eok ? (zpml ? kInfoLeanE : kInfoFastE) : 0u) | (zcol ? kInfoZeroCol : 0u) | (zrow ? kInfoZeroRow : 0u);
+        // the plain paths also serve planes that a DFT unit meets (they add
+        // the sums of the unit's points); the lean CPML paths do not
+        const bool hok = inside && !h_slots && ((w >> (kInfoZValidShift + 3)) & 7u) == 7u;
+        const bool eok = inside && ((w >> kInfoZValidShift) & 7u) == 7u;
+        const bool hlean = hok && !(w & kInfoDftH), elean = eok && !(w & kInfoDftE);
+        info[o] = w | (zpml ? kInfoZPml : 0u) | (hok && !zpml ? kInfoFastH : 0u) | (hlean && zpml ? kInfoLeanH : 0u) |
+                  (eok && !zpml ? kInfoFastE : 0u) | (elean && zpml ? kInfoLeanE : 0u) | (zcol ? kInfoZeroCol : 0u) |
+                  (zrow ? kInfoZeroRow : 0u);
     }
     }
 
@@ -1007,7 +1019,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         const bool lean_e = PML && (we & kInfoLeanE) && !e_slots;
         const bool pml_h = !fast_h && pml_tables && (wh & kInfoZPml);
         const bool pml_e = !fast_e && pml_tables && (we & kInfoZPml);
-        const bool dft_h = wh & kInfoDftH;
+        const bool dft_h = wh & kInfoDftH, dft_e = we & kInfoDftE;
         // CPML psi of this iteration's own H points, loaded before the TMA wait
         T ph[RPT][NPT][3][2];
 #pragma unroll
@@ -1168,6 +1180,20 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                             st_outv(&F.hout[1][idx + r * sy], hn1[r]);
                             st_outv(&F.hout[2][idx + r * sy], hn2[r]);
                         }
+                        // DFT sums of the points of the tile plane that a unit
+                        // meets (D/B value: g_inf of the default medium times H)
+                        if (dft_h)
+                            for (int r = 0; r < RPT; ++r)
+                                for (int p = 0; p < NPT; ++p)
+                                {
+                                    const T hv[3] = {hn0[r][p], hn1[r][p], hn2[r][p]};
+                                    for (int c = 0; c < 3; ++c)
+                                    {
+                                        const T vd = PH.g_def * hv[c];
+                                        dft_point<T>(PH.nunits, PH.units, PH.phase, 3 + c, x + p, X.y0 + r0 + r, k, (double)hv[c],
+                                                     (double)vd);
+                                    }
+                                }
                     }
                 };
                 if constexpr (sizeof(T) == 8)
@@ -1227,7 +1253,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                             for (int r = 0; r < RPT; ++r)
 #pragma unroll
                                 for (int p = 0; p < NPT; ++p)
-                                    h_own_general<T, false, U, A>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn, 63u, q >= 1, true,
+                                    h_own_general<T, PML, false, U, A>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn, 63u, q >= 1, true,
                                                                   false, false, idx + r * sy + p, ph[r][p]);
                         };
                         // fp64: a tile plane with CPML along one axis only
@@ -1254,7 +1280,7 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                         for (int r = 0; r < RPT; ++r)
 #pragma unroll
                             for (int p = 0; p < NPT; ++p)
-                                h_own_general<T, true, U>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn,
+                                h_own_general<T, PML, true, U>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn,
                                                           vxy[r][p] & (wh >> kInfoZValidShift), q >= 1, pml_h, h_slots, dft_h,
                                                           idx + r * sy + p, ph[r][p]);
                     }
@@ -1274,9 +1300,9 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                     {
                         auto halo = [&](auto unit) {
                             constexpr bool U = decltype(unit)::value;
-                            if (comp == 0) return fused_h_halo<T, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                            if (comp == 1) return fused_h_halo<T, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                            return fused_h_halo<T, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                            if (comp == 0) return fused_h_halo<T, PML, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                            if (comp == 1) return fused_h_halo<T, PML, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                            return fused_h_halo<T, PML, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
                         };
                         T v;
                         if constexpr (sizeof(T) == 8)
@@ -1325,6 +1351,17 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                         st_outv(&F.eout[0][idx_e + r * sy], ex);
                         st_outv(&F.eout[1][idx_e + r * sy], ey);
                         st_outv(&F.eout[2][idx_e + r * sy], ez);
+                        if (dft_e)
+                            for (int p = 0; p < NPT; ++p)
+                            {
+                                const T ev[3] = {ex[p], ey[p], ez[p]};
+                                for (int c = 0; c < 3; ++c)
+                                {
+                                    const T vd = PE.g_def * ev[c];
+                                    dft_point<T>(PE.nunits, PE.units, PE.phase, c, x + p, X.y0 + r0 + r, k - 1, (double)ev[c],
+                                                 (double)vd);
+                                }
+                            }
                     }
                 };
                 if constexpr (sizeof(T) == 8)
@@ -1362,8 +1399,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                             {
                                 auto lean = [&](auto ax) {
                                     constexpr int A = decltype(ax)::value;
-                                    e_own_general<T, false, STG, U, A>(X, q - 1, r0 + r, xi, eS, rp, rpp, 63u, true, false,
-                                                                       idx_e + r * sy + p, sl_e[r][p], pe);
+                                    e_own_general<T, PML, false, STG, U, A>(X, q - 1, r0 + r, xi, eS, rp, rpp, 63u, true, false,
+                                                                       false, idx_e + r * sy + p, sl_e[r][p], pe);
                                 };
                                 if constexpr (kAxisSpec<T>)
                                 {
@@ -1382,8 +1419,8 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
                                     lean(std::integral_constant<int, 7>{});
                             }
                             else
-                                e_own_general<T, true, STG, U>(X, q - 1, r0 + r, xi, eS, rp, rpp,
-                                                               vxy[r][p] & (we >> kInfoZValidShift), pml_e, e_slots,
+                                e_own_general<T, PML, true, STG, U>(X, q - 1, r0 + r, xi, eS, rp, rpp,
+                                                               vxy[r][p] & (we >> kInfoZValidShift), pml_e, e_slots, dft_e,
                                                                idx_e + r * sy + p, sl_e[r][p], pe);
                         };
                         if constexpr (sizeof(T) == 8)
@@ -1405,83 +1442,6 @@ __global__ void __launch_bounds__(256, PML ? FusedShape<T>::MINB : FusedShape<T>
         rn = (rn + 1) & 3;
     }
     if (STG) cp_async_wait_all();
-}
-
-// DFT sums of one side after the fused pass (DFT_Unit::update,
-// src/dft.cpp:29-62): one thread per monitored point of the side's units,
-// reading the new field from the pass's output buffers; for D/B monitors the
-// value is g_inf field + sum of the new polarisations, as material_at forms
-// it.  The fused pass itself leaves the sums alone, so that its registers
-// carry no DFT code; this runs before the E sources, which add their own
-// share of the sums.
-template <typename T>
-__global__ void k_dft(const __grid_constant__ SideParams<T> P, const T *f0, const T *f1, const T *f2, int64_t total)
-{
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= total) return;
-    int u = 0;
-    int64_t base = 0;
-    for (; u < P.nunits; ++u)
-    {
-        if (t < base + P.units[u].npts) break;
-        base += P.units[u].npts;
-    }
-    if (u == P.nunits) return;
-    const DftView &U = P.units[u];
-    const int64_t l = t - base;
-    const int li = (int)(l % U.ld[0]), lj = (int)((l / U.ld[0]) % U.ld[1]), lk = (int)(l / ((int64_t)U.ld[0] * U.ld[1]));
-    const int i = U.i0[0] + li, j = U.i0[1] + lj, k = U.i0[2] + lk;
-    const int c = U.comp - P.comp_base;
-    if (i < P.vlo[c][0] || i > P.vhi[c][0] || j < P.vlo[c][1] || j > P.vhi[c][1] || k < P.vlo[c][2] || k > P.vhi[c][2]) return;
-    const int64_t idx = (int64_t)i + (int64_t)j * P.sy + (int64_t)k * P.sz;
-    const T v = (c == 0 ? f0 : c == 1 ? f1 : f2)[idx];
-    T vd = P.g_def * v;
-    if (U.is_db)
-    {
-        const SlotView<T> &S = P.slot[c];
-        const int slot = S.map ? S.map[idx] : -1;
-        if (slot >= 0)
-        {
-            const int g = S.group[slot];
-            const int np = P.grp_np[g];
-            if (np == 0)
-                vd = S.g[slot] * v;
-            else
-            {
-                T psum = T(0);
-                for (int q = 0; q < np; ++q) psum = psum + S.P[q * S.n + slot];
-                vd = fma_rn(S.g[slot], v, psum);
-            }
-        }
-    }
-    const double x = U.is_db ? (double)vd : (double)v;
-    // eight frequencies at a time: their sixteen loads are in flight together
-    for (int f0 = 0; f0 < U.nf; f0 += 8)
-    {
-        const int nb = min(8, U.nf - f0);
-        double re[8], im[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (j < nb)
-            {
-                im[j] = U.im[(f0 + j) * U.npts + l];
-                re[j] = U.re[(f0 + j) * U.npts + l];
-            }
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (j < nb)
-            {
-                im[j] += P.phase[U.foff + f0 + j][1] * x;
-                re[j] += P.phase[U.foff + f0 + j][0] * x;
-            }
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            if (j < nb)
-            {
-                U.im[(f0 + j) * U.npts + l] = im[j];
-                U.re[(f0 + j) * U.npts + l] = re[j];
-            }
-    }
 }
 
 // One point of the last x / y layers that the fused pass leaves out (same

@@ -21,6 +21,7 @@
 #include <type_traits>
 #include <stdexcept>
 #include <string>
+#include <tuple>
 
 #include "engine.hpp"
 #include "fused.cuh"
@@ -194,7 +195,6 @@ public:
     ~CudaBackend() override
     {
         cudaSetDevice(dev_);
-        if (dft_) cudaStreamSynchronize(dft_);
         cudaStreamSynchronize(stream_);
         if (err_) cudaFree(err_);
         if (flag_) cudaFree(flag_);
@@ -208,24 +208,7 @@ public:
             cudaEventDestroy(ev.first);
             cudaEventDestroy(ev.second);
         }
-        if (dft_)
-        {
-            cudaEventDestroy(dft_ready_);
-            cudaEventDestroy(dft_join_);
-            for (cudaEvent_t e : dft_done_) cudaEventDestroy(e);
-            cudaStreamDestroy(dft_);
-        }
         cudaStreamDestroy(stream_);
-    }
-    // The fused pass's DFT sums run on their own stream, beside the next
-    // pass (see fused_t); every other operation of the handle first orders
-    // the handle's stream after them.
-    void join_dft()
-    {
-        if (!dft_pending_) return;
-        check(cudaEventRecord(dft_join_, dft_), "cudaEventRecord");
-        check(cudaStreamWaitEvent(stream_, dft_join_, 0), "cudaStreamWaitEvent");
-        dft_pending_ = false;
     }
     // every entry re-selects the handle's device: calls may come from any thread
     void use() const { check(cudaSetDevice(dev_), "cudaSetDevice"); }
@@ -240,14 +223,12 @@ public:
     void release(void *p) override
     {
         cudaSetDevice(dev_);
-        if (dft_) cudaStreamSynchronize(dft_);
         cudaStreamSynchronize(stream_);
         cudaFree(p);
     }
     void h2d(void *dst, const void *src, size_t bytes) override
     {
         use();
-        join_dft();
         h2d_bytes += bytes;
         check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream_), "cudaMemcpy H2D");
         check(cudaStreamSynchronize(stream_), "h2d sync");
@@ -255,7 +236,6 @@ public:
     void d2h(void *dst, const void *src, size_t bytes) override
     {
         use();
-        join_dft();
         d2h_bytes += bytes;
         check(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream_), "cudaMemcpy D2H");
         check(cudaStreamSynchronize(stream_), "d2h sync");
@@ -263,13 +243,11 @@ public:
     void zero(void *p, size_t bytes) override
     {
         use();
-        join_dft();
         check(cudaMemsetAsync(p, 0, bytes, stream_), "cudaMemsetAsync");
     }
     void sync() override
     {
         use();
-        join_dft();
         check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
         check_err();
     }
@@ -293,8 +271,13 @@ public:
     int fused_t(const FusedParams<T> &p)
     {
         use();
-        using SH = FusedShape<T>;
-        using LY = FusedLayout<T>;
+        // interior instance (SH: its tiles define the column grid) and CPML
+        // instance (SP: TX / SP::TX jobs per column)
+        using SH = FusedShape<T, false>;
+        using SP = FusedShape<T, true>;
+        using LY = FusedLayout<T, false>;
+        using LP = FusedLayout<T, true>;
+        static_assert(SH::TX % SP::TX == 0 && SH::TY == SP::TY && SH::KCH == SP::KCH, "instance shapes do not nest");
         if (!err_)
         {
             check(cudaMalloc(&err_, sizeof(int)), "cudaMalloc");
@@ -312,34 +295,28 @@ public:
             // go through
             int maxsm = 0;
             check(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev_), "cudaDeviceGetAttribute");
-            const int64_t need = std::max<int64_t>((int64_t)SH::MINB * (LY::SMEM_PML + 1024),
-                                                   (int64_t)SH::MINB_INTERIOR * (LY::SMEM + 1024));
+            const int64_t need = std::max<int64_t>((int64_t)SP::MINB * (LP::SMEM_PML + 1024), (int64_t)SH::MINB * (LY::SMEM + 1024));
             const int carve = FFIP_FUSED_CARVEOUT >= 0 ? FFIP_FUSED_CARVEOUT
                                                        : (int)std::min<int64_t>(100, (need * 100 + maxsm - 1) / std::max(maxsm, 1));
             for (int pml = 0; pml < 2; ++pml)
             {
                 const auto fn = pml ? k_fused<T, true> : k_fused<T, false>;
-                check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pml ? LY::SMEM_PML : LY::SMEM),
+                check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pml ? LP::SMEM_PML : LY::SMEM),
                       "cudaFuncSetAttribute");
                 check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve), "cudaFuncSetAttribute");
             }
         });
-        // the DFT sums of two passes ago (on dft_) read the output buffers of
-        // this pass
-        const int par = passes_ & 1;
-        if (dft_valid_[par]) check(cudaStreamWaitEvent(stream_, dft_done_[par], 0), "cudaStreamWaitEvent");
-        dft_valid_[par] = false;
-        ++passes_;
         FusedLaunch<T> L;
+        FusedLaunch<T> LC;  // the CPML instance's copy: tensor maps of its box width
         for (int c = 0; c < 3; ++c)
         {
             L.tm_e[c] = map_for(p.ein[c], p.e.Mx, p.e.My, p.e.Mz, SH::BX, SH::TY + 2);
             L.tm_h[c] = map_for(p.hin[c], p.e.Mx, p.e.My, p.e.Mz, SH::BX, SH::TY + 1);
+            LC.tm_e[c] = map_for(p.ein[c], p.e.Mx, p.e.My, p.e.Mz, SP::BX, SP::TY + 2);
+            LC.tm_h[c] = map_for(p.hin[c], p.e.Mx, p.e.My, p.e.Mz, SP::BX, SP::TY + 1);
         }
-        // DFT sums are added by k_dft after the pass, not inside it
+        // the DFT sums of the monitored points are added inside the pass
         L.fp = p;
-        L.fp.e.nunits = 0;
-        L.fp.h.nunits = 0;
         L.err = err_;
         // valid extents over all six components
         int xend = 0, yend = 0, kbeg = p.e.Mz, kend = 0;
@@ -378,7 +355,15 @@ public:
         const int64_t zlen = L.kend - L.kbeg;
         const int kmax = zlen * tiles < 20 * slots * SH::KCH ? SH::KCH_SHORT : SH::KCH;
         const int kch = (int)std::max<int64_t>(4, std::min<int64_t>(kmax, (zlen * tiles + want - 1) / want));
-        const Jobs &J = jobs_for(p, L, nbx, nby, SH::TX, SH::TY, kch);
+        const Jobs &J = jobs_for(p, L, nbx, nby, SH::TX, SP::TX, SH::TY, kch);
+        LC.fp = L.fp;
+        LC.err = L.err;
+        LC.xlim = L.xlim;
+        LC.ylim = L.ylim;
+        LC.xend = L.xend;
+        LC.yend = L.yend;
+        LC.kbeg = L.kbeg;
+        LC.kend = L.kend;
         int n = 0;
         const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
         const unsigned face_blocks = (unsigned)((nface + 255) / 256);
@@ -428,8 +413,8 @@ public:
         }
         if (J.nb > 0)
         {
-            L.jobs = J.dev;
-            k_fused<T, true><<<J.nb, block, LY::SMEM_PML, stream_>>>(L);
+            LC.jobs = J.dev;
+            k_fused<T, true><<<J.nb, block, LP::SMEM_PML, stream_>>>(LC);
             check(cudaGetLastError(), "k_fused launch");
             ++n;
         }
@@ -463,52 +448,6 @@ public:
             check(cudaGetLastError(), "k_face launch");
             ++n;
         }
-        // DFT sums of both sides from the new fields.  They read only this
-        // pass's output fields (and, for D/B monitors, the polarisations the
-        // next pass updates in place), so without D/B monitors they run on
-        // their own stream beside the next pass: the next-but-one pass, which
-        // overwrites these buffers, waits for them (above); sources, which
-        // add to the same sums, and every other operation join them first.
-        int64_t total[2] = {0, 0};
-        bool db = false;
-        for (int sd = 0; sd < 2; ++sd)
-        {
-            const SideParams<T> &P = sd == 0 ? p.e : p.h;
-            for (int u = 0; u < P.nunits; ++u)
-            {
-                total[sd] += P.units[u].npts;
-                db = db || P.units[u].is_db;
-            }
-        }
-        cudaStream_t ds = stream_;
-        if (total[0] + total[1] > 0 && !db)
-        {
-            if (!dft_)
-            {
-                check(cudaStreamCreateWithFlags(&dft_, cudaStreamNonBlocking), "cudaStreamCreate");
-                check(cudaEventCreateWithFlags(&dft_ready_, cudaEventDisableTiming), "cudaEventCreate");
-                check(cudaEventCreateWithFlags(&dft_join_, cudaEventDisableTiming), "cudaEventCreate");
-                for (cudaEvent_t &e : dft_done_) check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
-            }
-            check(cudaEventRecord(dft_ready_, stream_), "cudaEventRecord");
-            check(cudaStreamWaitEvent(dft_, dft_ready_, 0), "cudaStreamWaitEvent");
-            ds = dft_;
-        }
-        for (int sd = 0; sd < 2; ++sd)
-        {
-            if (!total[sd]) continue;
-            const SideParams<T> &P = sd == 0 ? p.e : p.h;
-            T *const *f = sd == 0 ? p.eout : p.hout;
-            k_dft<T><<<(unsigned)((total[sd] + 255) / 256), 256, 0, ds>>>(P, f[0], f[1], f[2], total[sd]);
-            check(cudaGetLastError(), "k_dft launch");
-            ++n;
-        }
-        if (ds == dft_)
-        {
-            check(cudaEventRecord(dft_done_[par], dft_), "cudaEventRecord");
-            dft_valid_[par] = true;
-            dft_pending_ = true;
-        }
         return n;
     }
     int fused(const FusedParams<double> &p) override { return fused_t(p); }
@@ -527,12 +466,12 @@ public:
         bool face_in_pml{false};
     };
     template <typename T>
-    const Jobs &jobs_for(const FusedParams<T> &p, const FusedLaunch<T> &L, int nbx, int nby, int TX, int TY, int KCH)
+    const Jobs &jobs_for(const FusedParams<T> &p, const FusedLaunch<T> &L, int nbx, int nby, int TX, int TXP, int TY, int KCH)
     {
         const SideParams<T> &P = p.e;
         char key[160];
-        std::snprintf(key, sizeof key, "%d %d %d %d %d %d %d %d %p %d", L.xlim, L.ylim, L.kbeg, L.kend, nbx, nby, TY, KCH,
-                      (const void *)P.pc[0][0], (int)sizeof(T));
+        std::snprintf(key, sizeof key, "%d %d %d %d %d %d %d %d %d %d %p %d", L.xlim, L.ylim, L.kbeg, L.kend, nbx, nby, TX, TXP, TY,
+                      KCH, (const void *)P.pc[0][0], (int)sizeof(T));
         auto it = jobs_.find(key);
         if (it != jobs_.end()) return it->second;
         // CPML flags per position along each axis (either parity)
@@ -588,7 +527,11 @@ public:
                 {
                     const int x0 = kXFirst + bx * TX;
                     const bool xin = !any(0, x0 - 1, x0 + TX - 1);
-                    (zin && yin && xin ? in : b).push_back(make_int4(x0, y0, ch.first, ch.second));
+                    if (zin && yin && xin)
+                        in.push_back(make_int4(x0, y0, ch.first, ch.second));
+                    else  // a column that touches a CPML point: TX / TXP jobs of the CPML instance
+                        for (int h = 0; h < TX / TXP; ++h)
+                            if (x0 + h * TXP < L.xlim) b.push_back(make_int4(x0 + h * TXP, y0, ch.first, ch.second));
                 }
             }
         }
@@ -607,7 +550,7 @@ public:
     template <typename T>
     CUtensorMap map_for(const T *base, int Mx, int My, int Mz, int bx, int by)
     {
-        auto key = std::make_pair((const void *)base, by);
+        auto key = std::make_tuple((const void *)base, bx, by);
         auto it = maps_.find(key);
         if (it != maps_.end()) return it->second;
         CUtensorMap m = make_map(base, Mx, My, Mz, bx, by);
@@ -619,7 +562,6 @@ public:
     void check_err()
     {
         if (!err_) return;
-        join_dft();
         int e = 0;
         check(cudaMemcpyAsync(&e, err_, sizeof(int), cudaMemcpyDeviceToHost, stream_), "cudaMemcpy err flag");
         check(cudaStreamSynchronize(stream_), "sync");
@@ -631,7 +573,6 @@ public:
     {
         if (!err_) return;
         use();
-        join_dft();
         check(cudaMemsetAsync(err_, 0, sizeof(int), stream_), "cudaMemsetAsync");
     }
 
@@ -639,7 +580,6 @@ public:
     bool any_nonfinite_t(const T *const *f, int nf, int64_t n)
     {
         use();
-        join_dft();
         if (!flag_) check(cudaMalloc(&flag_, sizeof(int)), "cudaMalloc");
         check(cudaMemsetAsync(flag_, 0, sizeof(int), stream_), "cudaMemsetAsync");
         if (!nsm_) check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
@@ -662,7 +602,6 @@ public:
     {
         if (!p.npts) return;
         use();
-        join_dft();
         k_sources<T><<<(p.npts + 127) / 128, 128, 0, stream_>>>(p);
         check(cudaGetLastError(), "k_sources launch");
     }
@@ -679,7 +618,6 @@ public:
             mv = max(mv, p.faces[f].v1);
         }
         use();
-        join_dft();
         dim3 block(32, 8);
         dim3 grid((mu + 31) / 32, (mv + 7) / 8, p.nfaces);
         k_ghosts<T><<<grid, block, 0, stream_>>>(p);
@@ -703,7 +641,6 @@ public:
     void dft_norm(const double *re, const double *im, int64_t n, double *out) override
     {
         use();
-        join_dft();
         k_dft_norm<<<1, 256, 0, stream_>>>(re, im, n, out);
         check(cudaGetLastError(), "k_dft_norm launch");
     }
@@ -719,8 +656,7 @@ public:
         {
             check(cudaEventRecord(a, stream_), "cudaEventRecord");
             f();
-            join_dft();
-            check(cudaEventRecord(b, stream_), "cudaEventRecord");
+                check(cudaEventRecord(b, stream_), "cudaEventRecord");
             check(cudaEventSynchronize(b), "cudaEventSynchronize");
             check(cudaEventElapsedTime(&ms, a, b), "cudaEventElapsedTime");
             check_err();
@@ -761,7 +697,6 @@ public:
     cudaStream_t stream()
     {
         use();
-        join_dft();
         return stream_;
     }
 
@@ -770,17 +705,11 @@ private:
     int dev_{0};
     int *err_{nullptr};
     int *flag_{nullptr};  // result word of the divergence check
-    std::map<std::pair<const void *, int>, CUtensorMap> maps_;
+    std::map<std::tuple<const void *, int, int>, CUtensorMap> maps_;
     std::map<std::string, Jobs> jobs_;
     cudaStream_t side_{nullptr};
     int nsm_{0};
     cudaEvent_t fork_{nullptr}, join_{nullptr}, face_h_{nullptr};
-    // DFT sums of the fused pass: their stream, the event they wait for, the
-    // event after them per pass parity, and a join event
-    cudaStream_t dft_{nullptr};
-    cudaEvent_t dft_ready_{nullptr}, dft_join_{nullptr}, dft_done_[2]{nullptr, nullptr};
-    bool dft_valid_[2]{false, false}, dft_pending_{false};
-    int64_t passes_{0};
     // timing events of the fused passes (time_passes / pass_ms): pairs in
     // use and the pool, reused across calls
     static constexpr size_t kPassEvents = 1024;

@@ -1,6 +1,6 @@
 """The surrogate's kernels (tensor-core bf16 GEMM, im2col, col2im) and its
-convolution against plain PyTorch fp32 references of the same operations on
-the same bf16-rounded inputs."""
+convolution, forward and backward, against CPU fp64 oracles (numpy / torch on
+the CPU in float64) of the same operations on the same bf16-rounded inputs."""
 import numpy as np
 import pytest
 
@@ -18,11 +18,11 @@ def test_gemm_matches_fp32_reference(M, N, K):
     g = torch.Generator(device="cuda").manual_seed(M * 7 + N)
     A = _bf(torch.randn(M, K, device="cuda", generator=g))
     B = _bf(torch.randn(K, N, device="cuda", generator=g))
-    ref = A.float() @ B.float()
-    got = S.gemm(A, B)
-    # bf16 products are exact in fp32; only the summation order differs
-    tol = 1e-5 * K ** 0.5 * ref.abs().max().item() + 1e-6
-    assert (got - ref).abs().max().item() <= tol
+    ref = A.cpu().double().numpy() @ B.cpu().double().numpy()  # CPU fp64 oracle
+    got = S.gemm(A, B).cpu().double().numpy()
+    # bf16 products are exact in fp32; the fp32 accumulation rounds
+    tol = 1e-5 * K ** 0.5 * np.abs(ref).max() + 1e-6
+    assert np.abs(got - ref).max() <= tol
 
 
 def test_gemm_strides_bias_and_accumulate():
@@ -32,10 +32,11 @@ def test_gemm_strides_bias_and_accumulate():
     B = _bf(torch.randn(90, 50, device="cuda", generator=g)).t()   # [50, 90], column-major view
     bias = torch.randn(40, device="cuda", generator=g)
     C0 = torch.randn(40, 90, device="cuda", generator=g)
-    ref = C0 + (A.t().float() @ B.float() + bias[:, None])
+    D = lambda t: t.cpu().double().numpy()  # noqa: E731
+    ref = D(C0) + (D(A.t()) @ D(B) + D(bias)[:, None])  # CPU fp64 oracle
     out = C0.clone()
     S.gemm(A.t(), B, bias=bias, out=out, accumulate=True)
-    assert (out - ref).abs().max().item() <= 1e-4
+    assert np.abs(D(out) - ref).max() <= 1e-4
 
 
 @pytest.mark.parametrize("dims", [3, 2])
@@ -52,23 +53,27 @@ def test_conv_forward_and_backward_match_fp32_reference(dims):
         w = _bf(torch.randn(7, 5, 1, 3, 3, device="cuda", generator=g) * 0.2).float()
         stride, pad = (1, 1, 1), (0, 1, 1)
     b = torch.randn(7, device="cuda", generator=g)
-    xr = x.float().requires_grad_(True)
-    wr = w.clone().requires_grad_(True)
-    br = b.clone().requires_grad_(True)
+    # CPU fp64 oracle of the convolution and its gradients
+    xr = x.cpu().double().requires_grad_(True)
+    wr = w.cpu().double().requires_grad_(True)
+    br = b.cpu().double().requires_grad_(True)
     yr = F.conv3d(xr, wr, br, stride=stride, padding=pad)
     dy = _bf(torch.randn(yr.shape, device="cuda", generator=g))
-    yr.backward(dy.float())
+    yr.backward(dy.cpu().double())
     xs = x.clone().requires_grad_(True)
     ws = w.clone().requires_grad_(True)
     bs = b.clone().requires_grad_(True)
     ys = S.conv(xs, ws, bs, stride, pad)
     assert ys.dtype == torch.bfloat16 and ys.shape == yr.shape
-    # the forward output is rounded to bf16
-    assert (ys.float() - yr).abs().max().item() <= 1e-2 * yr.abs().max().item()
+    C = lambda t: t.detach().cpu().double()  # noqa: E731
+    # the forward output is rounded to bf16 (relative 2^-8)
+    assert (C(ys) - C(yr)).abs().max().item() <= 1e-2 * C(yr).abs().max().item()
     ys.backward(dy)
-    assert (ws.grad - wr.grad).abs().max().item() <= 1e-4 * wr.grad.abs().max().item()
-    assert (bs.grad - br.grad).abs().max().item() <= 1e-4 * br.grad.abs().max().item()
-    assert (xs.grad.float() - xr.grad).abs().max().item() <= 1e-2 * xr.grad.abs().max().item()
+    # weight / bias gradients accumulate in fp32 from bf16 operands
+    assert (C(ws.grad) - C(wr.grad)).abs().max().item() <= 1e-4 * C(wr.grad).abs().max().item()
+    assert (C(bs.grad) - C(br.grad)).abs().max().item() <= 1e-4 * C(br.grad).abs().max().item()
+    # the input gradient is rounded to bf16
+    assert (C(xs.grad) - C(xr.grad)).abs().max().item() <= 1e-2 * C(xr.grad).abs().max().item()
 
 
 def test_network_shapes_and_a_few_training_steps_reduce_the_loss():
