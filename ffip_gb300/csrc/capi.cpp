@@ -3,6 +3,7 @@
 #include "../../include/ffip_gb300_surrogate.h"
 
 #include <cstring>
+#include <algorithm>
 #include <map>
 #include <memory>
 #include <stdexcept>
@@ -329,6 +330,22 @@ int ffip_check_inside(const double *req_pts, uint64_t n, const double *poly_pts,
         if ((n && (!req_pts || !out)) || (m && !poly_pts)) return fail(FFIP_ERR_INVALID, "null argument");
         if (n > (uint64_t(1) << 31) || m > (uint64_t(1) << 31)) return fail(FFIP_ERR_INVALID, "array too large");
         return ffipg::check_inside(req_pts, n, poly_pts, m, out);
+    });
+}
+
+int ffip_flux(ffip_sim *sim, const char *e1_group, const char *h2_group, const double *x, uint64_t nx, const double *y,
+              uint64_t ny, const double *z, uint64_t nz, const double *w, const double *freqs, uint64_t nf, double *flux)
+{
+    return guard([&]() -> int {
+        if (!sim || !e1_group || !h2_group || !x || !y || !z || !w || !flux || (!freqs && nf))
+            return fail(FFIP_ERR_INVALID, "null argument");
+        if (!nx || !ny || !nz) return fail(FFIP_ERR_INVALID, "flux: empty integration grid");
+        if (nx > (1u << 30) || ny > (1u << 30) || nz > (1u << 30) || nx * ny > (1ull << 40) || nx * ny * nz > (1ull << 40))
+            return fail(FFIP_ERR_INVALID, "flux: integration grid too large");
+        std::vector<double> vx(x, x + nx), vy(y, y + ny), vz(z, z + nz), vw(w, w + nx * ny * nz), vf(freqs, freqs + nf);
+        auto r = sim->eng->flux(e1_group, h2_group, vx, vy, vz, vw, vf);
+        std::copy(r.begin(), r.end(), flux);
+        return FFIP_OK;
     });
 }
 

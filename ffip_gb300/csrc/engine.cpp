@@ -62,6 +62,9 @@ public:
     void set_source_data(const std::map<std::string, std::vector<double>> &data) override;
     double bytes_per_step() const override { return bytes_per_step_; }
     double pass_bytes_per_step() const override { return pass_bytes_per_step_; }
+    std::vector<double> flux(const std::string &e1_group, const std::string &h2_group, const std::vector<double> &x,
+                             const std::vector<double> &y, const std::vector<double> &z, const std::vector<double> &w,
+                             const std::vector<double> &freqs) override;
 
 private:
     Plan P_;
@@ -195,6 +198,73 @@ void Engine<T>::init()
     init_ghosts();
     bind_params();
     compute_bytes();
+}
+
+template <typename T>
+std::vector<double> Engine<T>::flux(const std::string &e1_group, const std::string &h2_group, const std::vector<double> &x,
+                                    const std::vector<double> &y, const std::vector<double> &z, const std::vector<double> &w,
+                                    const std::vector<double> &freqs)
+{
+    if (freqs.empty()) return {};
+    if ((int)freqs.size() > kMaxFluxFreqs)
+        throw std::runtime_error("flux: at most " + std::to_string(kMaxFluxFreqs) + " frequencies per call");
+    if (x.empty() || y.empty() || z.empty() || w.size() != x.size() * y.size() * z.size())
+        throw std::runtime_error("flux: the weights must cover the x * y * z integration points");
+    // the output grid of a monitor group (the closure's points, dx/2 apart
+    // on the doubled grid) as the reference's interpolant sees it
+    auto grid = [&](const std::string &group, FluxGrid &G) {
+        const DftRequest *req = nullptr;
+        for (auto &r : P_.requests)
+            if (r.group == group) req = &r;
+        if (!req) throw std::runtime_error("flux: no monitor group '" + group + "'");
+        const DftUnit &U = P_.units[req->unit];
+        G = FluxGrid();
+        G.re = dre_[req->unit];
+        G.im = dim_[req->unit];
+        G.npts = U.npoints();
+        for (int a = 0; a < 3; ++a)
+        {
+            G.ld[a] = U.has_local ? U.ldim[a] : 0;
+            G.off[a] = U.has_local ? (U.l1[a] - U.c1[a]) / 2 : 0;
+            G.dim[a] = U.dim[a];
+            const double s0 = U.c1[a] * (P_.dx / 2), s1 = U.c2[a] * (P_.dx / 2);
+            if (U.dim[a] <= 1)
+            {
+                // one point: widened to +-dx/2, the value repeated
+                G.wide[a] = 1;
+                G.n[a] = 2;
+                G.g0[a] = s0 - P_.dx / 2;
+                G.gs[a] = P_.dx;
+            }
+            else
+            {
+                G.n[a] = U.dim[a];
+                G.g0[a] = s0;
+                G.gs[a] = (s1 - s0) / (U.dim[a] - 1);
+            }
+        }
+        for (size_t f = 0; f < freqs.size(); ++f)
+        {
+            auto it = std::lower_bound(U.freqs.begin(), U.freqs.end(), freqs[f]);
+            if (it == U.freqs.end() || *it != freqs[f]) throw std::runtime_error("flux: frequency not registered in '" + group + "'");
+            G.fidx[f] = (int)(it - U.freqs.begin());
+        }
+    };
+    FluxArgs A;
+    grid(e1_group, A.e1);
+    grid(h2_group, A.h2);
+    A.nf = (int)freqs.size();
+    A.n[0] = (int)x.size();
+    A.n[1] = (int)y.size();
+    A.n[2] = (int)z.size();
+    A.x = x.data();
+    A.y = y.data();
+    A.z = z.data();
+    A.w = w.data();
+    std::vector<double> out(freqs.size(), 0.0);
+    be_->flux(A, out.data());
+    ++nlaunch_;
+    return out;
 }
 
 template <typename T>

@@ -79,6 +79,9 @@ struct Backend
     virtual bool any_nonfinite(const float *const *f, int nf, int64_t n) = 0;
     // forgets a reported kernel timeout (after the state was reset)
     virtual void clear_error() {}
+    // out[f] = sum over the integration points of flux_point(A, t, f); the
+    // coordinate and weight arrays of A are host arrays, uploaded here
+    virtual void flux(const FluxArgs &A, double *out) = 0;
     virtual const char *name() const = 0;
     // device time of f() between events on the backend's stream (ms)
     virtual double timed(const std::function<void()> &f) = 0;
@@ -120,6 +123,11 @@ public:
     virtual double bytes_per_step() const = 0;
     // bytes_per_step without the DFT sums (the field pass's share)
     virtual double pass_bytes_per_step() const = 0;
+    // Poynting flux through a flux region per frequency from the E1 / H2
+    // monitor groups (their names), the integration points and weights
+    virtual std::vector<double> flux(const std::string &e1_group, const std::string &h2_group, const std::vector<double> &x,
+                                     const std::vector<double> &y, const std::vector<double> &z, const std::vector<double> &w,
+                                     const std::vector<double> &freqs) = 0;
 };
 
 std::unique_ptr<EngineBase> make_engine(Plan &&plan, Backend *be);

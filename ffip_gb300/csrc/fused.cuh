@@ -1184,15 +1184,17 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         // meets (D/B value: g_inf of the default medium times H)
                         if (dft_h)
                             for (int r = 0; r < RPT; ++r)
-                                for (int p = 0; p < NPT; ++p)
+                                for (int c = 0; c < 3; ++c)
                                 {
-                                    const T hv[3] = {hn0[r][p], hn1[r][p], hn2[r][p]};
-                                    for (int c = 0; c < 3; ++c)
+                                    const Vals<T, NPT> &hv = c == 0 ? hn0[r] : c == 1 ? hn1[r] : hn2[r];
+                                    double v[NPT], vd[NPT];
+#pragma unroll
+                                    for (int p = 0; p < NPT; ++p)
                                     {
-                                        const T vd = PH.g_def * hv[c];
-                                        dft_point<T>(PH.nunits, PH.units, PH.phase, 3 + c, x + p, X.y0 + r0 + r, k, (double)hv[c],
-                                                     (double)vd);
+                                        v[p] = (double)hv[p];
+                                        vd[p] = (double)(PH.g_def * hv[p]);
                                     }
+                                    dft_points<NPT>(PH.nunits, PH.units, PH.phase, 3 + c, x, X.y0 + r0 + r, k, v, vd);
                                 }
                     }
                 };
@@ -1352,15 +1354,17 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         st_outv(&F.eout[1][idx_e + r * sy], ey);
                         st_outv(&F.eout[2][idx_e + r * sy], ez);
                         if (dft_e)
-                            for (int p = 0; p < NPT; ++p)
+                            for (int c = 0; c < 3; ++c)
                             {
-                                const T ev[3] = {ex[p], ey[p], ez[p]};
-                                for (int c = 0; c < 3; ++c)
+                                const Vals<T, NPT> &ev = c == 0 ? ex : c == 1 ? ey : ez;
+                                double v[NPT], vd[NPT];
+#pragma unroll
+                                for (int p = 0; p < NPT; ++p)
                                 {
-                                    const T vd = PE.g_def * ev[c];
-                                    dft_point<T>(PE.nunits, PE.units, PE.phase, c, x + p, X.y0 + r0 + r, k - 1, (double)ev[c],
-                                                 (double)vd);
+                                    v[p] = (double)ev[p];
+                                    vd[p] = (double)(PE.g_def * ev[p]);
                                 }
+                                dft_points<NPT>(PE.nunits, PE.units, PE.phase, c, x, X.y0 + r0 + r, k - 1, v, vd);
                             }
                     }
                 };

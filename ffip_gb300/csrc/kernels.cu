@@ -26,6 +26,11 @@
 #include "engine.hpp"
 #include "fused.cuh"
 
+// the fused pass's CTA jobs heaviest first (DFT sums, material slots)
+#ifndef FFIP_FUSED_HEAVY_FIRST
+#define FFIP_FUSED_HEAVY_FIRST 1
+#endif
+
 namespace ffipg
 {
 namespace
@@ -124,6 +129,40 @@ __global__ void __launch_bounds__(256) k_nonfinite(const __grid_constant__ Nonfi
             bad = bad || !isfinite(a.f[i][t]);
     }
     if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
+}
+
+// flux through a flux region: per block, partial sums per frequency of
+// flux_point over a grid-stride range of integration points (a fixed
+// assignment, so the result does not depend on scheduling), then one block
+// adds the partials in block order
+constexpr int kFluxBlocks = 512;
+__global__ void __launch_bounds__(256) k_flux_partial(const __grid_constant__ FluxArgs A, double *partial)
+{
+    __shared__ double red[256];
+    const int64_t np = (int64_t)A.n[0] * A.n[1] * A.n[2];
+    for (int f = 0; f < A.nf; ++f)
+    {
+        double s = 0;
+        for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < np; t += (int64_t)gridDim.x * blockDim.x)
+            s += flux_point(A, t, f);
+        red[threadIdx.x] = s;
+        __syncthreads();
+        for (int w = 128; w > 0; w >>= 1)
+        {
+            if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) partial[(int64_t)f * gridDim.x + blockIdx.x] = red[0];
+        __syncthreads();
+    }
+}
+__global__ void k_flux_total(const double *partial, int nblocks, int nf, double *out)
+{
+    const int f = threadIdx.x;
+    if (f >= nf) return;
+    double s = 0;
+    for (int b = 0; b < nblocks; ++b) s += partial[(int64_t)f * nblocks + b];
+    out[f] = s;
 }
 
 // one flag per device and field type: the fused kernels' attributes
@@ -535,6 +574,57 @@ public:
                 }
             }
         }
+#if FFIP_FUSED_HEAVY_FIRST
+        // within each instance, the jobs that add DFT sums or update material
+        // slots (several times the work of a plain job) go first, so that the
+        // launch does not end on a few long jobs
+        {
+            std::vector<RowRange> rows[3];
+            for (int c = 0; c < 3; ++c)
+                if (P.slot[c].map)
+                {
+                    rows[c].resize((size_t)P.My * P.Mz);
+                    check(cudaMemcpy(rows[c].data(), P.slot[c].rows, rows[c].size() * sizeof(RowRange), cudaMemcpyDeviceToHost),
+                          "cudaMemcpy D2H");
+                }
+            auto heavy = [&](const int4 &j, int tx) {
+                int w = 0;
+                for (int sd = 0; sd < 2; ++sd)
+                {
+                    const SideParams<T> &S = sd ? p.h : p.e;
+                    for (int u = 0; u < S.nunits; ++u)
+                    {
+                        const DftView &U = S.units[u];
+                        if (U.i0[0] < j.x + tx && U.i0[0] + U.ld[0] > j.x && U.i0[1] < j.y + TY && U.i0[1] + U.ld[1] > j.y &&
+                            U.i0[2] < j.w && U.i0[2] + U.ld[2] > j.z - 1)
+                            w = 2;
+                    }
+                }
+                for (int c = 0; c < 3 && w < 1; ++c)
+                    for (int k = std::max(j.z - 1, 0); k < std::min(j.w, P.Mz) && w < 1 && !rows[c].empty(); ++k)
+                        for (int y = j.y; y < std::min(j.y + TY, P.My); ++y)
+                        {
+                            const RowRange &rr = rows[c][(size_t)k * P.My + y];
+                            if (rr.lo <= rr.hi && rr.lo < j.x + tx && rr.hi >= j.x)
+                            {
+                                w = 1;
+                                break;
+                            }
+                        }
+                return w;
+            };
+            auto order = [&](std::vector<int4> &v, int tx) {
+                std::vector<std::pair<int, size_t>> key(v.size());
+                for (size_t i = 0; i < v.size(); ++i) key[i] = {-heavy(v[i], tx), i};
+                std::stable_sort(key.begin(), key.end());
+                std::vector<int4> o(v.size());
+                for (size_t i = 0; i < v.size(); ++i) o[i] = v[key[i].second];
+                v.swap(o);
+            };
+            order(b, TXP);
+            order(in, TX);
+        }
+#endif
         Jobs J;
         J.nb = (int)b.size();
         J.ni = (int)in.size();
@@ -568,6 +658,45 @@ public:
         if (e)
             throw DeviceTimeout("fused kernel: a wait on its TMA rings or on its CTA's threads timed out; the field "
                                 "state is invalid until ffip_reset");
+    }
+    void flux(const FluxArgs &A0, double *out) override
+    {
+        use();
+        FluxArgs A = A0;
+        std::vector<double *> keep;
+        auto up = [&](const double *h, size_t n) {
+            double *d = nullptr;
+            check(cudaMalloc(&d, n * sizeof(double)), "cudaMalloc");
+            keep.push_back(d);
+            check(cudaMemcpyAsync(d, h, n * sizeof(double), cudaMemcpyHostToDevice, stream_), "cudaMemcpy H2D");
+            return d;
+        };
+        try
+        {
+            A.x = up(A0.x, A0.n[0]);
+            A.y = up(A0.y, A0.n[1]);
+            A.z = up(A0.z, A0.n[2]);
+            A.w = up(A0.w, (size_t)A0.n[0] * A0.n[1] * A0.n[2]);
+            double *partial = nullptr, *dout = nullptr;
+            check(cudaMalloc(&partial, (size_t)kFluxBlocks * A.nf * sizeof(double)), "cudaMalloc");
+            keep.push_back(partial);
+            check(cudaMalloc(&dout, A.nf * sizeof(double)), "cudaMalloc");
+            keep.push_back(dout);
+            k_flux_partial<<<kFluxBlocks, 256, 0, stream_>>>(A, partial);
+            check(cudaGetLastError(), "k_flux_partial launch");
+            k_flux_total<<<1, kMaxFluxFreqs, 0, stream_>>>(partial, kFluxBlocks, A.nf, dout);
+            check(cudaGetLastError(), "k_flux_total launch");
+            check(cudaMemcpyAsync(out, dout, A.nf * sizeof(double), cudaMemcpyDeviceToHost, stream_), "cudaMemcpy D2H");
+            check(cudaStreamSynchronize(stream_), "sync");
+            d2h_bytes += A.nf * sizeof(double);
+        }
+        catch (...)
+        {
+            cudaStreamSynchronize(stream_);
+            for (double *d : keep) cudaFree(d);
+            throw;
+        }
+        for (double *d : keep) cudaFree(d);
     }
     void clear_error() override
     {

@@ -95,26 +95,68 @@ struct SideParams
 };
 
 // ---------------------------------------------------------------------------
-// DFT accumulation of one point's new value into every matching unit
-template <typename T>
-FFIP_HD void dft_point(int nunits, const DftView *units, const double (*phase)[2], int gcomp, int i, int j, int k,
-                       double v, double vd)
+// DFT accumulation of the new values of NPT consecutive x points (i ..
+// i + NPT - 1, row j, plane k) of global component gcomp into every matching
+// unit.  Per chunk of frequencies every load of the running sums is issued
+// before the first store, so that a thread waits for one round trip per
+// chunk instead of one per sum (the arrays may alias as far as the compiler
+// knows); each sum gets the same single multiply-add as one at a time.
+template <int NPT>
+FFIP_HD void dft_points(int nunits, const DftView *units, const double (*phase)[2], int gcomp, int i, int j, int k,
+                        const double (&v)[NPT], const double (&vd)[NPT])
 {
+    constexpr int FC = 8 / NPT;  // frequencies per chunk
     for (int u = 0; u < nunits; ++u)
     {
         const DftView &U = units[u];
         if (U.comp != gcomp) continue;
-        int li = i - U.i0[0], lj = j - U.i0[1], lk = k - U.i0[2];
-        if ((unsigned)li >= (unsigned)U.ld[0] || (unsigned)lj >= (unsigned)U.ld[1] || (unsigned)lk >= (unsigned)U.ld[2]) continue;
-        int64_t l = ((int64_t)lk * U.ld[1] + lj) * U.ld[0] + li;
-        double x = U.is_db ? vd : v;
-        for (int f = 0; f < U.nf; ++f)
+        const int lj = j - U.i0[1], lk = k - U.i0[2], li = i - U.i0[0];
+        if ((unsigned)lj >= (unsigned)U.ld[1] || (unsigned)lk >= (unsigned)U.ld[2]) continue;
+        bool in[NPT];
+        bool any = false;
+        double x[NPT];
+#pragma unroll
+        for (int p = 0; p < NPT; ++p)
         {
-            double cw = phase[U.foff + f][0], sw = phase[U.foff + f][1];
-            U.im[f * U.npts + l] += sw * x;
-            U.re[f * U.npts + l] += cw * x;
+            in[p] = (unsigned)(li + p) < (unsigned)U.ld[0];
+            any = any || in[p];
+            x[p] = U.is_db ? vd[p] : v[p];
+        }
+        if (!any) continue;
+        const int64_t l = ((int64_t)lk * U.ld[1] + lj) * U.ld[0] + li;
+        for (int f0 = 0; f0 < U.nf; f0 += FC)
+        {
+            double re[FC][NPT], im[FC][NPT];
+#pragma unroll
+            for (int f = 0; f < FC; ++f)
+#pragma unroll
+                for (int p = 0; p < NPT; ++p)
+                    if (f0 + f < U.nf && in[p])
+                    {
+                        im[f][p] = U.im[(f0 + f) * U.npts + l + p];
+                        re[f][p] = U.re[(f0 + f) * U.npts + l + p];
+                    }
+#pragma unroll
+            for (int f = 0; f < FC; ++f)
+#pragma unroll
+                for (int p = 0; p < NPT; ++p)
+                    if (f0 + f < U.nf && in[p])
+                    {
+                        const double cw = phase[U.foff + f0 + f][0], sw = phase[U.foff + f0 + f][1];
+                        U.im[(f0 + f) * U.npts + l + p] = im[f][p] + sw * x[p];
+                        U.re[(f0 + f) * U.npts + l + p] = re[f][p] + cw * x[p];
+                    }
         }
     }
+}
+
+// one point
+template <typename T>
+FFIP_HD void dft_point(int nunits, const DftView *units, const double (*phase)[2], int gcomp, int i, int j, int k,
+                       double v, double vd)
+{
+    const double a[1] = {v}, b[1] = {vd};
+    dft_points<1>(nunits, units, phase, gcomp, i, j, k, a, b);
 }
 
 // Compile-time facts of global component GC (0..5 = Ex Ey Ez Hx Hy Hz): its
@@ -470,6 +512,100 @@ FFIP_HD void source_point(const SourceParams<T> &p, int q)
                 U.re[f * U.npts + p.mlin[m]] += p.phase[U.foff + f][0] * x;
             }
         }
+}
+
+// ---------------------------------------------------------------------------
+// Flux through a flux region (Flux_Region.get_values, ffip/simulation.py:
+// 121-160): at every integration point (x_i, y_j, z_k), the E1 and H2 DFT
+// monitors are interpolated linearly over their output grids (the
+// reference's Fields_DFT interpolant, ffip/simulation.py:55-91: an axis of
+// one point is widened to +-dx/2 with the value repeated), and Re(E1 conj(H2))
+// times the point's weight is summed per frequency.
+constexpr int kMaxFluxFreqs = 64;
+struct FluxGrid
+{
+    const double *re, *im;    // the monitor unit's sums [unit frequency][local point]
+    int64_t npts;
+    int ld[3];                // local box dims (points)
+    int off[3];               // local box offset within the output grid (points)
+    int dim[3];               // output grid dims (points)
+    double g0[3], gs[3];      // output grid: coordinate of point i = g0 + i gs (widened axes: 2 points)
+    int n[3];                 // grid points per axis for the interpolation (dim, or 2 where widened)
+    int wide[3];              // axis widened from one point
+    int fidx[kMaxFluxFreqs];  // unit frequency index of each requested frequency
+};
+struct FluxArgs
+{
+    FluxGrid e1, h2;
+    int nf;
+    int n[3];                 // integration points per axis
+    const double *x, *y, *z;  // their coordinates
+    const double *w;          // their weights, [k][j][i]
+};
+
+// scipy's RegularGridInterpolator, linear, along one axis: cell index and
+// the distance into it
+FFIP_HD void flux_axis(const FluxGrid &G, int a, double q, int &i, double &t)
+{
+    const int n = G.n[a];
+    // searchsorted(grid, q, "left") - 1, clipped to [0, n - 2]
+    int lo = 0, hi = n;
+    while (lo < hi)
+    {
+        const int mid = (lo + hi) / 2;
+        if (G.g0[a] + mid * G.gs[a] < q) lo = mid + 1;
+        else hi = mid;
+    }
+    i = lo - 1;
+    if (i < 0) i = 0;
+    if (i > n - 2) i = n - 2;
+    const double gi = G.g0[a] + i * G.gs[a], gj = G.g0[a] + (i + 1) * G.gs[a];
+    t = (q - gi) / (gj - gi);
+}
+
+// value of grid point (ix, iy, iz) of the output grid at unit frequency fi
+// (zero outside the unit's local box, as the output assembly leaves it)
+FFIP_HD void flux_node(const FluxGrid &G, int fi, int ix, int iy, int iz, double &re, double &im)
+{
+    const int p[3] = {G.wide[0] ? 0 : ix, G.wide[1] ? 0 : iy, G.wide[2] ? 0 : iz};
+    const int l0 = p[0] - G.off[0], l1 = p[1] - G.off[1], l2 = p[2] - G.off[2];
+    if (l0 < 0 || l1 < 0 || l2 < 0 || l0 >= G.ld[0] || l1 >= G.ld[1] || l2 >= G.ld[2])
+    {
+        re = im = 0.0;
+        return;
+    }
+    const int64_t l = ((int64_t)l2 * G.ld[1] + l1) * G.ld[0] + l0;
+    re = G.re[fi * G.npts + l];
+    im = G.im[fi * G.npts + l];
+}
+
+FFIP_HD void flux_interp(const FluxGrid &G, int f, double x, double y, double z, double &re, double &im)
+{
+    int i[3];
+    double t[3];
+    flux_axis(G, 0, x, i[0], t[0]);
+    flux_axis(G, 1, y, i[1], t[1]);
+    flux_axis(G, 2, z, i[2], t[2]);
+    re = im = 0.0;
+    for (int c = 0; c < 8; ++c)
+    {
+        const int dx = c & 1, dy = (c >> 1) & 1, dz = (c >> 2) & 1;
+        const double w = (dx ? t[0] : 1 - t[0]) * (dy ? t[1] : 1 - t[1]) * (dz ? t[2] : 1 - t[2]);
+        double r, m;
+        flux_node(G, G.fidx[f], i[0] + dx, i[1] + dy, i[2] + dz, r, m);
+        re += w * r;
+        im += w * m;
+    }
+}
+
+// contribution of integration point t (x fastest) to frequency f
+FFIP_HD double flux_point(const FluxArgs &A, int64_t t, int f)
+{
+    const int i = (int)(t % A.n[0]), j = (int)(t / A.n[0] % A.n[1]), k = (int)(t / ((int64_t)A.n[0] * A.n[1]));
+    double er, ei, hr, hi;
+    flux_interp(A.e1, f, A.x[i], A.y[j], A.z[k], er, ei);
+    flux_interp(A.h2, f, A.x[i], A.y[j], A.z[k], hr, hi);
+    return (er * hr + ei * hi) * A.w[t];  // Re(e1 conj(h2)) * weight
 }
 
 // ---------------------------------------------------------------------------

@@ -99,6 +99,7 @@ class Flux_Region:
         self.center, self.size = center.copy(), size.copy()
         self.frequency = np.sort(np.asarray(frequency))
         self.dx = sim.dx
+        self._sim = sim
         self._e1_dft = sim.add_dft_fields(center=center, size=size, frequency=frequency, field_component=self.e1_str)
         self._h2_dft = sim.add_dft_fields(center=center, size=size, frequency=frequency, field_component=self.h2_str)
 
@@ -151,7 +152,19 @@ class Flux_Region:
         Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
         return X * Y * Z * meas * self.weight
 
-    def get_values(self, scale=1, substract=None, **kwargs):
+    def get_values(self, scale=1, substract=None, device=False, **kwargs):
+        """Flux per frequency.  device=True (rebuild-only): the same sum on the
+        GPU from the monitors of a simulation kept there (run(keep=True)),
+        without copying them back (ffip_flux)."""
+        if device:
+            if substract is not None or kwargs:
+                raise ValueError("the device flux takes neither substract nor interpolation options")
+            kept = getattr(self._sim, "_kept", None)
+            if kept is None:
+                raise RuntimeError("the device flux needs a simulation kept on the device (run(keep=True))")
+            f, z, y, x = self.get_metadata(scale=scale)
+            return kept["sim"].flux(self.e1_dft.group_name, self.h2_dft.group_name, x, y, z, self.get_int_weights(scale=scale),
+                                    self.frequency)
         e1, h2 = self.get_fields(scale=scale, substract=substract, **kwargs)
         flux = np.real(e1 * np.conj(h2)) * self.get_int_weights(scale=scale)
         return np.sum(flux, axis=(1, 2, 3))
@@ -182,10 +195,11 @@ class Flux_Box:
     def get_flux_region(self, direction="x", side="negative"):
         return self.flux_regions[direction_dict[direction] * 2 + (0 if side_dict[side] == -1 else 1)]
 
-    def get_values(self, scale=1, substract=None, **kwargs):
+    def get_values(self, scale=1, substract=None, device=False, **kwargs):
         if substract is not None and not isinstance(substract, Flux_Box):
             raise TypeError("Substract is not an instance of Flux_Box")
-        return sum(r.get_values(scale=scale, substract=substract.flux_regions[i] if substract is not None else None, **kwargs)
+        return sum(r.get_values(scale=scale, substract=substract.flux_regions[i] if substract is not None else None,
+                                device=device, **kwargs)
                    for i, r in enumerate(self.flux_regions))
 
     def get_interpolant(self, scale=1, substract=None, **kwargs):

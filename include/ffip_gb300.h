@@ -132,6 +132,18 @@ int ffip_reset(ffip_sim *sim);
 
 int ffip_get_stats(ffip_sim *sim, ffip_stats *stats);
 
+/* Flux_Region.get_values (ffip/simulation.py:121-160) on the device: the
+ * Poynting flux, the sum over the integration points of Re(E1 conj(H2))
+ * times the point's weight, per frequency, where E1 / H2 are the DFT monitor
+ * groups e1_group / h2_group (output group names) interpolated linearly over
+ * their output grids (the reference's Fields_DFT interpolant,
+ * ffip/simulation.py:55-91).  The points are the grid x[nx] x y[ny] x z[nz];
+ * w[nz][ny][nx] are their weights (the reference's get_int_weights); freqs
+ * must be frequencies of both monitors (at most 64).  flux[nf] receives the
+ * sums; the monitors stay on the device. */
+int ffip_flux(ffip_sim *sim, const char *e1_group, const char *h2_group, const double *x, uint64_t nx, const double *y,
+              uint64_t ny, const double *z, uint64_t nz, const double *w, const double *freqs, uint64_t nf, double *flux);
+
 /* Blocks until all work of the handle has finished. */
 int ffip_sync(ffip_sim *sim);
 

@@ -105,6 +105,16 @@ public:
     }
     bool any_nonfinite(const double *const *f, int nf, int64_t n) override { return any_nonfinite_t(f, nf, n); }
     bool any_nonfinite(const float *const *f, int nf, int64_t n) override { return any_nonfinite_t(f, nf, n); }
+    void flux(const FluxArgs &A, double *out) override
+    {
+        const int64_t np = (int64_t)A.n[0] * A.n[1] * A.n[2];
+        for (int f = 0; f < A.nf; ++f)
+        {
+            double s = 0;
+            for (int64_t t = 0; t < np; ++t) s += flux_point(A, t, f);
+            out[f] = s;
+        }
+    }
     void dft_norm(const double *re, const double *im, int64_t n, double *out) override
     {
         double s = 0;
