@@ -30,6 +30,10 @@
 #ifndef FFIP_FUSED_HEAVY_FIRST
 #define FFIP_FUSED_HEAVY_FIRST 1
 #endif
+// tile columns with material slots (and no DFT unit) go to the CPML instance
+#ifndef FFIP_FUSED_SLOTS_TO_P
+#define FFIP_FUSED_SLOTS_TO_P 1
+#endif
 
 namespace ffipg
 {
@@ -508,9 +512,10 @@ public:
     const Jobs &jobs_for(const FusedParams<T> &p, const FusedLaunch<T> &L, int nbx, int nby, int TX, int TXP, int TY, int KCH)
     {
         const SideParams<T> &P = p.e;
-        char key[160];
-        std::snprintf(key, sizeof key, "%d %d %d %d %d %d %d %d %d %d %p %d", L.xlim, L.ylim, L.kbeg, L.kend, nbx, nby, TX, TXP, TY,
-                      KCH, (const void *)P.pc[0][0], (int)sizeof(T));
+        char key[256];
+        std::snprintf(key, sizeof key, "%d %d %d %d %d %d %d %d %d %d %p %d %p %p %p", L.xlim, L.ylim, L.kbeg, L.kend, nbx, nby, TX,
+                      TXP, TY, KCH, (const void *)P.pc[0][0], (int)sizeof(T), (const void *)P.slot[0].rows,
+                      (const void *)P.slot[1].rows, (const void *)P.slot[2].rows);
         auto it = jobs_.find(key);
         if (it != jobs_.end()) return it->second;
         // CPML flags per position along each axis (either parity)
@@ -554,6 +559,43 @@ public:
         split(L.kbeg, za);
         split(za, zb);
         split(zb, L.kend);
+        // E material slot row ranges (the fused pass updates no H slots
+        // with poles), for the job weights below
+        std::vector<RowRange> rows[3];
+        for (int c = 0; c < 3; ++c)
+            if (P.slot[c].map)
+            {
+                rows[c].resize((size_t)P.My * P.Mz);
+                check(cudaMemcpy(rows[c].data(), P.slot[c].rows, rows[c].size() * sizeof(RowRange), cudaMemcpyDeviceToHost),
+                      "cudaMemcpy D2H");
+            }
+        // 2: a DFT unit meets the job's box, 1: material slots in its rows
+        auto heavy = [&](const int4 &j, int tx) {
+            int w = 0;
+            for (int sd = 0; sd < 2; ++sd)
+            {
+                const SideParams<T> &S = sd ? p.h : p.e;
+                for (int u = 0; u < S.nunits; ++u)
+                {
+                    const DftView &U = S.units[u];
+                    if (U.i0[0] < j.x + tx && U.i0[0] + U.ld[0] > j.x && U.i0[1] < j.y + TY && U.i0[1] + U.ld[1] > j.y &&
+                        U.i0[2] < j.w && U.i0[2] + U.ld[2] > j.z - 1)
+                        w = 2;
+                }
+            }
+            for (int c = 0; c < 3 && w < 1; ++c)
+                for (int k = std::max(j.z - 1, 0); k < std::min(j.w, P.Mz) && w < 1 && !rows[c].empty(); ++k)
+                    for (int y = j.y; y < std::min(j.y + TY, P.My); ++y)
+                    {
+                        const RowRange &rr = rows[c][(size_t)k * P.My + y];
+                        if (rr.lo <= rr.hi && rr.lo < j.x + tx && rr.hi >= j.x)
+                        {
+                            w = 1;
+                            break;
+                        }
+                    }
+            return w;
+        };
         std::vector<int4> b, in;
         for (auto &ch : chunks)
         {
@@ -566,8 +608,13 @@ public:
                 {
                     const int x0 = kXFirst + bx * TX;
                     const bool xin = !any(0, x0 - 1, x0 + TX - 1);
-                    if (zin && yin && xin)
-                        in.push_back(make_int4(x0, y0, ch.first, ch.second));
+                    // a column with material slots (and no DFT unit) runs as
+                    // narrower jobs of the CPML instance as well: its one
+                    // point per thread and more CTAs per SM hide the latency
+                    // of the slot loads better
+                    const int4 j = make_int4(x0, y0, ch.first, ch.second);
+                    if (zin && yin && xin && !(FFIP_FUSED_SLOTS_TO_P && heavy(j, TX) == 1))
+                        in.push_back(j);
                     else  // a column that touches a CPML point: TX / TXP jobs of the CPML instance
                         for (int h = 0; h < TX / TXP; ++h)
                             if (x0 + h * TXP < L.xlim) b.push_back(make_int4(x0 + h * TXP, y0, ch.first, ch.second));
@@ -578,52 +625,16 @@ public:
         // within each instance, the jobs that add DFT sums or update material
         // slots (several times the work of a plain job) go first, so that the
         // launch does not end on a few long jobs
-        {
-            std::vector<RowRange> rows[3];
-            for (int c = 0; c < 3; ++c)
-                if (P.slot[c].map)
-                {
-                    rows[c].resize((size_t)P.My * P.Mz);
-                    check(cudaMemcpy(rows[c].data(), P.slot[c].rows, rows[c].size() * sizeof(RowRange), cudaMemcpyDeviceToHost),
-                          "cudaMemcpy D2H");
-                }
-            auto heavy = [&](const int4 &j, int tx) {
-                int w = 0;
-                for (int sd = 0; sd < 2; ++sd)
-                {
-                    const SideParams<T> &S = sd ? p.h : p.e;
-                    for (int u = 0; u < S.nunits; ++u)
-                    {
-                        const DftView &U = S.units[u];
-                        if (U.i0[0] < j.x + tx && U.i0[0] + U.ld[0] > j.x && U.i0[1] < j.y + TY && U.i0[1] + U.ld[1] > j.y &&
-                            U.i0[2] < j.w && U.i0[2] + U.ld[2] > j.z - 1)
-                            w = 2;
-                    }
-                }
-                for (int c = 0; c < 3 && w < 1; ++c)
-                    for (int k = std::max(j.z - 1, 0); k < std::min(j.w, P.Mz) && w < 1 && !rows[c].empty(); ++k)
-                        for (int y = j.y; y < std::min(j.y + TY, P.My); ++y)
-                        {
-                            const RowRange &rr = rows[c][(size_t)k * P.My + y];
-                            if (rr.lo <= rr.hi && rr.lo < j.x + tx && rr.hi >= j.x)
-                            {
-                                w = 1;
-                                break;
-                            }
-                        }
-                return w;
-            };
-            auto order = [&](std::vector<int4> &v, int tx) {
-                std::vector<std::pair<int, size_t>> key(v.size());
-                for (size_t i = 0; i < v.size(); ++i) key[i] = {-heavy(v[i], tx), i};
-                std::stable_sort(key.begin(), key.end());
-                std::vector<int4> o(v.size());
-                for (size_t i = 0; i < v.size(); ++i) o[i] = v[key[i].second];
-                v.swap(o);
-            };
-            order(b, TXP);
-            order(in, TX);
-        }
+        auto order = [&](std::vector<int4> &v, int tx) {
+            std::vector<std::pair<int, size_t>> key(v.size());
+            for (size_t i = 0; i < v.size(); ++i) key[i] = {-heavy(v[i], tx), i};
+            std::stable_sort(key.begin(), key.end());
+            std::vector<int4> o(v.size());
+            for (size_t i = 0; i < v.size(); ++i) o[i] = v[key[i].second];
+            v.swap(o);
+        };
+        order(b, TXP);
+        order(in, TX);
 #endif
         Jobs J;
         J.nb = (int)b.size();
