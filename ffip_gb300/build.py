@@ -15,7 +15,10 @@ LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libffip_gb300.so")
 CLI = os.path.join(LIBDIR, "run_sim_json")
 
-CUDA_SOURCES = ["kernels.cu", "adjoint.cu", "surrogate.cu"]
+CUDA_SOURCES = ["kernels.cu", "adjoint.cu", "surrogate.cu", "raster.cu"]
+# raster.cu rounds its double arithmetic like the host's media code (no
+# contraction into fused multiply-adds), so that both give the same tables
+CUDA_FLAGS = {"raster.cu": ["-fmad=false"]}
 CXX_SOURCES = ["plan.cpp", "engine.cpp", "capi.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -55,11 +58,11 @@ def build(force: bool = False, verbose: bool = False, defines=(), libdir: str | 
         o = os.path.join(bdir, s + ".o")
         objs.append(o)
         jobs.append([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-                     "-Xptxas", "-warn-spills", *dflags, *inc, "-c", os.path.join(CSRC, s), "-o", o])
+                     "-Xptxas", "-warn-spills", *CUDA_FLAGS.get(s, []), *dflags, *inc, "-c", os.path.join(CSRC, s), "-o", o])
     for s in CXX_SOURCES:
         o = os.path.join(bdir, s + ".o")
         objs.append(o)
-        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", *inc,
+        jobs.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function", *inc,
                      "-I", "/usr/local/cuda/include", "-c", os.path.join(CSRC, s), "-o", o])
     cli_obj = os.path.join(bdir, "run_sim_json.cpp.o")
     jobs.append(["g++", "-O2", "-std=c++17", "-Wall", *inc, "-c", os.path.join(CSRC, "run_sim_json.cpp"), "-o", cli_obj])

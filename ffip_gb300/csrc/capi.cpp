@@ -349,6 +349,16 @@ int ffip_flux(ffip_sim *sim, const char *e1_group, const char *h2_group, const d
     });
 }
 
+int ffip_media_info(ffip_sim *sim, uint64_t checksum[6], int32_t *device)
+{
+    return guard([&]() -> int {
+        if (!sim || !checksum || !device) return fail(FFIP_ERR_INVALID, "null argument");
+        sim->eng->media_checksum(checksum);
+        *device = sim->eng->device_media() ? 1 : 0;
+        return FFIP_OK;
+    });
+}
+
 int ffip_transpose_noalloc(const double *gx, uint64_t nx, const double *gy, uint64_t ny, const double *gz, uint64_t nz,
                            const double *pt, uint64_t npts, double *out)
 {

@@ -62,6 +62,8 @@ public:
     void set_source_data(const std::map<std::string, std::vector<double>> &data) override;
     double bytes_per_step() const override { return bytes_per_step_; }
     double pass_bytes_per_step() const override { return pass_bytes_per_step_; }
+    void media_checksum(uint64_t out[6]) override;
+    bool device_media() const override { return device_media_; }
     std::vector<double> flux(const std::string &e1_group, const std::string &h2_group, const std::vector<double> &x,
                              const std::vector<double> &y, const std::vector<double> &z, const std::vector<double> &w,
                              const std::vector<double> &freqs) override;
@@ -93,6 +95,9 @@ private:
     int64_t scratch_n_{0};
     double bytes_per_step_{0};
     double pass_bytes_per_step_{0};
+    bool device_media_{false};   // media rasterised by the backend
+    int64_t pole_sum_[6]{};      // active poles summed over each component's slots
+    bool comp_poles_[6]{};       // a component has slots with poles
 
     // allocation lifetimes: with the engine, until the media change, until
     // the sources change
@@ -123,7 +128,10 @@ private:
     }
 
     void init();
+    void media();
     void init_media();
+    void init_media_device();
+    void upload_pole_tables();
     void init_sources();
     void init_dft();
     void init_ghosts();
@@ -162,11 +170,14 @@ void Engine<T>::init()
             pml_c_[a][q] = upload(c);
             pml_ik_[a][q] = upload(ik);
         }
+    // the media: slot tables on the device (rasterised there, or uploaded
+    // from the host's rasterisation)
+    media();
     // fused pass eligibility (None boundaries everywhere, no magnetic poles)
     bool none_bc = true;
     for (int a = 0; a < 3; ++a) none_bc = none_bc && P_.bc[a][0] == BC_NONE && P_.bc[a][1] == BC_NONE;
     bool mag_poles = false;
-    for (int c = 3; c < 6; ++c) mag_poles = mag_poles || P_.slots[c].any_poles;
+    for (int c = 3; c < 6; ++c) mag_poles = mag_poles || comp_poles_[c];
     const bool eligible = none_bc && !mag_poles && be_->has_fused();
     if (P_.engine == "fused" && !eligible)
         throw std::runtime_error("engine \"fused\" requested but the fused pass needs None boundaries on every face, no magnetic poles and a CUDA backend");
@@ -192,12 +203,119 @@ void Engine<T>::init()
                 if (fused_ && c >= 3) psih_b_[c - 3][s] = dalloc<T>(cells);
             }
         }
-    init_media();
     init_dft();
     init_sources();
     init_ghosts();
     bind_params();
     compute_bytes();
+}
+
+template <typename T>
+void Engine<T>::media()
+{
+    if (P_.rasterize == "device" && !be_->can_rasterize()) throw std::runtime_error("rasterize \"device\": the backend cannot");
+    if (P_.rasterize == "device" || (P_.rasterize == "auto" && be_->can_rasterize()))
+    {
+        try
+        {
+            init_media_device();
+            return;
+        }
+        catch (const std::runtime_error &e)
+        {
+            // a geometry the device rasterisation does not cover ("auto"
+            // falls back to the host)
+            if (P_.rasterize == "device" || std::string(e.what()).rfind("device rasterisation:", 0) != 0) throw;
+        }
+    }
+    if (P_.rasterize != "host") rasterize_media(P_);
+    init_media();
+}
+
+template <typename T>
+void Engine<T>::init_media_device()
+{
+    for (void *p : slot_allocs_) be_->release(p);
+    slot_allocs_.clear();
+    for (int side = 0; side < 2; ++side)
+    {
+        P_.groups[side].clear();
+        P_.group_index[side].clear();
+    }
+    for (int c = 0; c < 6; ++c) P_.slots[c] = SlotList();
+    RasterComp out[6];
+    std::vector<PoleGroup> groups[2];
+    be_->rasterize(P_, sizeof(T) == 4, [this](size_t bytes) { return (void *)dalloc<uint8_t>(bytes, kMedia); }, out, groups);
+    for (int side = 0; side < 2; ++side)
+    {
+        P_.groups[side] = groups[side];
+        for (size_t g = 0; g < groups[side].size(); ++g) P_.group_index[side][groups[side][g].pool] = (int)g;
+    }
+    for (int c = 0; c < 6; ++c)
+    {
+        const RasterComp &R = out[c];
+        DevSlots<T> &D = slots_[c];
+        D = DevSlots<T>();
+        D.n = R.n;
+        D.stride = R.stride;
+        D.poles = R.stride > 0;
+        pole_sum_[c] = R.pole_sum;
+        comp_poles_[c] = D.poles;
+        if (!D.n) continue;
+        D.map = R.map;
+        D.rows = R.rows;
+        D.g = (T *)R.g;
+        D.coef = (T *)R.coef;
+        D.inv = (T *)R.inv;
+        D.group = R.group;
+        D.rec = (SlotRec<T> *)R.rec;
+        if (D.poles)
+        {
+            if (c >= 3) D.A = dalloc<T>(D.n, kMedia);  // H sources are applied before the H update
+            D.amp = (T *)R.amp;
+            D.P = dalloc<T>((size_t)D.stride * D.n, kMedia);
+            D.P1 = dalloc<T>((size_t)D.stride * D.n, kMedia);
+        }
+    }
+    upload_pole_tables();
+    device_media_ = true;
+}
+
+template <typename T>
+void Engine<T>::media_checksum(uint64_t out[6])
+{
+    // FNV-1a over the tables' bytes, copied back from the device
+    auto fnv = [](uint64_t h, const void *p, size_t n) {
+        const unsigned char *b = (const unsigned char *)p;
+        for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+        return h;
+    };
+    be_->sync();
+    for (int c = 0; c < 6; ++c)
+    {
+        const DevSlots<T> &D = slots_[c];
+        uint64_t h = 1469598103934665603ull;
+        h = fnv(h, &D.n, sizeof D.n);
+        h = fnv(h, &D.stride, sizeof D.stride);
+        auto add = [&](const void *dev, size_t bytes) {
+            if (!dev || !bytes) return;
+            std::vector<unsigned char> buf(bytes);
+            be_->d2h(buf.data(), dev, bytes);
+            h = fnv(h, buf.data(), bytes);
+        };
+        if (D.n)
+        {
+            add(D.map, (size_t)P_.cells() * sizeof(int));
+            add(D.rows, (size_t)P_.M[1] * P_.M[2] * sizeof(RowRange));
+            add(D.g, D.n * sizeof(T));
+            add(D.coef, D.n * sizeof(T));
+            add(D.inv, D.n * sizeof(T));
+            add(D.group, D.n);
+            add(D.rec, D.n * sizeof(SlotRec<T>));
+            add(D.amp, (size_t)D.stride * D.n * sizeof(T));
+        }
+        out[c] = h;
+    }
 }
 
 template <typename T>
@@ -328,6 +446,21 @@ void Engine<T>::init_media()
             D.P1 = dalloc<T>(amp.size(), kMedia);
         }
     }
+    for (int c = 0; c < 6; ++c)
+    {
+        const SlotList &L = P_.slots[c];
+        int64_t ps = 0;
+        for (size_t q = 0; q < L.group.size(); ++q) ps += (int64_t)P_.groups[c / 3][L.group[q]].pool.size();
+        pole_sum_[c] = ps;
+        comp_poles_[c] = L.any_poles;
+    }
+    upload_pole_tables();
+    device_media_ = false;
+}
+
+template <typename T>
+void Engine<T>::upload_pole_tables()
+{
     for (int side = 0; side < 2; ++side)
     {
         const auto &G = P_.groups[side];
@@ -643,13 +776,7 @@ void Engine<T>::compute_bytes()
                     if (a2 != a) other *= n[a2];
                 b += 2 * s * (double)(cnt * other);
             }
-        const SlotList &L = P_.slots[c];
-        const int side = c < 3 ? 0 : 1;
-        for (size_t q = 0; q < L.group.size(); ++q)
-        {
-            int np = (int)P_.groups[side][L.group[q]].pool.size();
-            if (np) b += s * 4 * np;
-        }
+        b += s * 4 * (double)pole_sum_[c];
     }
     pass_bytes_per_step_ = b;
     for (auto &U : P_.units) b += 32.0 * (double)U.npoints() * (double)U.freqs.size();
@@ -1012,11 +1139,16 @@ void Engine<T>::set_density(const std::string &dataset, const double *rho, uint6
         }
     if (!found) throw std::runtime_error("no density box uses dataset '" + dataset + "'");
     be_->sync();
-    rasterize_media(P_);
+    // rasterised again where the handle rasterised first
+    if (device_media_) init_media_device();
+    else
+    {
+        rasterize_media(P_);
+        init_media();
+    }
     bool mag_poles = false;
-    for (int c = 3; c < 6; ++c) mag_poles = mag_poles || P_.slots[c].any_poles;
+    for (int c = 3; c < 6; ++c) mag_poles = mag_poles || comp_poles_[c];
     if (fused_ && mag_poles) throw std::runtime_error("the new density adds magnetic poles, which the fused pass does not support");
-    init_media();
     reset();
     compute_bytes();
 }

@@ -49,6 +49,20 @@ struct Diverged : std::runtime_error
     using std::runtime_error::runtime_error;
 };
 
+// Material tables of one component built on the device (Backend::rasterize):
+// the arrays init_media uploads from a host SlotList, in device memory from
+// the engine's allocator; g, coef, inv, rec and amp hold the field type
+struct RasterComp
+{
+    int64_t n{0};         // slots
+    int stride{0};        // most active poles of one slot
+    int64_t pole_sum{0};  // active poles summed over the slots
+    int *map{nullptr};
+    RowRange *rows{nullptr};
+    void *g{nullptr}, *coef{nullptr}, *inv{nullptr}, *rec{nullptr}, *amp{nullptr};
+    uint8_t *group{nullptr};
+};
+
 struct Backend
 {
     virtual ~Backend() {}
@@ -82,6 +96,18 @@ struct Backend
     // out[f] = sum over the integration points of flux_point(A, t, f); the
     // coordinate and weight arrays of A are host arrays, uploaded here
     virtual void flux(const FluxArgs &A, double *out) = 0;
+    // rasterises the media of `plan` (geometry list, default medium,
+    // susceptibility pools) on the device: the slot tables of the six
+    // components (field type float when fp32) in memory from alloc, and the
+    // pole groups of both sides numbered by first appearance, as
+    // rasterize_media numbers them
+    virtual bool can_rasterize() const { return false; }
+    virtual void rasterize(const Plan &plan, bool fp32, const std::function<void *(size_t)> &alloc, RasterComp out[6],
+                           std::vector<PoleGroup> groups[2])
+    {
+        (void)plan, (void)fp32, (void)alloc, (void)out, (void)groups;
+        throw std::runtime_error("this backend does not rasterise media");
+    }
     virtual const char *name() const = 0;
     // device time of f() between events on the backend's stream (ms)
     virtual double timed(const std::function<void()> &f) = 0;
@@ -125,6 +151,12 @@ public:
     virtual double pass_bytes_per_step() const = 0;
     // Poynting flux through a flux region per frequency from the E1 / H2
     // monitor groups (their names), the integration points and weights
+    // FNV-1a hash of each component's device material tables (slot count,
+    // pole stride, slot map, row ranges, g_inf, dt/g_inf, 1/g_inf, group,
+    // packed record, amplitudes): equal hashes mean equal tables
+    virtual void media_checksum(uint64_t out[6]) = 0;
+    // whether the media were rasterised on the device
+    virtual bool device_media() const = 0;
     virtual std::vector<double> flux(const std::string &e1_group, const std::string &h2_group, const std::vector<double> &x,
                                      const std::vector<double> &y, const std::vector<double> &z, const std::vector<double> &w,
                                      const std::vector<double> &freqs) = 0;

@@ -1194,7 +1194,13 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                         v[p] = (double)hv[p];
                                         vd[p] = (double)(PH.g_def * hv[p]);
                                     }
-                                    dft_points<NPT>(PH.nunits, PH.units, PH.phase, 3 + c, x, X.y0 + r0 + r, k, v, vd);
+                                    // (the CPML instance adds its few such sums one at a
+                                    // time: no call from its loop)
+                                    if constexpr (PML)
+                                        for (int p = 0; p < NPT; ++p)
+                                            dft_point<T>(PH.nunits, PH.units, PH.phase, 3 + c, x + p, X.y0 + r0 + r, k, v[p], vd[p]);
+                                    else
+                                        dft_points<NPT>(PH.nunits, PH.units, PH.phase, 3 + c, x, X.y0 + r0 + r, k, v, vd);
                                 }
                     }
                 };
@@ -1364,7 +1370,11 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                     v[p] = (double)ev[p];
                                     vd[p] = (double)(PE.g_def * ev[p]);
                                 }
-                                dft_points<NPT>(PE.nunits, PE.units, PE.phase, c, x, X.y0 + r0 + r, k - 1, v, vd);
+                                if constexpr (PML)
+                                    for (int p = 0; p < NPT; ++p)
+                                        dft_point<T>(PE.nunits, PE.units, PE.phase, c, x + p, X.y0 + r0 + r, k - 1, v[p], vd[p]);
+                                else
+                                    dft_points<NPT>(PE.nunits, PE.units, PE.phase, c, x, X.y0 + r0 + r, k - 1, v, vd);
                             }
                     }
                 };

@@ -26,6 +26,14 @@
 #include "engine.hpp"
 #include "fused.cuh"
 
+namespace ffipg
+{
+// The device rasterisation of the media (raster.cu), on stream st; returns
+// with the stream drained
+void raster_media(const Plan &p, bool fp32, const std::function<void *(size_t)> &alloc, RasterComp out[6],
+                  std::vector<PoleGroup> groups[2], cudaStream_t st);
+} // namespace ffipg
+
 // the fused pass's CTA jobs heaviest first (DFT sums, material slots)
 #ifndef FFIP_FUSED_HEAVY_FIRST
 #define FFIP_FUSED_HEAVY_FIRST 1
@@ -708,6 +716,13 @@ public:
             throw;
         }
         for (double *d : keep) cudaFree(d);
+    }
+    bool can_rasterize() const override { return true; }
+    void rasterize(const Plan &plan, bool fp32, const std::function<void *(size_t)> &alloc, RasterComp out[6],
+                   std::vector<PoleGroup> groups[2]) override
+    {
+        use();
+        raster_media(plan, fp32, alloc, out, groups, stream_);
     }
     void clear_error() override
     {

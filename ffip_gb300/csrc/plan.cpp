@@ -626,6 +626,26 @@ void set_fields_output(Plan &p, const Json &outs)
 }
 } // namespace
 
+bool geometry_index_range(const Plan &p, const Geometry &geo, int c, int r0[3], int r1[3])
+{
+    // the component's points within the geometry's bounding box, one point of
+    // margin (the strict inside test decides)
+    double blo[3], bhi[3];
+    geo.bbox(blo, bhi);
+    bool empty = false;
+    for (int a = 0; a < 3; ++a)
+    {
+        int par = comp_parity(c, a);
+        int cl = (int)std::floor(blo[a]) - 1, ch = (int)std::ceil(bhi[a]) + 1;
+        if ((cl & 1) != par) ++cl;
+        if ((ch & 1) != par) --ch;
+        r0[a] = std::max(p.index_of(a, cl), p.vlo[c][a]);
+        r1[a] = std::min(p.index_of(a, ch), p.vhi[c][a]);
+        if (r0[a] > r1[a]) empty = true;
+    }
+    return !empty;
+}
+
 void rasterize_media(Plan &p)
 {
     // Structure::set_materials_from_geometry with No_Average,
@@ -658,21 +678,8 @@ void rasterize_media(Plan &p)
         std::vector<std::pair<uint64_t, int>> list;
         for (size_t g = 0; g < p.geoms.size(); ++g)
         {
-            double blo[3], bhi[3];
-            p.geoms[g].bbox(blo, bhi);
             int r0[3], r1[3];
-            bool empty = false;
-            for (int a = 0; a < 3; ++a)
-            {
-                int par = comp_parity(c, a);
-                int cl = (int)std::floor(blo[a]) - 1, ch = (int)std::ceil(bhi[a]) + 1;
-                if ((cl & 1) != par) ++cl;
-                if ((ch & 1) != par) --ch;
-                r0[a] = std::max(p.index_of(a, cl), p.vlo[c][a]);
-                r1[a] = std::min(p.index_of(a, ch), p.vhi[c][a]);
-                if (r0[a] > r1[a]) empty = true;
-            }
-            if (empty) continue;
+            if (!geometry_index_range(p, p.geoms[g], c, r0, r1)) continue;
             for (int k = r0[2]; k <= r1[2]; ++k)
                 for (int j = r0[1]; j <= r1[1]; ++j)
                     for (int i = r0[0]; i <= r1[0]; ++i)
@@ -929,7 +936,12 @@ void build_plan(const Json &cfg, const std::map<std::string, Dataset> &ds, Plan 
     p.default_medium = to_pool(p, bg);
     p.g_default[0] = p.default_medium.epsilon;
     p.g_default[1] = p.default_medium.mu;
-    rasterize_media(p);
+    // media on the host here unless the engine's backend rasterises them on
+    // the device ("rasterize": "auto" / "device")
+    p.rasterize = cfg.str("rasterize", "auto");
+    if (p.rasterize != "auto" && p.rasterize != "host" && p.rasterize != "device")
+        throw std::runtime_error("rasterize must be \"auto\", \"host\" or \"device\"");
+    if (p.rasterize == "host") rasterize_media(p);
     // geometry info request, src/simulation.cpp:190-233 (coordinates pass
     // through a std::vector<int> there, i.e. they are truncated toward zero)
     if (cfg.has("geometry info request"))

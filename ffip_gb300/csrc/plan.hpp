@@ -161,6 +161,10 @@ struct Plan
     int vlo[6][3], vhi[6][3];  // valid index range per component per axis
     bool precision_fp32{false};
     std::string engine{"auto"};
+    // where the media are rasterised: "host" (build_plan / rasterize_media),
+    // "device" (the engine's backend; an error if it cannot), "auto" (the
+    // backend if it can, else the host)
+    std::string rasterize{"auto"};
     int64_t divergence_check{4096};  // steps between checks for non-finite fields (0: never)
     uint64_t fused_wait_ns{2000000000ull};
     bool fused_stall_test{false};
@@ -217,6 +221,11 @@ void build_plan(const Json &cfg, const std::map<std::string, Dataset> &datasets,
 
 // Rebuilds the material slots (after a density dataset changed).
 void rasterize_media(Plan &plan);
+
+// Index box [r0, r1] (per axis) of component c's points that may lie inside
+// geo: its bounding box with one point of margin, clipped to the component's
+// valid range; false if empty.
+bool geometry_index_range(const Plan &p, const Geometry &geo, int c, int r0[3], int r1[3]);
 
 // Rebuilds the dipole lists from sources_cfg and source_data (after an
 // inhomogeneous source's amplitude/phase datasets changed).

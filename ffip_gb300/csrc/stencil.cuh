@@ -23,8 +23,12 @@
 
 #if defined(__CUDACC__)
 #define FFIP_HD __host__ __device__ __forceinline__
+#define FFIP_HD_CALL __host__ __device__ __noinline__
+#define FFIP_UNROLL _Pragma("unroll")
 #else
 #define FFIP_HD inline
+#define FFIP_HD_CALL inline
+#define FFIP_UNROLL
 #endif
 
 namespace ffipg
@@ -95,17 +99,44 @@ struct SideParams
 };
 
 // ---------------------------------------------------------------------------
-// DFT accumulation of the new values of NPT consecutive x points (i ..
-// i + NPT - 1, row j, plane k) of global component gcomp into every matching
-// unit.  Per chunk of frequencies every load of the running sums is issued
-// before the first store, so that a thread waits for one round trip per
-// chunk instead of one per sum (the arrays may alias as far as the compiler
-// knows); each sum gets the same single multiply-add as one at a time.
-template <int NPT>
-FFIP_HD void dft_points(int nunits, const DftView *units, const double (*phase)[2], int gcomp, int i, int j, int k,
-                        const double (&v)[NPT], const double (&vd)[NPT])
+// DFT accumulation of one point's new value into every matching unit
+template <typename T>
+FFIP_HD void dft_point(int nunits, const DftView *units, const double (*phase)[2], int gcomp, int i, int j, int k,
+                       double v, double vd)
 {
-    constexpr int FC = 8 / NPT;  // frequencies per chunk
+    for (int u = 0; u < nunits; ++u)
+    {
+        const DftView &U = units[u];
+        if (U.comp != gcomp) continue;
+        int li = i - U.i0[0], lj = j - U.i0[1], lk = k - U.i0[2];
+        if ((unsigned)li >= (unsigned)U.ld[0] || (unsigned)lj >= (unsigned)U.ld[1] || (unsigned)lk >= (unsigned)U.ld[2]) continue;
+        int64_t l = ((int64_t)lk * U.ld[1] + lj) * U.ld[0] + li;
+        double x = U.is_db ? vd : v;
+        for (int f = 0; f < U.nf; ++f)
+        {
+            double cw = phase[U.foff + f][0], sw = phase[U.foff + f][1];
+            U.im[f * U.npts + l] += sw * x;
+            U.re[f * U.npts + l] += cw * x;
+        }
+    }
+}
+
+// The same for the new values of NPT consecutive x points (i .. i + NPT - 1,
+// row j, plane k), as a called function (the plain paths of the fused pass
+// call it for tile planes that a unit meets; kept out of line so that its
+// registers do not count against the pass's loop).  Per chunk of FC
+// frequencies every load of the running sums is issued before the first
+// store, so that a thread waits for one round trip per chunk instead of one
+// per sum (the arrays may alias as far as the compiler knows); each sum gets
+// the same single multiply-add as in dft_point.
+#ifndef FFIP_DFT_CHUNK
+#define FFIP_DFT_CHUNK 8
+#endif
+template <int NPT>
+FFIP_HD_CALL void dft_points(int nunits, const DftView *units, const double (*phase)[2], int gcomp, int i, int j, int k,
+                             const double *v, const double *vd)
+{
+    constexpr int FC = FFIP_DFT_CHUNK / NPT;
     for (int u = 0; u < nunits; ++u)
     {
         const DftView &U = units[u];
@@ -115,7 +146,7 @@ FFIP_HD void dft_points(int nunits, const DftView *units, const double (*phase)[
         bool in[NPT];
         bool any = false;
         double x[NPT];
-#pragma unroll
+        FFIP_UNROLL
         for (int p = 0; p < NPT; ++p)
         {
             in[p] = (unsigned)(li + p) < (unsigned)U.ld[0];
@@ -127,18 +158,18 @@ FFIP_HD void dft_points(int nunits, const DftView *units, const double (*phase)[
         for (int f0 = 0; f0 < U.nf; f0 += FC)
         {
             double re[FC][NPT], im[FC][NPT];
-#pragma unroll
+            FFIP_UNROLL
             for (int f = 0; f < FC; ++f)
-#pragma unroll
+                FFIP_UNROLL
                 for (int p = 0; p < NPT; ++p)
                     if (f0 + f < U.nf && in[p])
                     {
                         im[f][p] = U.im[(f0 + f) * U.npts + l + p];
                         re[f][p] = U.re[(f0 + f) * U.npts + l + p];
                     }
-#pragma unroll
+            FFIP_UNROLL
             for (int f = 0; f < FC; ++f)
-#pragma unroll
+                FFIP_UNROLL
                 for (int p = 0; p < NPT; ++p)
                     if (f0 + f < U.nf && in[p])
                     {
@@ -148,15 +179,6 @@ FFIP_HD void dft_points(int nunits, const DftView *units, const double (*phase)[
                     }
         }
     }
-}
-
-// one point
-template <typename T>
-FFIP_HD void dft_point(int nunits, const DftView *units, const double (*phase)[2], int gcomp, int i, int j, int k,
-                       double v, double vd)
-{
-    const double a[1] = {v}, b[1] = {vd};
-    dft_points<1>(nunits, units, phase, gcomp, i, j, k, a, b);
 }
 
 // Compile-time facts of global component GC (0..5 = Ex Ey Ez Hx Hy Hz): its

@@ -36,7 +36,7 @@ class Stats(ctypes.Structure):
 EXPORTS = ["ffip_create", "ffip_step", "ffip_step_timed", "ffip_step_timed_pass", "ffip_run", "ffip_output_count",
            "ffip_output_group", "ffip_output_array", "ffip_set_density", "ffip_reset", "ffip_get_stats", "ffip_sync",
            "ffip_stream", "ffip_destroy", "ffip_last_error", "ffip_transpose", "ffip_sensitivity", "ffip_transpose_noalloc",
-           "ffip_set_source_data", "ffip_to_convolve", "ffip_check_inside", "ffip_flux"]
+           "ffip_set_source_data", "ffip_to_convolve", "ffip_check_inside", "ffip_flux", "ffip_media_info"]
 
 
 def _declare(lib):
@@ -62,6 +62,7 @@ def _declare(lib):
     lib.ffip_transpose_noalloc.argtypes = [D, U64, D, U64, D, U64, D, U64, D]
     lib.ffip_to_convolve.argtypes = [D, U64, U64, D, U64, U64, D, ctypes.c_int]
     lib.ffip_check_inside.argtypes = [D, U64, D, U64, ctypes.POINTER(ctypes.c_uint8)]
+    lib.ffip_media_info.argtypes = [P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_int32)]
     lib.ffip_flux.argtypes = [P, ctypes.c_char_p, ctypes.c_char_p, D, U64, D, U64, D, U64, D, D, U64, D]
     lib.ffip_sensitivity.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double, D, D, D, D, U64,
                                      D, U64, D, U64, D, U64, D]
@@ -172,6 +173,14 @@ class NativeSim:
         self._check(self.lib.ffip_flux(self.h, e1_group.encode(), h2_group.encode(), _dptr(x), x.size, _dptr(y), y.size,
                                        _dptr(z), z.size, _dptr(w), _dptr(f), f.size, _dptr(out)))
         return out
+
+    def media_info(self):
+        """(per-component hashes of the device material tables, whether the
+        media were rasterised on the GPU)"""
+        cs = (ctypes.c_uint64 * 6)()
+        dev = ctypes.c_int32()
+        self._check(self.lib.ffip_media_info(self.h, cs, ctypes.byref(dev)))
+        return [int(v) for v in cs], bool(dev.value)
 
     def stream(self) -> int:
         return self.lib.ffip_stream(self.h) or 0

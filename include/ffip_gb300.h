@@ -144,6 +144,17 @@ int ffip_get_stats(ffip_sim *sim, ffip_stats *stats);
 int ffip_flux(ffip_sim *sim, const char *e1_group, const char *h2_group, const double *x, uint64_t nx, const double *y,
               uint64_t ny, const double *z, uint64_t nz, const double *w, const double *freqs, uint64_t nf, double *flux);
 
+/* The handle's material tables: an FNV-1a hash per component of the slot
+ * map, row ranges, g_inf, dt/g_inf, 1/g_inf, pole group, packed record and
+ * pole amplitudes as they sit on the device (equal hashes: equal tables),
+ * and *device = 1 when the media were rasterised on the GPU (config key
+ * "rasterize": "auto" (default: on the GPU where the geometry allows),
+ * "device" or "host"; ffip_set_density rasterises again where the handle
+ * did first).  The rasterisation follows Structure::set_materials_from_
+ * geometry and the density boxes' get_medium (src/structure.cpp:155-249,
+ * src/geometry.cpp:49-107); no reference interface reads the tables back. */
+int ffip_media_info(ffip_sim *sim, uint64_t checksum[6], int32_t *device);
+
 /* Blocks until all work of the handle has finished. */
 int ffip_sync(ffip_sim *sim);
 

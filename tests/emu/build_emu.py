@@ -18,7 +18,7 @@ def build() -> str:
         return OUT
     os.makedirs(os.path.dirname(OUT), exist_ok=True)
     tmp = OUT + ".tmp%d" % os.getpid()
-    subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-I", CSRC, "-I", os.path.join(ROOT, "include"),
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-fopenmp", "-I", CSRC, "-I", os.path.join(ROOT, "include"),
                            *srcs, "-o", tmp])
     os.replace(tmp, OUT)
     return OUT
