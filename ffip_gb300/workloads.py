@@ -152,13 +152,13 @@ def filtered_noise(shape, sigma, seed):
 
 
 def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0.11), steps=5000, nprobe=4,
-                   seed=2024, precision="fp32", exact=True, broadband=True):
+                   seed=2024, precision="fp32", exact=True, broadband=True, eps_design=12.0):
     """The adjoint-gradient workload: a size[0] x size[0] x size[1] cell box
     (dx = 1, Courant 0.5) with a `pml`-cell CPML; a design box of
     design[0] x design[0] x design[1] cells centred at the origin whose
     density (nodes at every cell corner: (design + 1) per axis) is seeded
     filtered noise (sigma = 3 nodes), eps = 1 + 11 rho (medium1 eps 12,
-    medium2 vacuum); an Ex current sheet (Gaussian1, f = 0.1) half-way
+    medium2 vacuum; eps_design replaces the 12); an Ex current sheet (Gaussian1, f = 0.1) half-way
     between the lower CPML and the design box; objective F = sum over
     `nprobe` seeded probe cells above the design box and over `freqs` of
     |Ex|^2.  One forward run and, with broadband=True, one adjoint run for
@@ -194,7 +194,7 @@ def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0
                 bb.source(f, center=V(*p), size=V(0, 0, 0), dim=V(1, 1, 1),
                           udfs=[field_match_objective(np.zeros((1, 1, 1)), "Ex", weight=1.0)])
             vol = Adjoint_Volume(adj, fwd, frequency=f, center=V(0, 0, 0), size=V(dn, dn, dz), dim=V(dn + 1, dn + 1, dz + 1),
-                                 density=rho0, medium1=Medium(epsilon=12), medium2=Medium(), norm=bb.norm(f), geometry=geom)
+                                 density=rho0, medium1=Medium(epsilon=eps_design), medium2=Medium(), norm=bb.norm(f), geometry=geom)
             geom = vol.geom
             bb.add_volume(vol)
         return D.AdjointProblem(fwd, [bb], run_until_time(steps * dt), exact=exact), rho0
@@ -208,7 +208,7 @@ def adjoint_design(size=(192, 160), design=(96, 24), pml=16, freqs=(0.09, 0.1, 0
         t = np.arange(adj_func.start_time, adj_func.end_time, dt)
         norm = np.sum(np.exp(-2j * np.pi * f * t) * adj_func(t))
         vol = Adjoint_Volume(adj, fwd, frequency=f, center=V(0, 0, 0), size=V(dn, dn, dz), dim=V(dn + 1, dn + 1, dz + 1),
-                             density=rho0, medium1=Medium(epsilon=12), medium2=Medium(), norm=norm, geometry=geom)
+                             density=rho0, medium1=Medium(epsilon=eps_design), medium2=Medium(), norm=norm, geometry=geom)
         geom = vol.geom
         terms.append(D.AdjointTerm(adj, srcs, vol))
     return D.AdjointProblem(fwd, terms, run_until_time(steps * dt), exact=exact), rho0
