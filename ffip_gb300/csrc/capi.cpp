@@ -26,9 +26,11 @@ uint64_t adjoint_transpose_noalloc_capacity();
 int to_convolve(const double *in1, int n0, int n1, const double *in2, int m0, int m1, double *out, int transpose);
 int check_inside(const double *req, uint64_t n, const double *poly, uint64_t m, unsigned char *out);
 int sg_gemm(int M, int N, int K, const void *A, int64_t ars, int64_t acs, const void *B, int64_t brs, int64_t bcs, float *C,
-            int64_t crs, int64_t ccs, const float *bias, int accumulate, void *stream);
+            int64_t crs, int64_t ccs, const float *bias, int accumulate, void *stream, int path);
+int sg_check();
 int sg_im2col(const void *x, const int *shape, const int *kernel, const int *stride, const int *pad, void *cols, void *stream);
 int sg_col2im(const float *dcols, const int *shape, const int *kernel, const int *stride, const int *pad, float *dx, void *stream);
+int sg_im2col_t(const void *x, const int *shape, const int *kernel, const int *stride, const int *pad, void *colsT, void *stream);
 } // namespace ffipg
 
 struct ffip_sim
@@ -379,8 +381,22 @@ int ffip_sg_gemm(int M, int N, int K, const void *A, int64_t ars, int64_t acs, c
 {
     return guard([&]() -> int {
         if ((M > 0 && N > 0) && (!C || (K > 0 && (!A || !B)))) return fail(FFIP_ERR_INVALID, "null argument");
-        return ffipg::sg_gemm(M, N, K, A, ars, acs, B, brs, bcs, C, crs, ccs, bias, accumulate, stream);
+        return ffipg::sg_gemm(M, N, K, A, ars, acs, B, brs, bcs, C, crs, ccs, bias, accumulate, stream, 0);
     });
+}
+
+int ffip_sg_gemm_path(int M, int N, int K, const void *A, int64_t ars, int64_t acs, const void *B, int64_t brs, int64_t bcs,
+                      float *C, int64_t crs, int64_t ccs, const float *bias, int accumulate, void *stream, int path)
+{
+    return guard([&]() -> int {
+        if ((M > 0 && N > 0) && (!C || (K > 0 && (!A || !B)))) return fail(FFIP_ERR_INVALID, "null argument");
+        return ffipg::sg_gemm(M, N, K, A, ars, acs, B, brs, bcs, C, crs, ccs, bias, accumulate, stream, path);
+    });
+}
+
+int ffip_sg_check(void)
+{
+    return guard([&]() -> int { return ffipg::sg_check(); });
 }
 
 int ffip_sg_im2col(const void *x, const int *shape5, const int *kernel3, const int *stride3, const int *pad3, void *cols,
@@ -389,6 +405,15 @@ int ffip_sg_im2col(const void *x, const int *shape5, const int *kernel3, const i
     return guard([&]() -> int {
         if (!x || !shape5 || !kernel3 || !stride3 || !pad3 || !cols) return fail(FFIP_ERR_INVALID, "null argument");
         return ffipg::sg_im2col(x, shape5, kernel3, stride3, pad3, cols, stream);
+    });
+}
+
+int ffip_sg_im2col_t(const void *x, const int *shape5, const int *kernel3, const int *stride3, const int *pad3, void *colsT,
+                     void *stream)
+{
+    return guard([&]() -> int {
+        if (!x || !shape5 || !kernel3 || !stride3 || !pad3 || !colsT) return fail(FFIP_ERR_INVALID, "null argument");
+        return ffipg::sg_im2col_t(x, shape5, kernel3, stride3, pad3, colsT, stream);
     });
 }
 

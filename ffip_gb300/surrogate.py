@@ -38,9 +38,13 @@ def lib():
         P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
         IP = ctypes.POINTER(ctypes.c_int)
         L.ffip_sg_gemm.argtypes = [I, I, I, P, I64, I64, P, I64, I64, P, I64, I64, P, I, P]
+        L.ffip_sg_gemm_path.argtypes = [I, I, I, P, I64, I64, P, I64, I64, P, I64, I64, P, I, P, I]
+        L.ffip_sg_check.argtypes = []
         L.ffip_sg_im2col.argtypes = [P, IP, IP, IP, IP, P, P]
+        L.ffip_sg_im2col_t.argtypes = [P, IP, IP, IP, IP, P, P]
         L.ffip_sg_col2im.argtypes = [P, IP, IP, IP, IP, P, P]
-        for f in ("ffip_sg_gemm", "ffip_sg_im2col", "ffip_sg_col2im"):
+        for f in ("ffip_sg_gemm", "ffip_sg_gemm_path", "ffip_sg_check", "ffip_sg_im2col", "ffip_sg_im2col_t",
+                  "ffip_sg_col2im"):
             getattr(L, f).restype = ctypes.c_int
         _L = L
     return _L
@@ -61,9 +65,11 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def gemm(A, B, bias=None, out=None, accumulate=False):
+def gemm(A, B, bias=None, out=None, accumulate=False, path=0):
     """out[M,N] (fp32) = A[M,K] @ B[K,N] (+ bias), A and B bf16 2-D CUDA
-    tensors of any strides (on the project's tensor-core GEMM)."""
+    tensors of any strides (on the project's tensor-core GEMMs: tcgen05 when
+    K is contiguous in both, A.stride(1) == 1 and B.stride(0) == 1, mma.sync
+    otherwise; path 1 / 2 forces one of them)."""
     torch = _torch()
     if A.dtype != torch.bfloat16 or B.dtype != torch.bfloat16:
         raise TypeError("gemm takes bf16 operands")
@@ -78,10 +84,15 @@ def gemm(A, B, bias=None, out=None, accumulate=False):
         raise ValueError("gemm output must be fp32 of shape (M, N)")
     if bias is not None and (bias.dtype != torch.float32 or not bias.is_contiguous()):
         raise ValueError("bias must be a contiguous fp32 vector")
-    _check(lib().ffip_sg_gemm(M, N, K, A.data_ptr(), A.stride(0), A.stride(1), B.data_ptr(), B.stride(0), B.stride(1),
-                              out.data_ptr(), out.stride(0), out.stride(1), bias.data_ptr() if bias is not None else None,
-                              1 if accumulate else 0, _stream()))
+    _check(lib().ffip_sg_gemm_path(M, N, K, A.data_ptr(), A.stride(0), A.stride(1), B.data_ptr(), B.stride(0), B.stride(1),
+                                   out.data_ptr(), out.stride(0), out.stride(1), bias.data_ptr() if bias is not None else None,
+                                   1 if accumulate else 0, _stream(), int(path)))
     return out
+
+
+def check():
+    """Synchronises and raises if a tcgen05 GEMM gave up on a bounded wait."""
+    _check(lib().ffip_sg_check())
 
 
 def _ints(v):
@@ -101,6 +112,19 @@ def im2col(x, kernel, stride, pad):
     _check(lib().ffip_sg_im2col(x.data_ptr(), _ints(x.shape), _ints(kernel), _ints(stride), _ints(pad), cols.data_ptr(),
                                 _stream()))
     return cols
+
+
+def im2col_t(x, kernel, stride, pad):
+    """The column matrix transposed, [N*Do*Ho*Wo, C*kd*kh*kw]: the forward
+    GEMM's reduction index contiguous."""
+    torch = _torch()
+    x = x.contiguous()
+    N, C = x.shape[:2]
+    Do, Ho, Wo = conv_out(x.shape, kernel, stride, pad)
+    colsT = torch.empty((N * Do * Ho * Wo, C * kernel[0] * kernel[1] * kernel[2]), dtype=torch.bfloat16, device=x.device)
+    _check(lib().ffip_sg_im2col_t(x.data_ptr(), _ints(x.shape), _ints(kernel), _ints(stride), _ints(pad), colsT.data_ptr(),
+                                  _stream()))
+    return colsT
 
 
 def col2im(dcols, shape, kernel, stride, pad):
@@ -126,28 +150,34 @@ def conv(x, w, b, stride, pad):
             @staticmethod
             def forward(ctx, x, w, b, stride, pad):
                 kernel = tuple(w.shape[2:])
-                cols = im2col(x, kernel, stride, pad)
+                # every GEMM below takes its operands with the reduction
+                # index contiguous (the tcgen05 kernel's layout) where the
+                # sizes allow it
+                colsT = im2col_t(x, kernel, stride, pad)  # [N*P, C*k]
                 Co = w.shape[0]
-                wb = w.reshape(Co, -1).to(torch.bfloat16)
-                y = gemm(wb, cols, bias=b.contiguous())  # [Co, N*P]
+                wb = w.reshape(Co, -1).to(torch.bfloat16).contiguous()
+                y = gemm(wb, colsT.t(), bias=b.contiguous())  # [Co, N*P]
                 N = x.shape[0]
                 Do, Ho, Wo = conv_out(x.shape, kernel, stride, pad)
                 y = y.reshape(Co, N, Do, Ho, Wo).permute(1, 0, 2, 3, 4).contiguous().to(torch.bfloat16)
-                ctx.save_for_backward(cols, wb)
+                ctx.save_for_backward(x, wb)
                 ctx.geom = (tuple(x.shape), kernel, stride, pad, tuple(w.shape))
                 return y
 
             @staticmethod
             def backward(ctx, dy):
-                cols, wb = ctx.saved_tensors
+                x, wb = ctx.saved_tensors
                 xshape, kernel, stride, pad, wshape = ctx.geom
                 Co = wshape[0]
-                dy2 = dy.to(torch.bfloat16).permute(1, 0, 2, 3, 4).reshape(Co, -1).contiguous()  # [Co, N*P]
-                dw = gemm(dy2, cols.t()).reshape(wshape)  # [Co, C*k]
+                dyb = dy.to(torch.bfloat16)
+                dy2 = dyb.permute(1, 0, 2, 3, 4).reshape(Co, -1).contiguous()  # [Co, N*P]
+                cols = im2col(x, kernel, stride, pad)  # [C*k, N*P]
+                dw = gemm(cols, dy2.t()).t().reshape(wshape)  # dW^T [C*k, Co]
                 db = dy2.float().sum(1)
                 dx = None
                 if ctx.needs_input_grad[0]:
-                    dcols = gemm(wb.t(), dy2)  # [C*k, N*P]
+                    dy2t = dyb.permute(0, 2, 3, 4, 1).reshape(-1, Co).contiguous()  # [N*P, Co]
+                    dcols = gemm(wb.t().contiguous(), dy2t.t())  # [C*k, N*P]
                     dx = col2im(dcols, xshape, kernel, stride, pad).to(torch.bfloat16)
                 return dx, dw, db, None, None
 

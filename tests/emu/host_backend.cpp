@@ -157,7 +157,12 @@ int check_inside(const double *, uint64_t, const double *, uint64_t, unsigned ch
     throw std::runtime_error("not emulated");
 }
 int sg_gemm(int, int, int, const void *, int64_t, int64_t, const void *, int64_t, int64_t, float *, int64_t, int64_t,
-            const float *, int, void *)
+            const float *, int, void *, int)
+{
+    throw std::runtime_error("not emulated");
+}
+int sg_check() { throw std::runtime_error("not emulated"); }
+int sg_im2col_t(const void *, const int *, const int *, const int *, const int *, void *, void *)
 {
     throw std::runtime_error("not emulated");
 }

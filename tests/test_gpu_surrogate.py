@@ -25,6 +25,36 @@ def test_gemm_matches_fp32_reference(M, N, K):
     assert np.abs(got - ref).max() <= tol
 
 
+@pytest.mark.parametrize("M,N,K", [(128, 128, 64), (37, 129, 72), (5, 7, 8), (200, 300, 136), (256, 512, 6912),
+                                   (300, 1000, 864)])
+def test_tcgen05_and_mma_sync_gemms_match_the_cpu_oracle(M, N, K):
+    """Both tensor-core kernels on K-contiguous operands (the tcgen05 layout:
+    A[m][k] row-major, B given as B^T[n][k]), with bias, then accumulating
+    into the result, against a CPU fp64 oracle."""
+    from ffip_gb300 import surrogate as S
+    g = torch.Generator(device="cuda").manual_seed(M + 3 * N + 7 * K)
+    A = _bf(torch.randn(M, K, device="cuda", generator=g))
+    Bt = _bf(torch.randn(N, K, device="cuda", generator=g))
+    bias = torch.randn(M, device="cuda", generator=g)
+    D = lambda t: t.cpu().double().numpy()  # noqa: E731
+    ref = D(A) @ D(Bt).T + D(bias)[:, None]
+    tol = 1e-5 * K ** 0.5 * np.abs(ref).max() + 1e-6
+    for path in (1, 2):
+        out = S.gemm(A, Bt.t(), bias=bias, path=path)
+        S.gemm(A, Bt.t(), out=out, accumulate=True, path=path)
+        S.check()
+        assert np.abs(D(out) - (2 * ref - D(bias)[:, None])).max() <= 2 * tol, path
+        assert np.abs(D(S.gemm(A, Bt.t(), bias=bias, path=path)) - ref).max() <= tol, path
+
+
+def test_tcgen05_gemm_rejects_operands_it_does_not_take():
+    from ffip_gb300 import surrogate as S
+    A = _bf(torch.randn(16, 24, device="cuda"))
+    B = _bf(torch.randn(24, 16, device="cuda"))  # row-major B: k is not contiguous
+    with pytest.raises(Exception, match="tensor-core GEMM"):
+        S.gemm(A, B, path=1)
+
+
 def test_gemm_strides_bias_and_accumulate():
     from ffip_gb300 import surrogate as S
     g = torch.Generator(device="cuda").manual_seed(1)
