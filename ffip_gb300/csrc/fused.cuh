@@ -190,6 +190,12 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
     }
 }
 
+// the general E path of the interior instance (fp32) adds the DFT sums of
+// a tile row's points together, with their loads batched
+#ifndef FFIP_FUSED_DFT_DEFER
+#define FFIP_FUSED_DFT_DEFER 1
+#endif
+
 // the lean CPML path is compiled per axis for tile planes with CPML along
 // one axis only (fp64: bound by the fp64 pipe, every instruction left out
 // counts; fp32 keeps one generic copy)
@@ -695,7 +701,7 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T, P> &X, int q, in
 template <typename T, bool P, bool FULL = true, bool STAGED = false, bool UNIT = false, int AX = 7>
 __device__ __forceinline__ void e_own_general(const FusedCtx<T, P> &X, int qe, int row, int xi, int eS, int rn, int rp,
                                               unsigned vb, bool pml, bool slots, bool dft, int idx, const int (&sl)[3],
-                                              const T (&ps)[3][2])
+                                              const T (&ps)[3][2], double (*dv)[2] = nullptr)
 {
     using SH = FusedShape<T, P>;
     constexpr int BX = SH::BX, RW = SH::RW;
@@ -768,7 +774,15 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T, P> &X, int qe, i
             st_out(&F.eout[c][idx], v);
             if (en(a1)) st_out(&PE.psi[c][0][idx], ps1);
             if (en(a2)) st_out(&PE.psi[c][1][idx], ps2);
-            if (dft) dft_point<T>(PE.nunits, PE.units, PE.phase, c, x, y, k, (double)v, (double)vd);
+            if (dft && !dv) dft_point<T>(PE.nunits, PE.units, PE.phase, c, x, y, k, (double)v, (double)vd);
+        }
+        // dv: the caller adds the DFT sums of the row's points together
+        // (a point without component c adds zero)
+        if (dv)
+        {
+            const bool val = (vb >> c) & 1u;
+            dv[c][0] = val ? (double)v : 0.0;
+            dv[c][1] = val ? (double)vd : 0.0;
         }
     }
 }
@@ -1389,8 +1403,13 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
             else
             {
                 if (STG && pml_e) cp_async_wait_all();
+                // the interior instance adds the DFT sums of a row's points
+                // together, with their loads batched (dft_points)
+                constexpr bool DEFER = FFIP_FUSED_DFT_DEFER && !PML && sizeof(T) == 4;
+                double dv[NPT][3][2];
 #pragma unroll
                 for (int r = 0; r < RPT; ++r)
+                {
 #pragma unroll
                     for (int p = 0; p < NPT; ++p)
                     {
@@ -1435,7 +1454,8 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                             else
                                 e_own_general<T, PML, true, STG, U>(X, q - 1, r0 + r, xi, eS, rp, rpp,
                                                                vxy[r][p] & (we >> kInfoZValidShift), pml_e, e_slots, dft_e,
-                                                               idx_e + r * sy + p, sl_e[r][p], pe);
+                                                               idx_e + r * sy + p, sl_e[r][p], pe,
+                                                               DEFER && dft_e ? dv[p] : nullptr);
                         };
                         if constexpr (sizeof(T) == 8)
                         {
@@ -1445,6 +1465,19 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         else
                             general_e_own(std::false_type{});
                     }
+                    if (DEFER && dft_e && !lean_e)
+                        for (int c = 0; c < 3; ++c)
+                        {
+                            double v[NPT], vd[NPT];
+#pragma unroll
+                            for (int p = 0; p < NPT; ++p)
+                            {
+                                v[p] = dv[p][c][0];
+                                vd[p] = dv[p][c][1];
+                            }
+                            dft_points<NPT>(PE.nunits, PE.units, PE.phase, c, x, X.y0 + r0 + r, k - 1, v, vd);
+                        }
+                }
             }
         }
         eS = eA;
