@@ -247,6 +247,44 @@ def large_leg(dev, steps=100):
             "seconds_per_design_iter_1fwd_16adj": 17 * run_s}
 
 
+def set_density_leg(dev):
+    """One design iteration's media update (ffip_set_density: new density,
+    media re-derived, fields reset) on the adjoint workload's forward
+    simulation (192 x 192 x 160 cells, 96 x 96 x 24 two-medium box, 97 x 97
+    x 25 density nodes) and on the large design grid (512 x 512 x 384 cells,
+    256 x 256 x 32 Lorentz/vacuum box, 257 x 257 x 33 nodes): median wall
+    time of 3 updates with the media rasterised on the GPU and on the host."""
+    from ffip_gb300 import native, workloads
+    prob, rho = workloads.adjoint_design(precision="fp32")
+    cfg = prob.forward_simulation.config(prob.stop)
+    ds = prob.forward_simulation.dump()
+    name = [k for k in ds if k.startswith("two medium box")][0]
+    big_cfg, big_ds = workloads.large_design(precision="fp32")
+    out = {}
+    for label, (c0, d0, nm, r0) in (("adjoint_design_192x192x160", (cfg, ds, name, rho)),
+                                    ("large_design_512x512x384", (big_cfg, big_ds, "two medium box 0",
+                                                                  big_ds["two medium box 0"]))):
+        res = {}
+        for mode in ("device", "host"):
+            c = dict(c0)
+            c["rasterize"] = mode
+            c["device"] = dev
+            s = native.NativeSim(c, d0)
+            times = []
+            rng = np.random.default_rng(5)
+            for _ in range(3):
+                r2 = np.clip(np.asarray(r0) + 0.05 * rng.normal(size=np.shape(r0)), 0, 1)
+                s.sync()
+                t0 = time.perf_counter()
+                s.set_density(nm, r2)
+                s.sync()
+                times.append(time.perf_counter() - t0)
+            s.close()
+            res[mode + "_ms"] = statistics.median(times) * 1e3
+        out[label] = res
+    return out
+
+
 def vacuum64_leg(dev, cpu):
     """The plain fp64 vacuum box (64^3, 8-cell CPML, one Ez point current,
     Ez DFT plane at 3 frequencies, 1000 steps): GPU fp64 device time, and the
@@ -475,6 +513,11 @@ def main():
     #      run per frequency + gradient), simulations kept between iterations
     if a.design_iters > 0 and not a.fp32_only:
         out["design_iter"] = design_leg(a.design_iters, dev, world)
+    if not a.fp32_only:
+        try:
+            out["set_density"] = set_density_leg(dev)
+        except Exception as e:  # reported, not fatal
+            out["set_density"] = {"error": str(e)[:300]}
     if not a.no_large and not a.fp32_only:
         try:
             out["large_design"] = large_leg(dev)

@@ -386,10 +386,13 @@ public:
         // x, 1 along y); one or two layers beyond a whole number of tiles go
         // to k_face
         const int nxp = xend - kXFirst, nyp = yend - 1;
-        const int rx = nxp % SH::TX, ry = nyp % SH::TY;
-        const int nbx = (nxp >= SH::TX && rx <= 2) ? nxp / SH::TX : (nxp + SH::TX - 1) / SH::TX;
+        // x is cut into units of the CPML instance's tile width: a unit
+        // that touches CPML runs as a CPML job, two (or TX / TX_P) adjacent
+        // units without CPML as one interior job
+        const int rx = nxp % SP::TX, ry = nyp % SH::TY;
+        const int nbx = (nxp >= SP::TX && rx <= 2) ? nxp / SP::TX : (nxp + SP::TX - 1) / SP::TX;
         const int nby = (nyp >= SH::TY && ry <= 2) ? nyp / SH::TY : (nyp + SH::TY - 1) / SH::TY;
-        L.xlim = std::min(xend, kXFirst + nbx * SH::TX);
+        L.xlim = std::min(xend, kXFirst + nbx * SP::TX);
         L.ylim = std::min(yend, 1 + nby * SH::TY);
         L.xend = xend;
         L.yend = yend;
@@ -400,7 +403,7 @@ public:
         // waves of CTAs, fewer still when the grid has too few tiles to fill
         // the GPU twice (each chunk recomputes one H plane, so at least 4)
         if (!nsm_) check(cudaDeviceGetAttribute(&nsm_, cudaDevAttrMultiProcessorCount, dev_), "cudaDeviceGetAttribute");
-        const int64_t tiles = (int64_t)std::max(nbx, 1) * std::max(nby, 1);
+        const int64_t tiles = (int64_t)std::max((nbx * SP::TX + SH::TX - 1) / SH::TX, 1) * std::max(nby, 1);
         const int64_t slots = (int64_t)nsm_ * SH::MINB;  // CTAs resident at once
         const int64_t want = 2 * slots;                  // CTAs for two waves
         const int64_t zlen = L.kend - L.kbeg;
@@ -506,7 +509,9 @@ public:
 
     // CTA jobs of the fused pass (x0, y0, k0, k1): the jobs whose tile, halo
     // and planes touch a CPML point first (nb of them), then the others (ni).
-    // Built once per grid and CPML tables.
+    // Built once per grid, CPML tables and media.  nbx counts x units of
+    // TXP columns (the CPML instance's tile width); an interior job covers
+    // TX / TXP adjacent units.
     struct Jobs
     {
         int4 *dev{nullptr};
@@ -612,20 +617,34 @@ public:
             {
                 const int y0 = 1 + by * TY;
                 const bool yin = !any(1, y0 - 1, y0 + TY - 1);
-                for (int bx = 0; bx < std::max(nbx, 1); ++bx)
+                // units that the interior instance may take: no CPML point in
+                // the unit with its low-x halo (nor in the row or the chunk);
+                // FFIP_FUSED_SLOTS_TO_P: nor material slots (without a DFT
+                // unit): the CPML instance's one point per thread and more
+                // CTAs per SM hide the latency of the slot loads better
+                const int nu = std::max(nbx, 1), per = TX / TXP;
+                std::vector<char> plain(nu);
+                for (int u = 0; u < nu; ++u)
                 {
-                    const int x0 = kXFirst + bx * TX;
-                    const bool xin = !any(0, x0 - 1, x0 + TX - 1);
-                    // a column with material slots (and no DFT unit) runs as
-                    // narrower jobs of the CPML instance as well: its one
-                    // point per thread and more CTAs per SM hide the latency
-                    // of the slot loads better
-                    const int4 j = make_int4(x0, y0, ch.first, ch.second);
-                    if (zin && yin && xin && !(FFIP_FUSED_SLOTS_TO_P && heavy(j, TX) == 1))
-                        in.push_back(j);
-                    else  // a column that touches a CPML point: TX / TXP jobs of the CPML instance
-                        for (int h = 0; h < TX / TXP; ++h)
-                            if (x0 + h * TXP < L.xlim) b.push_back(make_int4(x0 + h * TXP, y0, ch.first, ch.second));
+                    const int x0 = kXFirst + u * TXP;
+                    plain[u] = zin && yin && !any(0, x0 - 1, x0 + TXP - 1) &&
+                               !(FFIP_FUSED_SLOTS_TO_P && heavy(make_int4(x0, y0, ch.first, ch.second), TXP) == 1);
+                }
+                for (int u = 0; u < nu;)
+                {
+                    const int x0 = kXFirst + u * TXP;
+                    bool all = u + per <= nu;
+                    for (int t = 0; t < per && all; ++t) all = plain[u + t] != 0;
+                    if (all)
+                    {
+                        in.push_back(make_int4(x0, y0, ch.first, ch.second));
+                        u += per;
+                    }
+                    else
+                    {
+                        if (x0 < L.xlim) b.push_back(make_int4(x0, y0, ch.first, ch.second));
+                        ++u;
+                    }
                 }
             }
         }

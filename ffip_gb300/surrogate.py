@@ -292,34 +292,29 @@ class DesignWorkload:
     def problem(self, spot: int = 8):
         """The adjoint problem of the spot objective F = -(1/2) sum over the
         central spot x spot cell centres of the output plane, both components
-        and the three frequencies, of |E|^2 (= -intensity/2): one adjoint
-        simulation per frequency, the design box shared with the forward
-        simulation."""
+        and the three frequencies, of |E|^2 (= -intensity/2): one broadband
+        adjoint run for the three frequencies (design.BroadbandAdjoint), the
+        design box shared with the forward simulation."""
         if self._adjoint is not None:
             return self._adjoint
         from . import workloads
-        from .design import AdjointProblem, AdjointTerm
+        from .design import AdjointProblem, BroadbandAdjoint
         from .geom import Medium, Vector3
-        from .simulation import PML, Adjoint_Source, Adjoint_Volume, Simulation, field_match_objective
+        from .simulation import PML, Adjoint_Volume, Simulation, field_match_objective
         from .source import Gaussian1
         V = Vector3
         cells, depth, pml, precision, device, steps = self._spec
-        terms = []
+        adj = Simulation(size=V(cells, cells, depth), resolution=1,
+                         pmls=[PML(thickness=pml, sigma_max=workloads.sigma_max(3, pml))], precision=precision,
+                         device=device)
+        bb = BroadbandAdjoint(adj, self.sim, Gaussian1(0.1, cutoff=4, start_time=0.0), self.FREQS, 0.5)
         for f in self.FREQS:
-            adj = Simulation(size=V(cells, cells, depth), resolution=1,
-                             pmls=[PML(thickness=pml, sigma_max=workloads.sigma_max(3, pml))], precision=precision,
-                             device=device)
-            adj_func = Gaussian1(0.1, cutoff=4, start_time=0.5 / f)
-            src = Adjoint_Source(adj, self.sim, function=adj_func, frequency=f, center=V(0, 0, self.z_out),
-                                 size=V(spot - 1, spot - 1, 0), dim=V(spot, spot, 1),
-                                 udfs=[field_match_objective(np.zeros((1, spot, spot)), c, weight=-1.0) for c in ("Ex", "Ey")])
-            t = np.arange(adj_func.start_time, adj_func.end_time, 0.5)
-            norm = np.sum(np.exp(-2j * np.pi * f * t) * adj_func(t))
-            vol = Adjoint_Volume(adj, self.sim, frequency=f, center=V(0, 0, 0), size=V(self.dn, self.dn, self.dz),
-                                 dim=V(self.dn, self.dn, self.dz), density=self.box.density, medium1=Medium(epsilon=12),
-                                 medium2=Medium(), norm=norm, geometry=self.box)
-            terms.append(AdjointTerm(adj, [src], vol))
-        self._adjoint = AdjointProblem(self.sim, terms, self.stop)
+            bb.source(f, center=V(0, 0, self.z_out), size=V(spot - 1, spot - 1, 0), dim=V(spot, spot, 1),
+                      udfs=[field_match_objective(np.zeros((1, spot, spot)), c, weight=-1.0) for c in ("Ex", "Ey")])
+            bb.add_volume(Adjoint_Volume(adj, self.sim, frequency=f, center=V(0, 0, 0), size=V(self.dn, self.dn, self.dz),
+                                         dim=V(self.dn, self.dn, self.dz), density=self.box.density,
+                                         medium1=Medium(epsilon=12), medium2=Medium(), norm=bb.norm(f), geometry=self.box))
+        self._adjoint = AdjointProblem(self.sim, [bb], self.stop)
         return self._adjoint
 
     def fields(self, rho: np.ndarray) -> np.ndarray:
@@ -414,18 +409,94 @@ def intensity(fields: np.ndarray, spot: int = 8) -> float:
     return float((f ** 2).sum())
 
 
+def design_loop(prob, x0, steps, mode, net=None, scale=1.0, max_accepted=8, target=None, max_iters=None, rng=None):
+    """Minimise the problem's objective from x0 along its adjoint gradient
+    (one forward and one broadband adjoint run per gradient), trying the
+    step sizes `steps` along the normalised steepest-descent direction:
+      plain:    every step size checked by a forward FDTD run, the best kept;
+      screened: the surrogate `net` ranks the step sizes and forward runs
+                check the best two in turn (mode "random": the same with a
+                random order, the loop without a model).
+    Every accepted step is an FDTD-verified improvement.  Stops after
+    `max_accepted` accepted steps, or once the objective is at or below
+    `target`.  Returns seconds, FDTD runs and the objective trace."""
+    x = np.asarray(x0, dtype=np.float64).copy()
+    steps = np.asarray(steps, dtype=np.float64)
+    max_iters = max_iters or 3 * max_accepted
+    t0 = time.perf_counter()
+    F, g = prob.value_and_gradient(x)
+    runs = 1 + len(prob.terms)
+    accepted, trace, runs_at = 0, [F], [runs]
+    for _ in range(max_iters):
+        if accepted >= max_accepted or (target is not None and F <= target):
+            break
+        d = -g / max(np.abs(g).max(), 1e-30)
+        cands = [np.clip(x + s_ * d, 0, 1) for s_ in steps]
+        if mode == "plain":
+            vals = [prob.forward(c) for c in cands]
+            runs += len(cands)
+            best = int(np.argmin(vals))
+            if vals[best] < F:
+                x = cands[best]
+                F, g = prob.value_and_gradient(x)
+                runs += 1 + len(prob.terms)
+                accepted += 1
+                trace.append(F)
+                runs_at.append(runs)
+            else:
+                steps = steps / 4
+            continue
+        if mode == "screened":
+            pred = predict(net, np.stack(cands).astype(np.float32), scale)
+            order = np.argsort([spot_objective(q) for q in pred])
+        else:
+            order = (rng or np.random.default_rng(0)).permutation(len(cands))
+        ok = False
+        for j in order[:2]:
+            v = prob.forward(cands[j])
+            runs += 1
+            if v < F:
+                x, F = cands[j], v
+                g = prob.gradient()
+                runs += len(prob.terms)
+                accepted += 1
+                trace.append(F)
+                runs_at.append(runs)
+                ok = True
+                break
+        if not ok:
+            steps = steps / 4
+    dt = time.perf_counter() - t0
+    return {"accepted": accepted, "seconds": dt, "fdtd_runs": runs, "seconds_per_accepted": dt / max(accepted, 1),
+            "objective": trace, "runs_at_accepted": runs_at, "reached": target is None or F <= target}
+
+
+def compare_loops(wl, net, scale, iters=8, candidates=8, seed=0, log=None):
+    """Plain loop for `iters` accepted steps; its final objective is the
+    target of the screened loop (trained network) and of the same loop with
+    a random ranking (no model), each allowed up to 4 x iters accepted steps:
+    FDTD runs and seconds to reach an equal objective."""
+    prob = wl.problem()
+    x0 = random_designs(1, (wl.dz, wl.dn, wl.dn), seed + 7)[0]
+    steps = np.geomspace(0.01, 0.3, candidates)
+    res = {"plain": design_loop(prob, x0, steps, "plain", max_accepted=iters)}
+    target = res["plain"]["objective"][-1]
+    res["screened"] = design_loop(prob, x0, steps, "screened", net, scale, max_accepted=4 * iters, target=target,
+                                  max_iters=12 * iters)
+    res["random"] = design_loop(prob, x0, steps, "random", max_accepted=4 * iters, target=target, max_iters=12 * iters,
+                                rng=np.random.default_rng(seed))
+    if log:
+        for k, r in res.items():
+            log("%s: %d accepted in %.1f s (%d FDTD runs), objective %.5g -> %.5g%s" % (
+                k, r["accepted"], r["seconds"], r["fdtd_runs"], r["objective"][0], r["objective"][-1],
+                "" if r["reached"] else " (target not reached)"))
+    return res
+
+
 def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed=0, log=print):
-    """Generate, train, evaluate on held-out runs, then compare two design
-    loops of `iters` accepted iterations that minimise the spot objective
-    (maximise the output-plane intensity in the central 8 x 8 cells), both
-    stepping along the adjoint gradient:
-      plain:    `candidates` step sizes each checked by a forward FDTD run,
-                then the gradient at the best (forward + adjoint runs);
-      screened: the surrogate ranks the same step sizes, a forward run
-                checks the best (the second best if it fails), then the
-                adjoint runs.
-    Every accepted step is checked by a full FDTD run in both loops.  Reports
-    seconds and FDTD runs per accepted iteration."""
+    """Generate, train, evaluate on held-out runs, then compare the design
+    loops (compare_loops): seconds and FDTD runs to reach the plain loop's
+    objective after `iters` accepted steps."""
     wl = DesignWorkload()
     rho, y, t_gen = generate(designs, seed, wl)
     log("generated %d designs in %.1f s" % (designs, t_gen))
@@ -436,66 +507,17 @@ def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed
     pred = predict(net, rho[ntr:], tr["scale"])
     err_mean, err_max = relative_error(pred, y[ntr:])
     log("held-out relative error mean %.4f max %.4f" % (err_mean, err_max))
-    # design loops on the spot objective F (minimised): each iteration takes
-    # the adjoint gradient at the current design (one forward and three
-    # adjoint runs) and tries `candidates` step sizes along it
-    prob = wl.problem()
-    x0 = random_designs(1, (wl.dz, wl.dn, wl.dn), seed + 7)[0]
-    steps = np.geomspace(0.01, 0.3, candidates)
-    res = {}
-    for mode in ("plain", "screened"):
-        x = x0.copy()
-        t0 = time.perf_counter()
-        runs = 0
-        F, g = prob.value_and_gradient(x)
-        runs += 1 + len(prob.terms)
-        accepted, trace = 0, [F]
-        for it in range(3 * iters):
-            if accepted >= iters:
-                break
-            d = -g / max(np.abs(g).max(), 1e-30)
-            cands = [np.clip(x + s_ * d, 0, 1) for s_ in steps]
-            if mode == "plain":
-                # every candidate checked by a forward run, the best kept
-                vals = [prob.forward(c) for c in cands]
-                runs += len(cands)
-                best = int(np.argmin(vals))
-                if vals[best] < F:
-                    x = cands[best]
-                    F, g = prob.value_and_gradient(x)
-                    runs += 1 + len(prob.terms)
-                    accepted += 1
-                    trace.append(F)
-                else:
-                    steps = steps / 4
-            else:
-                # the surrogate ranks the candidates; a forward run checks
-                # the best two in turn, and the adjoint runs follow at once
-                pred = predict(net, np.stack(cands), tr["scale"])
-                order = np.argsort([spot_objective(q) for q in pred])
-                ok = False
-                for j in order[:2]:
-                    v = prob.forward(cands[j])
-                    runs += 1
-                    if v < F:
-                        x, F = cands[j], v
-                        g = prob.gradient()
-                        runs += len(prob.terms)
-                        accepted += 1
-                        trace.append(F)
-                        ok = True
-                        break
-                if not ok:
-                    steps = steps / 4
-        dt = time.perf_counter() - t0
-        res[mode] = {"accepted": accepted, "seconds": dt, "fdtd_runs": runs,
-                     "seconds_per_accepted": dt / max(accepted, 1), "objective": trace}
-        log("%s: %d accepted in %.1f s (%d FDTD runs), objective %.5g -> %.5g" % (mode, accepted, dt, runs, trace[0], trace[-1]))
+    res = compare_loops(wl, net, tr["scale"], iters, candidates, seed, log)
     wl.release()
-    return {"designs": designs, "held_out": held_out, "generation_seconds": t_gen, "params": nparams,
-            "train": {"epochs": epochs, "seconds": tr["seconds"], "final_loss": tr["loss"][-1]},
-            "held_out_rel_error_mean": err_mean, "held_out_rel_error_max": err_max, "loops": res,
-            "screened_speedup_per_accepted": res["plain"]["seconds_per_accepted"] / res["screened"]["seconds_per_accepted"]}
+    out = {"designs": designs, "held_out": held_out, "generation_seconds": t_gen, "params": nparams,
+           "train": {"epochs": epochs, "seconds": tr["seconds"], "final_loss": tr["loss"][-1]},
+           "held_out_rel_error_mean": err_mean, "held_out_rel_error_max": err_max, "loops": res}
+    if res["screened"]["reached"]:
+        out["screened_speedup_equal_objective"] = res["plain"]["seconds"] / res["screened"]["seconds"]
+        out["screened_runs_ratio_equal_objective"] = res["plain"]["fdtd_runs"] / res["screened"]["fdtd_runs"]
+    if res["random"]["reached"]:
+        out["random_speedup_equal_objective"] = res["plain"]["seconds"] / res["random"]["seconds"]
+    return out
 
 
 def main(argv=None):
