@@ -520,8 +520,37 @@ def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed
     return out
 
 
+def gemm_bench(M=256, N=32768, K=864, reps=20, log=print):
+    """Times both GEMM kernels on one of the network's convolution shapes
+    (K-contiguous operands): 5 warm-up calls, `reps` timed with CUDA events;
+    returns {path: (ms, TFLOP/s)}."""
+    torch = _torch()
+    g = torch.Generator(device="cuda").manual_seed(0)
+    A = torch.randn(M, K, device="cuda", generator=g).to(torch.bfloat16)
+    Bt = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    out = torch.empty(M, N, device="cuda")
+    res = {}
+    for path, name in ((1, "tcgen05"), (2, "mma.sync")):
+        for _ in range(5):
+            gemm(A, Bt.t(), out=out, path=path)
+        check()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            gemm(A, Bt.t(), out=out, path=path)
+        e1.record()
+        torch.cuda.synchronize()
+        check()
+        ms = e0.elapsed_time(e1) / reps
+        res[name] = (ms, 2.0 * M * N * K / ms / 1e9)
+        if log:
+            log("%s gemm %dx%dx%d: %.4f ms, %.1f TFLOP/s" % (name, M, N, K, ms, res[name][1]))
+    return res
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
+    ap.add_argument("--gemm-bench", action="store_true", help="time the two GEMM kernels on a convolution shape")
     ap.add_argument("--designs", type=int, default=2048)
     ap.add_argument("--held-out", type=int, default=256)
     ap.add_argument("--epochs", type=int, default=50)
@@ -529,6 +558,9 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--out", default=None)
     a = ap.parse_args(argv)
+    if a.gemm_bench:
+        gemm_bench()
+        return
     r = run_study(a.designs, a.held_out, a.epochs, a.iters, seed=a.seed)
     txt = json.dumps(r)
     print(txt)
