@@ -240,7 +240,8 @@ class AdjointProblem:
         F = 0.0
         for t in self.terms:
             F = F + t.evaluate()
-        self.value = float(np.real(F))
+        # (a flux objective is an array over its frequencies: their sum)
+        self.value = float(np.real(np.sum(F)))
         self._pending = True
         return self.value
 

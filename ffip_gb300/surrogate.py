@@ -321,6 +321,11 @@ class DesignWorkload:
         """FDTD: the 12 x 64 x 64 output (Re, Im of Ex, Ey at each frequency)."""
         self.box.density = np.asarray(rho, dtype=np.float64)
         self.sim.run(self.stop, keep=True)
+        return self.last_fields()
+
+    def last_fields(self) -> np.ndarray:
+        """The output of the forward simulation's last run (the design loop's
+        forward runs leave it there too)."""
         out = []
         for d in self.dfts:
             it = d.get_interpolant(method="linear")
@@ -409,7 +414,44 @@ def intensity(fields: np.ndarray, spot: int = 8) -> float:
     return float((f ** 2).sum())
 
 
-def design_loop(prob, x0, steps, mode, net=None, scale=1.0, max_accepted=8, target=None, max_iters=None, rng=None):
+class OnlineRefiner:
+    """Refines the surrogate on the design loop's own FDTD runs: every
+    forward run of a screened candidate adds (design, output fields) to a
+    buffer, and `steps` Adam steps on the buffer's latest `window` samples
+    (together with as many samples of the training set) follow, so that the
+    network learns the neighbourhood the loop moves through."""
+
+    def __init__(self, net, wl, scale, train_rho, train_y, steps=8, window=16, lr=1e-3, seed=0):
+        torch = _torch()
+        self.net, self.wl, self.scale, self.steps, self.window = net, wl, scale, steps, window
+        self.rho, self.y = train_rho, train_y
+        self.opt = torch.optim.Adam(net.parameters(), lr=lr)
+        self.buf_x, self.buf_y = [], []
+        self.rng = np.random.default_rng(seed)
+        self.seconds = 0.0
+
+    def __call__(self, x):
+        torch = _torch()
+        t0 = time.perf_counter()
+        self.buf_x.append(np.asarray(x, dtype=np.float32))
+        self.buf_y.append(self.wl.last_fields() / self.scale)
+        dev = torch.device("cuda")
+        bx = np.stack(self.buf_x[-self.window:])
+        by = np.stack(self.buf_y[-self.window:])
+        for _ in range(self.steps):
+            idx = self.rng.integers(0, len(self.rho), size=len(bx))
+            X = torch.tensor(np.concatenate([bx, self.rho[idx]]), device=dev)
+            Y = torch.tensor(np.concatenate([by, self.y[idx] / self.scale]), device=dev)
+            loss = torch.mean((self.net(X) - Y) ** 2)
+            self.opt.zero_grad(set_to_none=True)
+            loss.backward()
+            self.opt.step()
+        torch.cuda.synchronize()
+        self.seconds += time.perf_counter() - t0
+
+
+def design_loop(prob, x0, steps, mode, net=None, scale=1.0, max_accepted=8, target=None, max_iters=None, rng=None,
+                observe=None):
     """Minimise the problem's objective from x0 along its adjoint gradient
     (one forward and one broadband adjoint run per gradient), trying the
     step sizes `steps` along the normalised steepest-descent direction:
@@ -419,7 +461,9 @@ def design_loop(prob, x0, steps, mode, net=None, scale=1.0, max_accepted=8, targ
                 random order, the loop without a model).
     Every accepted step is an FDTD-verified improvement.  Stops after
     `max_accepted` accepted steps, or once the objective is at or below
-    `target`.  Returns seconds, FDTD runs and the objective trace."""
+    `target`.  observe(x): called after each screened candidate's forward
+    run (an OnlineRefiner).  Returns seconds, FDTD runs and the objective
+    trace."""
     x = np.asarray(x0, dtype=np.float64).copy()
     steps = np.asarray(steps, dtype=np.float64)
     max_iters = max_iters or 3 * max_accepted
@@ -455,6 +499,8 @@ def design_loop(prob, x0, steps, mode, net=None, scale=1.0, max_accepted=8, targ
         for j in order[:2]:
             v = prob.forward(cands[j])
             runs += 1
+            if observe is not None:
+                observe(cands[j])
             if v < F:
                 x, F = cands[j], v
                 g = prob.gradient()
@@ -471,11 +517,13 @@ def design_loop(prob, x0, steps, mode, net=None, scale=1.0, max_accepted=8, targ
             "objective": trace, "runs_at_accepted": runs_at, "reached": target is None or F <= target}
 
 
-def compare_loops(wl, net, scale, iters=8, candidates=8, seed=0, log=None):
+def compare_loops(wl, net, scale, iters=8, candidates=8, seed=0, log=None, train_rho=None, train_y=None):
     """Plain loop for `iters` accepted steps; its final objective is the
-    target of the screened loop (trained network) and of the same loop with
-    a random ranking (no model), each allowed up to 4 x iters accepted steps:
-    FDTD runs and seconds to reach an equal objective."""
+    target of the screened loop (trained network; refined online on the
+    loop's own runs when the training set is given) and of the same loop
+    with a random ranking (no model), each allowed up to 4 x iters accepted
+    steps: FDTD runs and seconds to reach an equal objective."""
+    import copy
     prob = wl.problem()
     x0 = random_designs(1, (wl.dz, wl.dn, wl.dn), seed + 7)[0]
     steps = np.geomspace(0.01, 0.3, candidates)
@@ -483,6 +531,12 @@ def compare_loops(wl, net, scale, iters=8, candidates=8, seed=0, log=None):
     target = res["plain"]["objective"][-1]
     res["screened"] = design_loop(prob, x0, steps, "screened", net, scale, max_accepted=4 * iters, target=target,
                                   max_iters=12 * iters)
+    if train_rho is not None:
+        net2 = copy.deepcopy(net)
+        ref = OnlineRefiner(net2, wl, scale, train_rho, train_y, seed=seed)
+        res["screened_online"] = design_loop(prob, x0, steps, "screened", net2, scale, max_accepted=4 * iters, target=target,
+                                             max_iters=12 * iters, observe=ref)
+        res["screened_online"]["refine_seconds"] = ref.seconds
     res["random"] = design_loop(prob, x0, steps, "random", max_accepted=4 * iters, target=target, max_iters=12 * iters,
                                 rng=np.random.default_rng(seed))
     if log:
@@ -507,7 +561,7 @@ def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed
     pred = predict(net, rho[ntr:], tr["scale"])
     err_mean, err_max = relative_error(pred, y[ntr:])
     log("held-out relative error mean %.4f max %.4f" % (err_mean, err_max))
-    res = compare_loops(wl, net, tr["scale"], iters, candidates, seed, log)
+    res = compare_loops(wl, net, tr["scale"], iters, candidates, seed, log, rho[:ntr], y[:ntr])
     wl.release()
     out = {"designs": designs, "held_out": held_out, "generation_seconds": t_gen, "params": nparams,
            "train": {"epochs": epochs, "seconds": tr["seconds"], "final_loss": tr["loss"][-1]},
@@ -517,6 +571,8 @@ def run_study(designs=2048, held_out=256, epochs=50, iters=8, candidates=8, seed
         out["screened_runs_ratio_equal_objective"] = res["plain"]["fdtd_runs"] / res["screened"]["fdtd_runs"]
     if res["random"]["reached"]:
         out["random_speedup_equal_objective"] = res["plain"]["seconds"] / res["random"]["seconds"]
+    if res.get("screened_online", {}).get("reached"):
+        out["screened_online_runs_ratio_equal_objective"] = res["plain"]["fdtd_runs"] / res["screened_online"]["fdtd_runs"]
     return out
 
 
