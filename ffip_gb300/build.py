@@ -62,7 +62,7 @@ def build(force: bool = False, verbose: bool = False, defines=(), libdir: str | 
     for s in CXX_SOURCES:
         o = os.path.join(bdir, s + ".o")
         objs.append(o)
-        jobs.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function", *inc,
+        jobs.append(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-Wall", "-Wno-unused-function", *dflags, *inc,
                      "-I", "/usr/local/cuda/include", "-c", os.path.join(CSRC, s), "-o", o])
     cli_obj = os.path.join(bdir, "run_sim_json.cpp.o")
     jobs.append(["g++", "-O2", "-std=c++17", "-Wall", *inc, "-c", os.path.join(CSRC, "run_sim_json.cpp"), "-o", cli_obj])

@@ -134,11 +134,15 @@ constexpr int fused_box_width(int xoff, int tx, int elems16) { return (xoff + tx
 // runs as TX / TX_P narrower jobs of the CPML instance.
 template <typename T, bool P>
 struct FusedShape;
+#ifndef FFIP_FUSED_F32_XOFF
+#define FFIP_FUSED_F32_XOFF 4
+#endif
 template <bool P>
 struct FusedShape<float, P>
 {
     static constexpr int NPT = P ? FFIP_FUSED_F32_NPT_PML : FFIP_FUSED_F32_NPT, TX = 32 * NPT, RPT = FFIP_FUSED_F32_RPT,
-                         TY = 8 * RPT, XOFF = 4, BX = fused_box_width(XOFF, TX, 4), RW = XOFF + TX,
+                         TY = 8 * RPT, XOFF = FFIP_FUSED_F32_XOFF, BX = fused_box_width(XOFF, TX, 4),
+                         RW = (XOFF + TX + 3) / 4 * 4,
                          SE = NPT == 1 ? FFIP_FUSED_F32_SE : FFIP_FUSED_F32_SE_X2, SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH,
                          KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT, MINB = NPT == 1 ? FFIP_FUSED_F32_MINB : FFIP_FUSED_F32_MINB_X2,
                          STAGE_PSI = FFIP_FUSED_F32_STAGE_PSI;
@@ -189,6 +193,12 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
         for (int i = 0; i < N; ++i) p[i] = v.v[i];
     }
 }
+
+// fp32 interior instance: E rows with material slots on a tile plane that
+// is otherwise plain take the plain path with the slot points patched
+#ifndef FFIP_FUSED_SLOT_PATCH
+#define FFIP_FUSED_SLOT_PATCH 1
+#endif
 
 // the general E path of the interior instance (fp32) adds the DFT sums of
 // a tile row's points together, with their loads batched
@@ -1028,7 +1038,10 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
         const unsigned wh = info[q], we = q >= 1 ? info[q - 1] : 0u;
         const bool e_slots = (we & rowmask) != 0u;
         const bool fast_h = wh & kInfoFastH;
-        const bool fast_e = (we & kInfoFastE) && !e_slots;
+        // E rows with material slots on an otherwise plain tile plane: the
+        // plain path with the slot points patched (fp32 interior instance)
+        const bool fast_e_sl = FFIP_FUSED_SLOT_PATCH && !PML && sizeof(T) == 4 && (we & kInfoFastE) && e_slots;
+        const bool fast_e = ((we & kInfoFastE) && !e_slots) || fast_e_sl;
         const bool lean_h = PML && (wh & kInfoLeanH);
         const bool lean_e = PML && (we & kInfoLeanE) && !e_slots;
         const bool pml_h = !fast_h && pml_tables && (wh & kInfoZPml);
@@ -1342,8 +1355,9 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
         {
             if (fast_e)
             {
-                auto fast_e_own = [&](auto unit) {
+                auto fast_e_own = [&](auto unit, auto slotted) {
                     constexpr bool U = decltype(unit)::value;
+                    constexpr bool SL = decltype(slotted)::value;
                     const T *eS0 = X.e_tile(eS, 0) + offE, *eS1 = X.e_tile(eS, 1) + offE, *eS2 = X.e_tile(eS, 2) + offE;
                     const T *n0 = X.hn_plane(rp, 0) + offN, *n1 = X.hn_plane(rp, 1) + offN, *n2 = X.hn_plane(rp, 2) + offN;
                     const T *p0 = X.hn_plane(rpp, 0) + offN, *p1 = X.hn_plane(rpp, 1) + offN;
@@ -1370,6 +1384,33 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                             ey[p] = e1[p] + coefE * curl_diff<U>(hx[r + 1][p], hxp[p], hz[r + 1][p], hzx, ide);
                             ez[p] = e2[p] + coefE * curl_diff<U>(hyr[p], hyx, hx[r + 1][p], hx[r][p], ide);
                         }
+                        // SL: the points with a material slot take the slot's
+                        // update from the same curl terms (as the general path)
+                        T vds[3][NPT];
+                        if constexpr (SL)
+                        {
+#pragma unroll
+                            for (int p = 0; p < NPT; ++p)
+                            {
+                                vds[0][p] = PE.g_def * ex[p];
+                                vds[1][p] = PE.g_def * ey[p];
+                                vds[2][p] = PE.g_def * ez[p];
+                            }
+#pragma unroll
+                            for (int p = 0; p < NPT; ++p)
+                            {
+                                const T hzx = p > 0 ? hz[r + 1][p - 1] : hzw, hyx = p > 0 ? hyr[p - 1] : hyw;
+                                if (sl_e[r][p][0] >= 0)
+                                    ex[p] = material_rec(PE, PE.slot[0], sl_e[r][p][0], e0[p],
+                                                         curl_diff<U>(hz[r + 1][p], hz[r][p], hyr[p], hyp[p], ide), &vds[0][p]);
+                                if (sl_e[r][p][1] >= 0)
+                                    ey[p] = material_rec(PE, PE.slot[1], sl_e[r][p][1], e1[p],
+                                                         curl_diff<U>(hx[r + 1][p], hxp[p], hz[r + 1][p], hzx, ide), &vds[1][p]);
+                                if (sl_e[r][p][2] >= 0)
+                                    ez[p] = material_rec(PE, PE.slot[2], sl_e[r][p][2], e2[p],
+                                                         curl_diff<U>(hyr[p], hyx, hx[r + 1][p], hx[r][p], ide), &vds[2][p]);
+                            }
+                        }
                         st_outv(&F.eout[0][idx_e + r * sy], ex);
                         st_outv(&F.eout[1][idx_e + r * sy], ey);
                         st_outv(&F.eout[2][idx_e + r * sy], ez);
@@ -1382,7 +1423,10 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                 for (int p = 0; p < NPT; ++p)
                                 {
                                     v[p] = (double)ev[p];
-                                    vd[p] = (double)(PE.g_def * ev[p]);
+                                    if constexpr (SL)
+                                        vd[p] = (double)vds[c][p];
+                                    else
+                                        vd[p] = (double)(PE.g_def * ev[p]);
                                 }
                                 if constexpr (PML)
                                     for (int p = 0; p < NPT; ++p)
@@ -1394,11 +1438,13 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 };
                 if constexpr (sizeof(T) == 8)
                 {
-                    if (unit_dx) fast_e_own(std::true_type{});
-                    else fast_e_own(std::false_type{});
+                    if (unit_dx) fast_e_own(std::true_type{}, std::false_type{});
+                    else fast_e_own(std::false_type{}, std::false_type{});
                 }
+                else if (fast_e_sl)
+                    fast_e_own(std::false_type{}, std::true_type{});
                 else
-                    fast_e_own(std::false_type{});
+                    fast_e_own(std::false_type{}, std::false_type{});
             }
             else
             {

@@ -32,7 +32,10 @@ constexpr int kMaxPoles = 8;                    // poles per grid point in one s
 // 128-byte boundary and the fused pass's tiles start at index kXFirst, so
 // that every tile's TMA box (kXFirst elements to the left of the tile) and
 // the vector loads and stores of its own points are 16-byte aligned
-constexpr int kXFirst = 4;
+#ifndef FFIP_XFIRST
+#define FFIP_XFIRST 4
+#endif
+constexpr int kXFirst = FFIP_XFIRST;
 
 enum Comp { EX = 0, EY = 1, EZ = 2, HX = 3, HY = 4, HZ = 5 };
 enum BC { BC_PEC = 0, BC_PMC = 1, BC_NONE = 2, BC_SYNC = 3, BC_PERIOD = 4 };
