@@ -135,7 +135,7 @@ constexpr int fused_box_width(int xoff, int tx, int elems16) { return (xoff + tx
 template <typename T, bool P>
 struct FusedShape;
 #ifndef FFIP_FUSED_F32_XOFF
-#define FFIP_FUSED_F32_XOFF 4
+#define FFIP_FUSED_F32_XOFF 2
 #endif
 template <bool P>
 struct FusedShape<float, P>
@@ -1223,7 +1223,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                     }
                                     // (the CPML instance adds its few such sums one at a
                                     // time: no call from its loop)
-                                    if constexpr (PML)
+                                    if constexpr (PML || NPT == 1)
                                         for (int p = 0; p < NPT; ++p)
                                             dft_point<T>(PH.nunits, PH.units, PH.phase, 3 + c, x + p, X.y0 + r0 + r, k, v[p], vd[p]);
                                     else
@@ -1428,7 +1428,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                     else
                                         vd[p] = (double)(PE.g_def * ev[p]);
                                 }
-                                if constexpr (PML)
+                                if constexpr (PML || NPT == 1)
                                     for (int p = 0; p < NPT; ++p)
                                         dft_point<T>(PE.nunits, PE.units, PE.phase, c, x + p, X.y0 + r0 + r, k - 1, v[p], vd[p]);
                                 else
@@ -1451,7 +1451,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 if (STG && pml_e) cp_async_wait_all();
                 // the interior instance adds the DFT sums of a row's points
                 // together, with their loads batched (dft_points)
-                constexpr bool DEFER = FFIP_FUSED_DFT_DEFER && !PML && sizeof(T) == 4;
+                constexpr bool DEFER = FFIP_FUSED_DFT_DEFER && !PML && sizeof(T) == 4 && NPT > 1;
                 double dv[NPT][3][2];
 #pragma unroll
                 for (int r = 0; r < RPT; ++r)

@@ -33,7 +33,7 @@ constexpr int kMaxPoles = 8;                    // poles per grid point in one s
 // that every tile's TMA box (kXFirst elements to the left of the tile) and
 // the vector loads and stores of its own points are 16-byte aligned
 #ifndef FFIP_XFIRST
-#define FFIP_XFIRST 4
+#define FFIP_XFIRST 2
 #endif
 constexpr int kXFirst = FFIP_XFIRST;
 
