@@ -70,13 +70,14 @@ namespace ffipg
 // STAGE_PSI: the CPML instance stages psi in shared memory by cp.async,
 // ahead of use (fp32 only: the fp64 pass is bound by fp64 arithmetic, and
 // there the copy instructions cost more than the latency they hide).  Tiles
-// start at x0 = kXFirst + TX * bx (the first index that holds grid points);
-// the TMA box starts XOFF elements to the left, at a 16-byte boundary
-// (TX * bx), and spans BX >= XOFF + TX + 1 elements (x0 - XOFF .. x0 + TX),
-// rounded up to 16 bytes; a thread's own points sit XOFF + NPT lane + p into
-// a box row (8-byte aligned pairs in fp32).  The H ring planes hold rows of
-// RW = XOFF + TX elements: the low-x halo column at XOFF - 1, the tile's own
-// points from XOFF on.
+// start at x0 = kXFirst + 32 u (u a unit of the job lists; kXFirst, the first
+// index that holds grid points, is 2); the TMA box starts XOFF = 2 elements
+// to the left, at a 16-byte boundary (32 u), and spans BX >= XOFF + TX + 1
+// elements (x0 - XOFF .. x0 + TX), rounded up to 16 bytes; a thread's own
+// points sit XOFF + NPT lane + p into a box row (8-byte aligned pairs in
+// fp32).  The H ring planes hold rows of RW elements (XOFF + TX rounded up to
+// 16 bytes): the low-x halo column at XOFF - 1, the tile's own points from
+// XOFF on.
 #ifndef FFIP_FUSED_F32_NPT
 #define FFIP_FUSED_F32_NPT 2
 #endif

@@ -29,9 +29,10 @@ namespace ffipg
 constexpr double kPi = 3.141592653589793e+00;  // src/utility.cpp:5
 constexpr int kMaxPoles = 8;                    // poles per grid point in one slot
 // first array index along x that holds grid points: rows start on a
-// 128-byte boundary and the fused pass's tiles start at index kXFirst, so
-// that every tile's TMA box (kXFirst elements to the left of the tile) and
-// the vector loads and stores of its own points are 16-byte aligned
+// 128-byte boundary and the fused pass's tiles start at index kXFirst + 32 u,
+// so that every tile's TMA box (kXFirst elements to the left of the tile) is
+// 16-byte aligned and the pairs of points that a thread loads and stores as
+// one vector are 8-byte aligned
 #ifndef FFIP_XFIRST
 #define FFIP_XFIRST 2
 #endif

@@ -59,6 +59,8 @@ class Fields_DFT:
         self.frequency = np.asarray(g["f"])
         self.x, self.y, self.z = np.asarray(g["x"]), np.asarray(g["y"]), np.asarray(g["z"])
         self.v = g["real"] + 1j * g["imag"]
+        # the output grid as written (before the widening below)
+        self.raw = (self.frequency.copy(), self.z.copy(), self.y.copy(), self.x.copy(), self.v)
         if not self.degenerate:
             # size-1 axes are widened so that interpolation works (simulation.py:55-72)
             if self.frequency.size == 1:
@@ -640,6 +642,28 @@ def sensitivity_scatter(factor, norm, fwd, adj, deps, x, y, z, gx, gy, gz):
     return out
 
 
+def _dft_at_points(dft, f, x, y, z):
+    """A DFT monitor's values at frequency f and points (x, y, z): where every
+    point is a node of the monitor's output grid (the design box's own grid
+    points are), read directly -- the linear interpolant returns the node's
+    value there -- else through the interpolant."""
+    def index(grid, q):
+        grid = np.asarray(grid, dtype=float)
+        i = np.clip(np.searchsorted(grid, q), 0, grid.size - 1)
+        j = np.clip(i - 1, 0, grid.size - 1)
+        i = np.where(np.abs(grid[j] - q) < np.abs(grid[i] - q), j, i)
+        return i, np.all(np.abs(grid[i] - q) <= 1e-9 * max(1.0, float(np.abs(grid).max())))
+    rf, rz, ry, rx, rv = dft.raw
+    fi = np.flatnonzero(np.asarray(rf) == f)
+    ix, okx = index(rx, x)
+    iy, oky = index(ry, y)
+    iz, okz = index(rz, z)
+    if fi.size and okx and oky and okz:
+        return rv[fi[0], iz, iy, ix]
+    pts = np.stack((f * np.ones(np.shape(z)), z, y, x), axis=-1)
+    return dft.get_interpolant(method="linear", bounds_error=True)(pts)
+
+
 class Adjoint_Volume:
     """Design region and its sensitivity (simulation.py:759-915)."""
 
@@ -727,9 +751,8 @@ class Adjoint_Volume:
         res = 0
         for i in range(3):
             x, y, z = self.design_points(i)
-            pts = np.stack((self.frequency * np.ones(z.shape), z, y, x), axis=-1)
-            fwd = self.forward_dfts[i].get_interpolant(method="linear", bounds_error=True)(pts)
-            adj = self.adjoint_dfts[i].get_interpolant(method="linear", bounds_error=True)(pts)
+            fwd = _dft_at_points(self.forward_dfts[i], self.frequency, x, y, z)
+            adj = _dft_at_points(self.adjoint_dfts[i], self.frequency, x, y, z)
             deps = self.epsilon_der(rho_interp(np.stack((z, y, x), axis=-1)))
             res = res + sensitivity_scatter(factor, self.norm, fwd, adj, np.asarray(deps, dtype=complex), x, y, z,
                                             self.x, self.y, self.z)

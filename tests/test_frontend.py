@@ -79,3 +79,29 @@ def test_pml_keeps_explicit_sigma_max():
     p = ffip.PML(thickness=2, sigma_max=3.0)
     ffip.Simulation(size=ffip.Vector3(8, 8, 8), resolution=1, pmls=[p])
     assert p.get_json()["sigma max"] == 3.0
+
+
+def test_dft_values_at_grid_nodes_read_directly_equal_the_interpolant():
+    """Adjoint_Volume reads the forward / adjoint DFT monitors at the design
+    box's own grid points: directly where the points are nodes of the
+    monitor's output grid, through the reference's linear interpolant
+    (ffip/simulation.py:55-91) elsewhere; at the nodes the two agree to
+    rounding (the interpolant's weights at a node are 0 and 1 up to an ulp;
+    the widened one-frequency axis averages two equal values)."""
+    from ffip_gb300.geom import Vector3
+    from ffip_gb300.simulation import Fields_DFT, _dft_at_points
+    rng = np.random.default_rng(0)
+    d = Fields_DFT(Vector3(0, 0, 0), Vector3(4, 3, 0), [0.1], "Ex", suffix="t", dx=1.0)
+    x, y, z = np.arange(-2.5, 2.6, 1.0), np.arange(-1.5, 1.6, 0.5), np.array([0.0])
+    shape = (1, z.size, y.size, x.size)
+    d.read({d.group_name: {"f": np.array([0.1]), "x": x, "y": y, "z": z, "real": rng.normal(size=shape),
+                           "imag": rng.normal(size=shape)}})
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    got = _dft_at_points(d, 0.1, X.ravel(), Y.ravel(), Z.ravel())
+    want = d.get_interpolant(method="linear", bounds_error=True)(
+        np.stack((np.full(X.size, 0.1), Z.ravel(), Y.ravel(), X.ravel()), axis=-1))
+    np.testing.assert_allclose(got, want, rtol=1e-14, atol=1e-15)
+    # off-node points take the interpolant
+    xs = np.array([-2.0, 0.25]), np.array([-1.5, 0.0]), np.array([0.0, 0.0])
+    off = _dft_at_points(d, 0.1, *xs)
+    np.testing.assert_allclose(off, d.get_interpolant(method="linear")(np.stack((np.full(2, 0.1), xs[2], xs[1], xs[0]), -1)))
