@@ -473,9 +473,9 @@ def main():
     step_achieved = res["fp32"]["bytes_per_step"] / (t32 * 1e-3) / 1e9
     # the dominant kernel's own figure: one launch of the fused pass covers
     # every cell of one step; its algorithmic bytes are the step's (fields,
-    # CPML psi, polarisation state, DFT sums: the DFT sums of the previous
-    # step run in k_dft on their own stream inside the pass's window), over
-    # the pass's device time (events around each pass on the stepper's stream)
+    # CPML psi, polarisation state, DFT sums: the pass adds the sums of the
+    # monitored points itself), over the pass's device time (events around
+    # each pass on the stepper's stream)
     tp32 = res["fp32"]["pass_ms"] / a.steps
     if res["fp32"]["fused"] and tp32 > 0:
         achieved = res["fp32"]["bytes_per_step"] / (tp32 * 1e-3) / 1e9
