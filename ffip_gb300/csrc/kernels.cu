@@ -38,6 +38,11 @@ void raster_media(const Plan &p, bool fp32, const std::function<void *(size_t)> 
 #ifndef FFIP_FUSED_HEAVY_FIRST
 #define FFIP_FUSED_HEAVY_FIRST 1
 #endif
+// jobs that meet DFT monitors split along z (1 + frequencies / this many
+// pieces; 0: not split)
+#ifndef FFIP_FUSED_DFT_SPLIT
+#define FFIP_FUSED_DFT_SPLIT 2
+#endif
 // tile columns with material slots (and no DFT unit) go to the CPML instance
 // (off: measured 6 % slower on the 256^3 dispersive workload, where the CPML
 // instance is the longer of the two)
@@ -650,6 +655,42 @@ public:
                 }
             }
         }
+#if FFIP_FUSED_DFT_SPLIT > 0
+        // a job whose planes meet DFT monitors carries the monitors' running
+        // sums beside its field traffic (fp64 re + im per frequency, read and
+        // written): it is split along z into about 1 + (frequencies summed
+        // over the monitors it meets) / FFIP_FUSED_DFT_SPLIT shorter jobs, so
+        // that the pass does not wait on a few long ones
+        auto dft_freqs = [&](const int4 &j, int tx) {
+            int nf = 0;
+            for (int sd = 0; sd < 2; ++sd)
+            {
+                const SideParams<T> &S = sd ? p.h : p.e;
+                for (int u = 0; u < S.nunits; ++u)
+                {
+                    const DftView &U = S.units[u];
+                    if (U.i0[0] < j.x + tx && U.i0[0] + U.ld[0] > j.x && U.i0[1] < j.y + TY && U.i0[1] + U.ld[1] > j.y &&
+                        U.i0[2] < j.w && U.i0[2] + U.ld[2] > j.z - 1)
+                        nf += U.nf;
+                }
+            }
+            return nf;
+        };
+        auto split_dft = [&](std::vector<int4> &v, int tx) {
+            std::vector<int4> o;
+            o.reserve(v.size());
+            for (const int4 &j : v)
+            {
+                const int nf = dft_freqs(j, tx), planes = j.w - j.z;
+                const int m = nf ? std::max(1, std::min(planes, 1 + nf / FFIP_FUSED_DFT_SPLIT)) : 1;
+                for (int i = 0; i < m; ++i)
+                    o.push_back(make_int4(j.x, j.y, j.z + (int)((int64_t)planes * i / m), j.z + (int)((int64_t)planes * (i + 1) / m)));
+            }
+            v.swap(o);
+        };
+        split_dft(b, TXP);
+        split_dft(in, TX);
+#endif
 #if FFIP_FUSED_HEAVY_FIRST
         // within each instance, the jobs that add DFT sums or update material
         // slots (several times the work of a plain job) go first, so that the
