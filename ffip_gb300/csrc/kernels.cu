@@ -41,7 +41,7 @@ void raster_media(const Plan &p, bool fp32, const std::function<void *(size_t)> 
 // jobs that meet DFT monitors split along z (1 + frequencies / this many
 // pieces; 0: not split)
 #ifndef FFIP_FUSED_DFT_SPLIT
-#define FFIP_FUSED_DFT_SPLIT 2
+#define FFIP_FUSED_DFT_SPLIT 4
 #endif
 // tile columns with material slots (and no DFT unit) go to the CPML instance
 // (off: measured 6 % slower on the 256^3 dispersive workload, where the CPML
