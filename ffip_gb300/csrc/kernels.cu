@@ -43,6 +43,11 @@ void raster_media(const Plan &p, bool fp32, const std::function<void *(size_t)> 
 #ifndef FFIP_FUSED_DFT_SPLIT
 #define FFIP_FUSED_DFT_SPLIT 4
 #endif
+// CPML jobs ordered by the number of axes along which they meet CPML (after
+// the DFT and slot weights)
+#ifndef FFIP_FUSED_CPML_ORDER
+#define FFIP_FUSED_CPML_ORDER 0
+#endif
 // tile columns with material slots (and no DFT unit) go to the CPML instance
 // (off: measured 6 % slower on the 256^3 dispersive workload, where the CPML
 // instance is the longer of the two)
@@ -695,9 +700,15 @@ public:
         // within each instance, the jobs that add DFT sums or update material
         // slots (several times the work of a plain job) go first, so that the
         // launch does not end on a few long jobs
+        // CPML jobs: the more axes along which the job's box meets CPML, the
+        // more psi it updates (FFIP_FUSED_CPML_ORDER)
+        auto cpml_axes = [&](const int4 &j, int tx) {
+            return (int)any(0, j.x - 1, j.x + tx - 1) + (int)any(1, j.y - 1, j.y + TY - 1) + (int)any(2, j.z - 1, j.w - 1);
+        };
         auto order = [&](std::vector<int4> &v, int tx) {
             std::vector<std::pair<int, size_t>> key(v.size());
-            for (size_t i = 0; i < v.size(); ++i) key[i] = {-heavy(v[i], tx), i};
+            for (size_t i = 0; i < v.size(); ++i)
+                key[i] = {-(4 * heavy(v[i], tx) + (FFIP_FUSED_CPML_ORDER ? cpml_axes(v[i], tx) : 0)), i};
             std::stable_sort(key.begin(), key.end());
             std::vector<int4> o(v.size());
             for (size_t i = 0; i < v.size(); ++i) o[i] = v[key[i].second];
