@@ -195,6 +195,11 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
     }
 }
 
+// plain paths: x +- 1 neighbours from the adjacent lane by warp shuffle
+#ifndef FFIP_FUSED_SHFL
+#define FFIP_FUSED_SHFL 1
+#endif
+
 // fp32 interior instance: E rows with material slots on a tile plane that
 // is otherwise plain take the plain path with the slot points patched
 #ifndef FFIP_FUSED_SLOT_PATCH
@@ -1180,8 +1185,25 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                     {
                         const Vals<T, NPT> eya = ldv<NPT>(eA1 + r * BX), eyb = ldv<NPT>(eB1 + r * BX), exb = ldv<NPT>(eB0 + r * BX);
                         const Vals<T, NPT> h0 = ldv<NPT>(hA0 + r * BX), h1 = ldv<NPT>(hA1 + r * BX), h2 = ldv<NPT>(hA2 + r * BX);
-                        // x + 1 neighbours: the next point of the pair, or the box column after it
-                        const T eyn = eA1[r * BX + NPT], ezn = eA2[r * BX + NPT];
+                        // x + 1 neighbours: the next point of the pair, or the
+                        // next lane's first point (warp shuffle; the last lane
+                        // reads the box column after the tile)
+                        T eyn, ezn;
+                        if constexpr (FFIP_FUSED_SHFL)
+                        {
+                            eyn = __shfl_down_sync(0xffffffffu, eya[0], 1);
+                            ezn = __shfl_down_sync(0xffffffffu, eza[r][0], 1);
+                            if (lane == 31)
+                            {
+                                eyn = eA1[r * BX + NPT];
+                                ezn = eA2[r * BX + NPT];
+                            }
+                        }
+                        else
+                        {
+                            eyn = eA1[r * BX + NPT];
+                            ezn = eA2[r * BX + NPT];
+                        }
 #pragma unroll
                         for (int p = 0; p < NPT; ++p)
                         {
@@ -1374,8 +1396,25 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                     {
                         const Vals<T, NPT> hyr = ldv<NPT>(n1 + r * RW), hyp = ldv<NPT>(p1 + r * RW), hxp = ldv<NPT>(p0 + r * RW);
                         const Vals<T, NPT> e0 = ldv<NPT>(eS0 + r * BX), e1 = ldv<NPT>(eS1 + r * BX), e2 = ldv<NPT>(eS2 + r * BX);
-                        // x - 1 neighbours: the previous point of the pair, or the ring column before it
-                        const T hzw = n2[r * RW - 1], hyw = n1[r * RW - 1];
+                        // x - 1 neighbours: the previous point of the pair, or
+                        // the previous lane's last point (warp shuffle; the
+                        // first lane reads the ring's halo column)
+                        T hzw, hyw;
+                        if constexpr (FFIP_FUSED_SHFL)
+                        {
+                            hzw = __shfl_up_sync(0xffffffffu, hz[r + 1][NPT - 1], 1);
+                            hyw = __shfl_up_sync(0xffffffffu, hyr[NPT - 1], 1);
+                            if (lane == 0)
+                            {
+                                hzw = n2[r * RW - 1];
+                                hyw = n1[r * RW - 1];
+                            }
+                        }
+                        else
+                        {
+                            hzw = n2[r * RW - 1];
+                            hyw = n1[r * RW - 1];
+                        }
                         Vals<T, NPT> ex, ey, ez;
 #pragma unroll
                         for (int p = 0; p < NPT; ++p)
