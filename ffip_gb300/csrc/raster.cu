@@ -189,13 +189,16 @@ struct PointMed
     int key;
 };
 
-__device__ bool point_medium(const RasterArgs &A, int i, int j, int k, PointMed &m)
+// gl / gn: the geometries (in list order) that may contain points of the
+// calling block; gl = nullptr: all of them
+__device__ bool point_medium(const RasterArgs &A, int i, int j, int k, PointMed &m, const int *gl, int gn)
 {
     const double x = coord_of(A, 0, i), y = coord_of(A, 1, j), z = coord_of(A, 2, k);
     const int c = A.c;
     int gi = -1;
-    for (int g = 0; g < A.ng; ++g)
+    for (int q = 0; q < gn; ++q)
     {
+        const int g = gl ? gl[q] : q;
         const RGeom &G = A.geo[g];
         if (i < G.r0[c][0] || i > G.r1[c][0] || j < G.r0[c][1] || j > G.r1[c][1] || k < G.r0[c][2] || k > G.r1[c][2]) continue;
         if (r_inside(G, x, y, z))
@@ -283,9 +286,65 @@ __device__ __forceinline__ void point_of(const RasterArgs &A, int64_t t, int &i,
 
 __device__ __forceinline__ bool is_slot(const RasterArgs &A, const PointMed &m) { return !(m.nb == 0 && m.g == A.g_def); }
 
+// The geometries whose index box meets the index box of the block's 256
+// points (scan order t0 .. t0 + 255), in list order, into gl (capacity
+// kBlockGeoms); returns their count, or -1 when they do not fit (the caller
+// then walks the whole list).  Every thread of the block calls it.
+constexpr int kBlockGeoms = 256;
+__device__ int block_geoms(const RasterArgs &A, int64_t total, int *gl, int *warp_n)
+{
+    const int64_t t0 = blockIdx.x * (int64_t)kRasterThreads, t1 = min(t0 + kRasterThreads, total) - 1;
+    int i0, j0, k0, i1, j1, k1;
+    point_of(A, t0, i0, j0, k0);
+    point_of(A, t1, i1, j1, k1);
+    int lo[3], hi[3];
+    lo[2] = k0;
+    hi[2] = k1;
+    if (k0 == k1 && j0 == j1)
+    {
+        lo[0] = i0, hi[0] = i1, lo[1] = hi[1] = j0;
+    }
+    else
+    {
+        lo[0] = A.first[0], hi[0] = A.first[0] + A.n[0] - 1;
+        if (k0 == k1) lo[1] = j0, hi[1] = j1;
+        else lo[1] = A.first[1], hi[1] = A.first[1] + A.n[1] - 1;
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, c = A.c;
+    int n = 0;
+    for (int base = 0; base < A.ng; base += kRasterThreads)
+    {
+        const int g = base + threadIdx.x;
+        bool hit = false;
+        if (g < A.ng)
+        {
+            const RGeom &G = A.geo[g];
+            hit = true;
+            for (int a = 0; a < 3; ++a) hit = hit && G.r0[c][a] <= hi[a] && G.r1[c][a] >= lo[a] && G.r0[c][a] <= G.r1[c][a];
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (lane == 0) warp_n[wid] = __popc(bal);
+        __syncthreads();
+        int before = 0, all = 0;
+        for (int w = 0; w < kRasterThreads / 32; ++w)
+        {
+            if (w < wid) before += warp_n[w];
+            all += warp_n[w];
+        }
+        if (hit && n + all <= kBlockGeoms) gl[n + before + __popc(bal & ((1u << lane) - 1u))] = g;
+        n += all;
+        __syncthreads();
+        if (n > kBlockGeoms) return -1;
+    }
+    return n;
+}
+
 // pass 1: slot points per block, most active poles, active poles summed
 __global__ void __launch_bounds__(kRasterThreads) k_raster_count(const __grid_constant__ RasterArgs A, int64_t total)
 {
+    __shared__ int gl[kBlockGeoms];
+    __shared__ int warp_n[kRasterThreads / 32];
+    const int gn = block_geoms(A, total, gl, warp_n);
     const int64_t t = blockIdx.x * (int64_t)kRasterThreads + threadIdx.x;
     bool s = false;
     int nb = 0;
@@ -294,7 +353,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster_count(const __grid_co
         int i, j, k;
         point_of(A, t, i, j, k);
         PointMed m;
-        if (!point_medium(A, i, j, k, m)) atomicExch(A.err, 1);
+        if (!point_medium(A, i, j, k, m, gn < 0 ? nullptr : gl, gn < 0 ? A.ng : gn)) atomicExch(A.err, 1);
         else
         {
             s = is_slot(A, m);
@@ -324,6 +383,9 @@ __device__ void write_slot(const RasterArgs &A, int64_t s, const PointMed &m)
 __global__ void __launch_bounds__(kRasterThreads) k_raster_emit(const __grid_constant__ RasterArgs A, int64_t total)
 {
     __shared__ int warp_tot[kRasterThreads / 32];
+    __shared__ int gl[kBlockGeoms];
+    const int gn = block_geoms(A, total, gl, warp_tot);
+    __syncthreads();
     const int64_t t = blockIdx.x * (int64_t)kRasterThreads + threadIdx.x;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     bool s = false;
@@ -332,7 +394,7 @@ __global__ void __launch_bounds__(kRasterThreads) k_raster_emit(const __grid_con
     if (t < total)
     {
         point_of(A, t, i, j, k);
-        s = point_medium(A, i, j, k, m) && is_slot(A, m);
+        s = point_medium(A, i, j, k, m, gn < 0 ? nullptr : gl, gn < 0 ? A.ng : gn) && is_slot(A, m);
     }
     const unsigned bal = __ballot_sync(0xffffffffu, s);
     if (lane == 0) warp_tot[wid] = __popc(bal);
