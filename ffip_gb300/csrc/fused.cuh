@@ -196,8 +196,10 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
 }
 
 // plain paths: x +- 1 neighbours from the adjacent lane by warp shuffle
+// instead of shared memory (off: 5 % slower on the 256^3 workload, the
+// shuffles' registers make both fp32 instances spill)
 #ifndef FFIP_FUSED_SHFL
-#define FFIP_FUSED_SHFL 1
+#define FFIP_FUSED_SHFL 0
 #endif
 
 // fp32 interior instance: E rows with material slots on a tile plane that
