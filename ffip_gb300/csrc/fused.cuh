@@ -195,6 +195,11 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
     }
 }
 
+// CPML instance: a warp covers 16 columns of two tile rows (see k_fused)
+#ifndef FFIP_FUSED_PML_SPLITWARP
+#define FFIP_FUSED_PML_SPLITWARP 0
+#endif
+
 // plain paths: x +- 1 neighbours from the adjacent lane by warp shuffle
 // instead of shared memory (off: 5 % slower on the 256^3 workload, the
 // shuffles' registers make both fp32 instances spill)
@@ -820,7 +825,15 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     const SideParams<T> &PE = F.e;
     const SideParams<T> &PH = F.h;
     const int lane = threadIdx.x, wid = threadIdx.y, tid = wid * 32 + lane;
-    const int r0 = wid * RPT;  // first tile row of this thread
+    // own points of a thread: column ol (NPT points from ol NPT) of tile row
+    // r0 (RPT rows).  SPLITW (the CPML instance, one point and one row per
+    // thread): warp w covers 16 columns of two rows (columns 16 (w & 1) ..,
+    // rows 2 (w >> 1), + 1), so that in a tile whose first half lies in the x
+    // slab the CPML work falls to whole warps instead of half-masked ones;
+    // otherwise warp w covers row w, one column per lane
+    constexpr bool SPLITW = FFIP_FUSED_PML_SPLITWARP && PML && NPT == 1 && RPT == 1 && SH::TX == 32;
+    const int ol = SPLITW ? (lane & 15) + 16 * (wid & 1) : lane;
+    const int r0 = SPLITW ? 2 * (wid >> 1) + (lane >> 4) : wid * RPT;  // first tile row of this thread
     FusedCtx<T, PML> X;
     X.smem = smem;
     X.L = &L;
@@ -981,7 +994,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     }
     }
 
-    const int x = X.x0 + lane * NPT;  // first own point of this thread
+    const int x = X.x0 + ol * NPT;  // first own point of this thread
     // per own row and point: components with a grid point at (x + p, y) that
     // this pass owns
     unsigned vxy[RPT][NPT];
@@ -1003,13 +1016,14 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     __syncthreads();
     const int sz = (int)PE.sz, sy = (int)PE.sy;
     const int own0 = x + (X.y0 + r0) * sy;              // first own point of row r0 at z = 0
-    const int offE = (r0 + 1) * BX + XOFF + lane * NPT;  // first own point of row r0 in an E or H box
-    const int offN = (r0 + 1) * RW + XOFF + lane * NPT;  // first own point of row r0 in an H ring plane
+    const int offE = (r0 + 1) * BX + XOFF + ol * NPT;  // first own point of row r0 in an E or H box
+    const int offN = (r0 + 1) * RW + XOFF + ol * NPT;  // first own point of row r0 in an H ring plane
     const T coefH = PH.coef_def, coefE = PE.coef_def, idh = PH.inv_dx, ide = PE.inv_dx;
     // fp64: the plain path without the 1/dx multiplications when 1/dx is 1
     // (the pass is bound by the fp64 pipe there)
     const bool unit_dx = sizeof(T) == 8 && idh == T(1) && ide == T(1);
-    const unsigned rowmask = ((1u << RPT) - 1u) << r0;
+    // the rows of this thread's warp (the path choices stay warp-uniform)
+    const unsigned rowmask = SPLITW ? 3u << (2 * (wid >> 1)) : ((1u << RPT) - 1u) << r0;
     // fp64: axes x / y (bits 0 / 1) with CPML at the tile's own points, per side
     const unsigned axw = kAxisSpec<T> && PML ? info[LY::NZ] : 0u;
     const int ax_e = (int)(axw & 3u), ax_h = (int)((axw >> 2) & 3u);
@@ -1070,7 +1084,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
 #pragma unroll
                 for (int p = 0; p < NPT; ++p)
                 {
-                    const bool ch[3] = {X.tab(0, 1)[lane * NPT + p + 1].nz(), X.tab(1, 1)[r0 + r + 1].nz(), cz};
+                    const bool ch[3] = {X.tab(0, 1)[ol * NPT + p + 1].nz(), X.tab(1, 1)[r0 + r + 1].nz(), cz};
                     const unsigned vb = vxy[r][p] & (wh >> kInfoZValidShift);
 #pragma unroll
                     for (int c = 0; c < 3; ++c)
@@ -1096,7 +1110,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
 #pragma unroll
                 for (int p = 0; p < NPT; ++p)
                 {
-                    const bool ce[3] = {X.tab(0, 0)[lane * NPT + p + 1].nz(), X.tab(1, 0)[r0 + r + 1].nz(), cz};
+                    const bool ce[3] = {X.tab(0, 0)[ol * NPT + p + 1].nz(), X.tab(1, 0)[r0 + r + 1].nz(), cz};
                     const unsigned vb = vxy[r][p] & (we >> kInfoZValidShift);
 #pragma unroll
                     for (int c = 0; c < 3; ++c)
@@ -1191,7 +1205,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         // next lane's first point (warp shuffle; the last lane
                         // reads the box column after the tile)
                         T eyn, ezn;
-                        if constexpr (FFIP_FUSED_SHFL)
+                        if constexpr (FFIP_FUSED_SHFL && !SPLITW)
                         {
                             eyn = __shfl_down_sync(0xffffffffu, eya[0], 1);
                             ezn = __shfl_down_sync(0xffffffffu, eza[r][0], 1);
@@ -1313,7 +1327,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                             for (int r = 0; r < RPT; ++r)
 #pragma unroll
                                 for (int p = 0; p < NPT; ++p)
-                                    h_own_general<T, PML, false, U, A>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn, 63u, q >= 1, true,
+                                    h_own_general<T, PML, false, U, A>(X, q, r0 + r, ol * NPT + p, eA, eB, hA, rn, 63u, q >= 1, true,
                                                                   false, false, idx + r * sy + p, ph[r][p]);
                         };
                         // fp64: a tile plane with CPML along one axis only
@@ -1340,7 +1354,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         for (int r = 0; r < RPT; ++r)
 #pragma unroll
                             for (int p = 0; p < NPT; ++p)
-                                h_own_general<T, PML, true, U>(X, q, r0 + r, lane * NPT + p, eA, eB, hA, rn,
+                                h_own_general<T, PML, true, U>(X, q, r0 + r, ol * NPT + p, eA, eB, hA, rn,
                                                           vxy[r][p] & (wh >> kInfoZValidShift), q >= 1, pml_h, h_slots, dft_h,
                                                           idx + r * sy + p, ph[r][p]);
                     }
@@ -1402,7 +1416,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         // the previous lane's last point (warp shuffle; the
                         // first lane reads the ring's halo column)
                         T hzw, hyw;
-                        if constexpr (FFIP_FUSED_SHFL)
+                        if constexpr (FFIP_FUSED_SHFL && !SPLITW)
                         {
                             hzw = __shfl_up_sync(0xffffffffu, hz[r + 1][NPT - 1], 1);
                             hyw = __shfl_up_sync(0xffffffffu, hyr[NPT - 1], 1);
@@ -1513,7 +1527,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                 pe[c][1] = *stage_slot(r, p, c, 1);
                             }
                         }
-                        const int xi = lane * NPT + p;
+                        const int xi = ol * NPT + p;
                         auto general_e_own = [&](auto unit) {
                             constexpr bool U = decltype(unit)::value;
                             if (lean_e)
