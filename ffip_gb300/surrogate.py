@@ -378,6 +378,7 @@ def train(net, rho, y, epochs=50, batch=32, lr=1e-3, seed=0, log=None):
             opt.step()
             tot += float(loss.detach()) * len(idx)
         hist.append(tot / len(order))
+        check()  # a tcgen05 GEMM that gave up on a bounded wait fails the epoch
         if log:
             torch.cuda.synchronize()
             log("epoch %d loss %.5f (%.1f s)" % (ep, hist[-1], time.perf_counter() - t0))
@@ -392,6 +393,7 @@ def predict(net, rho, scale, batch=64):
     with torch.no_grad():
         for i in range(0, len(rho), batch):
             out.append(net(torch.tensor(np.asarray(rho[i:i + batch], dtype=np.float32), device=dev)).cpu().numpy() * scale)
+    check()
     return np.concatenate(out)
 
 

@@ -81,3 +81,33 @@ def test_adjoint_design_density_update_equals_the_host_rasterisation():
             sums[r] = (first, s.media_info()[0])
     assert sums["host"] == sums["device"]
     assert sums["host"][0] != sums["host"][1]
+
+
+def test_density_box_with_more_candidate_poles_falls_back_to_the_host():
+    """A general medium box whose medium table uses more distinct poles (13)
+    than the device rasterisation's candidate list holds (12) -- each table
+    entry two of them, so a point has at most four -- is rasterised on the
+    host under "auto", with the same outputs as "host", and "device" refuses
+    it with a clear error."""
+    from ffip_gb300 import native
+    cfg, ds, _ = load("density_boxes")
+    cfg, ds = copy.deepcopy(cfg), dict(ds)
+    box = [g for g in cfg["geometry"] if g["type"] == "general medium box"][0]
+    npole, nfun = 13, len(ds[box["density function dataset"]])
+    box["medium"]["electric susceptibility"] = [
+        {"type": "Lorentz", "frequency": 0.1 + 0.01 * t, "gamma": 0.02, "amplitude": 1.0} for t in range(npole)]
+    amp = np.zeros((nfun, npole))
+    for i in range(nfun):
+        amp[i, i % npole] = 0.5
+        amp[i, (i + 2) % npole] = 0.25
+    ds[box["electric susceptibility amplitudes dataset"]] = amp.ravel()
+    outs = {}
+    for r in ("auto", "host"):
+        with make(cfg, ds, r, "fp64") as s:
+            assert not s.media_info()[1]
+            s.run(cfg["stop condition"])
+            outs[r] = flatten(s.outputs())
+    for k in outs["host"]:
+        assert np.array_equal(outs["host"][k], outs["auto"][k]), k
+    with pytest.raises(native.FfipError, match="device rasterisation"):
+        make(cfg, ds, "device", "fp64")
