@@ -355,14 +355,26 @@ def generate(n, seed=0, workload: Optional[DesignWorkload] = None):
     return rho.astype(np.float32), y, time.perf_counter() - t0
 
 
-def train(net, rho, y, epochs=50, batch=32, lr=1e-3, seed=0, log=None):
-    """Adam on the mean squared error of the label-normalised outputs."""
+def spot_weights(shape, spot=8, weight=0.0):
+    """Per-pixel loss weights of an output plane: 1, and 1 + weight in the
+    central spot x spot cells (the region the design objective reads),
+    normalised to mean 1."""
+    w = np.ones(shape[-2:], dtype=np.float32)
+    c0, c1 = shape[-2] // 2 - spot // 2, shape[-1] // 2 - spot // 2
+    w[c0:c0 + spot, c1:c1 + spot] += weight
+    return w / w.mean()
+
+
+def train(net, rho, y, epochs=50, batch=32, lr=1e-3, seed=0, log=None, spot_weight=0.0):
+    """Adam on the mean squared error of the label-normalised outputs
+    (spot_weight > 0: the central spot's pixels weigh 1 + spot_weight)."""
     torch = _torch()
     dev = torch.device("cuda")
     net.to(dev)
     scale = float(np.sqrt(np.mean(y ** 2))) or 1.0
     X = torch.tensor(rho, device=dev)
     Y = torch.tensor(y / scale, device=dev)
+    W = torch.tensor(spot_weights(y.shape, weight=spot_weight), device=dev)
     opt = torch.optim.Adam(net.parameters(), lr=lr)
     g = np.random.default_rng(seed)
     hist = []
@@ -372,7 +384,7 @@ def train(net, rho, y, epochs=50, batch=32, lr=1e-3, seed=0, log=None):
         tot = 0.0
         for i in range(0, len(order), batch):
             idx = torch.tensor(order[i:i + batch], device=dev)
-            loss = torch.mean((net(X[idx]) - Y[idx]) ** 2)
+            loss = torch.mean(W * (net(X[idx]) - Y[idx]) ** 2)
             opt.zero_grad(set_to_none=True)
             loss.backward()
             opt.step()
@@ -423,9 +435,10 @@ class OnlineRefiner:
     (together with as many samples of the training set) follow, so that the
     network learns the neighbourhood the loop moves through."""
 
-    def __init__(self, net, wl, scale, train_rho, train_y, steps=8, window=16, lr=1e-3, seed=0):
+    def __init__(self, net, wl, scale, train_rho, train_y, steps=8, window=16, lr=1e-3, seed=0, spot_weight=0.0):
         torch = _torch()
         self.net, self.wl, self.scale, self.steps, self.window = net, wl, scale, steps, window
+        self.W = torch.tensor(spot_weights(train_y.shape, weight=spot_weight), device=torch.device("cuda"))
         self.rho, self.y = train_rho, train_y
         self.opt = torch.optim.Adam(net.parameters(), lr=lr)
         self.buf_x, self.buf_y = [], []
@@ -444,7 +457,7 @@ class OnlineRefiner:
             idx = self.rng.integers(0, len(self.rho), size=len(bx))
             X = torch.tensor(np.concatenate([bx, self.rho[idx]]), device=dev)
             Y = torch.tensor(np.concatenate([by, self.y[idx] / self.scale]), device=dev)
-            loss = torch.mean((self.net(X) - Y) ** 2)
+            loss = torch.mean(self.W * (self.net(X) - Y) ** 2)
             self.opt.zero_grad(set_to_none=True)
             loss.backward()
             self.opt.step()
@@ -519,7 +532,7 @@ def design_loop(prob, x0, steps, mode, net=None, scale=1.0, max_accepted=8, targ
             "objective": trace, "runs_at_accepted": runs_at, "reached": target is None or F <= target}
 
 
-def compare_loops(wl, net, scale, iters=8, candidates=8, seed=0, log=None, train_rho=None, train_y=None):
+def compare_loops(wl, net, scale, iters=8, candidates=8, seed=0, log=None, train_rho=None, train_y=None, spot_weight=0.0):
     """Plain loop for `iters` accepted steps; its final objective is the
     target of the screened loop (trained network; refined online on the
     loop's own runs when the training set is given) and of the same loop
@@ -535,7 +548,7 @@ def compare_loops(wl, net, scale, iters=8, candidates=8, seed=0, log=None, train
                                   max_iters=12 * iters)
     if train_rho is not None:
         net2 = copy.deepcopy(net)
-        ref = OnlineRefiner(net2, wl, scale, train_rho, train_y, seed=seed)
+        ref = OnlineRefiner(net2, wl, scale, train_rho, train_y, seed=seed, spot_weight=spot_weight)
         res["screened_online"] = design_loop(prob, x0, steps, "screened", net2, scale, max_accepted=4 * iters, target=target,
                                              max_iters=12 * iters, observe=ref)
         res["screened_online"]["refine_seconds"] = ref.seconds
