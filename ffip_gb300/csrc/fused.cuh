@@ -202,8 +202,10 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
 #endif
 
 // plain paths: x +- 1 neighbours from the adjacent lane by warp shuffle
-// instead of shared memory (off: 5 % slower on the 256^3 workload, the
-// shuffles' registers make both fp32 instances spill)
+// instead of shared memory, per instance: bit 0 the fp32 interior instance,
+// bit 1 the fp32 CPML instance, bit 2 the fp64 interior instance, bit 3 the
+// fp64 CPML instance (both fp32 instances together: 5 % slower on the 256^3
+// workload, the shuffles' registers make them spill)
 #ifndef FFIP_FUSED_SHFL
 #define FFIP_FUSED_SHFL 0
 #endif
@@ -834,6 +836,8 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     // otherwise warp w covers row w, one column per lane
     constexpr bool SPLITW = (FFIP_FUSED_PML_SPLITWARP == 1 || (FFIP_FUSED_PML_SPLITWARP == 2 && sizeof(T) == 8)) && PML &&
                             NPT == 1 && RPT == 1 && SH::TX == 32;
+    // warp-shuffle neighbours in this instance (lanes along x: not with SPLITW)
+    constexpr bool SHFL = ((FFIP_FUSED_SHFL >> ((sizeof(T) == 8 ? 2 : 0) + (PML ? 1 : 0))) & 1) && !SPLITW;
     const int ol = SPLITW ? (lane & 15) + 16 * (wid & 1) : lane;
     const int r0 = SPLITW ? 2 * (wid >> 1) + (lane >> 4) : wid * RPT;  // first tile row of this thread
     FusedCtx<T, PML> X;
@@ -1207,7 +1211,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         // next lane's first point (warp shuffle; the last lane
                         // reads the box column after the tile)
                         T eyn, ezn;
-                        if constexpr (FFIP_FUSED_SHFL && !SPLITW)
+                        if constexpr (SHFL)
                         {
                             eyn = __shfl_down_sync(0xffffffffu, eya[0], 1);
                             ezn = __shfl_down_sync(0xffffffffu, eza[r][0], 1);
@@ -1418,7 +1422,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         // the previous lane's last point (warp shuffle; the
                         // first lane reads the ring's halo column)
                         T hzw, hyw;
-                        if constexpr (FFIP_FUSED_SHFL && !SPLITW)
+                        if constexpr (SHFL)
                         {
                             hzw = __shfl_up_sync(0xffffffffu, hz[r + 1][NPT - 1], 1);
                             hyw = __shfl_up_sync(0xffffffffu, hyr[NPT - 1], 1);
