@@ -221,11 +221,11 @@ void Engine<T>::media()
             init_media_device();
             return;
         }
-        catch (const std::runtime_error &e)
+        catch (const RasterUnsupported &)
         {
             // a geometry the device rasterisation does not cover ("auto"
             // falls back to the host)
-            if (P_.rasterize == "device" || std::string(e.what()).rfind("device rasterisation:", 0) != 0) throw;
+            if (P_.rasterize == "device") throw;
         }
     }
     if (P_.rasterize != "host") rasterize_media(P_);

@@ -43,6 +43,13 @@ struct DeviceTimeout : std::runtime_error
     using std::runtime_error::runtime_error;
 };
 
+// The device rasterisation does not cover a geometry of the plan (the
+// engine then rasterises on the host unless "device" was asked for).
+struct RasterUnsupported : std::runtime_error
+{
+    using std::runtime_error::runtime_error;
+};
+
 // The divergence check found non-finite field values.
 struct Diverged : std::runtime_error
 {

@@ -545,8 +545,8 @@ void raster_media(const Plan &P, bool fp32, const std::function<void *(size_t)> 
                 if (nz) cand.push_back((int)q);
             }
             if ((int)cand.size() > kMaxCand)
-                throw std::runtime_error("device rasterisation: a density box with more than " + std::to_string(kMaxCand) +
-                                         " distinct poles");
+                throw RasterUnsupported("device rasterisation: a density box with more than " + std::to_string(kMaxCand) +
+                                        " distinct poles");
             R.ncand = (int)cand.size();
             for (int t = 0; t < R.ncand; ++t) R.cand[t] = cand[t];
             auto amp_of = [&](const std::vector<double> &a, int q) { return q < (int)a.size() ? a[q] : 0.0; };
@@ -648,7 +648,7 @@ void raster_media(const Plan &P, bool fp32, const std::function<void *(size_t)> 
             }
             if (!total) continue;
             const int64_t nblk = (total + kRasterThreads - 1) / kRasterThreads;
-            if (nblk > INT_MAX) throw std::runtime_error("device rasterisation: grid too large");
+            if (nblk > INT_MAX) throw RasterUnsupported("device rasterisation: grid too large");
             int *d_count = S.get<int>(nblk);
             int64_t *d_off = S.get<int64_t>(nblk);
             ck(cudaMemsetAsync(d_err, 0, sizeof(int), st), "cudaMemset");
