@@ -88,6 +88,7 @@ private:
     SideParams<T> sp_[2];
     SourceParams<T> srcp_[2];
     GhostParams<T> gp_{};
+    GhostParams<T> gph_{};  // the H faces of gp_ (the fused pass fills them between its halves)
     bool fused_{false};
     int64_t ts_{0};
     int64_t nlaunch_{0};
@@ -173,14 +174,12 @@ void Engine<T>::init()
     // the media: slot tables on the device (rasterised there, or uploaded
     // from the host's rasterisation)
     media();
-    // fused pass eligibility (None boundaries everywhere, no magnetic poles)
-    bool none_bc = true;
-    for (int a = 0; a < 3; ++a) none_bc = none_bc && P_.bc[a][0] == BC_NONE && P_.bc[a][1] == BC_NONE;
+    // fused pass eligibility (no magnetic poles)
     bool mag_poles = false;
     for (int c = 3; c < 6; ++c) mag_poles = mag_poles || comp_poles_[c];
-    const bool eligible = none_bc && !mag_poles && be_->has_fused();
+    const bool eligible = !mag_poles && be_->has_fused();
     if (P_.engine == "fused" && !eligible)
-        throw std::runtime_error("engine \"fused\" requested but the fused pass needs None boundaries on every face, no magnetic poles and a CUDA backend");
+        throw std::runtime_error("engine \"fused\" requested but the fused pass needs a grid without magnetic poles and a CUDA backend");
     if (P_.engine != "auto" && P_.engine != "fused" && P_.engine != "unfused")
         throw std::runtime_error("engine must be \"auto\", \"fused\" or \"unfused\"");
     fused_ = eligible && P_.engine != "unfused";
@@ -636,6 +635,11 @@ void Engine<T>::init_ghosts()
     gp_.nfaces = nf;
     gp_.sy = P_.Mx_pad;
     gp_.sz = P_.plane();
+    gph_ = GhostParams<T>();
+    gph_.sy = gp_.sy;
+    gph_.sz = gp_.sz;
+    for (int f = 0; f < nf; ++f)
+        if (gp_.faces[f].comp >= 3) gph_.faces[gph_.nfaces++] = gp_.faces[f];
 }
 
 template <typename T>
@@ -837,7 +841,8 @@ void Engine<T>::one_step()
         }
         fp.wait_ns = P_.fused_wait_ns;
         fp.stall_test = P_.fused_stall_test ? 1 : 0;
-        nlaunch_ += be_->fused(fp);
+        for (int c = 0; c < 6; ++c) gph_.f[c] = buf_[nx][c];
+        nlaunch_ += be_->fused(fp, gph_.nfaces ? &gph_ : nullptr);
         cur_ = nx;
         for (int c = 0; c < 3; ++c)
         {

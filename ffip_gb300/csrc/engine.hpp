@@ -82,9 +82,11 @@ struct Backend
     virtual void update(const SideParams<double> &p, bool is_e) = 0;
     virtual void update(const SideParams<float> &p, bool is_e) = 0;
     virtual bool has_fused() const { return false; }
-    // one fused time step; returns the number of kernels it launched
-    virtual int fused(const FusedParams<double> &) { return 0; }
-    virtual int fused(const FusedParams<float> &) { return 0; }
+    // one fused time step; returns the number of kernels it launched.
+    // hghost (may be null): the H ghost faces (PEC / PMC / periodic), filled
+    // in the new H between the pass and the E points that read them
+    virtual int fused(const FusedParams<double> &, const GhostParams<double> *) { return 0; }
+    virtual int fused(const FusedParams<float> &, const GhostParams<float> *) { return 0; }
     virtual void sources(const SourceParams<double> &p) = 0;
     virtual void sources(const SourceParams<float> &p) = 0;
     virtual void ghosts(const GhostParams<double> &p) = 0;

@@ -25,8 +25,8 @@
 // new one, field buffers (and the H-side CPML psi) ping-pong between steps;
 // E-side CPML psi and polarisation state are only touched by their owner and
 // are updated in place.  Each chunk starts by recomputing H of the plane
-// below it (no writes).  Used with "None" boundaries on every face and no
-// magnetic poles (the engine checks this).
+// below it (no writes).  Used on grids without magnetic poles (the engine
+// checks this).
 //
 // Two code paths per side and plane.  The common one (a tile plane with no
 // CPML, no material slot, no DFT unit, every point valid) is the plain curl
@@ -44,6 +44,12 @@
 // When the valid x (y) extent exceeds a whole number of tiles by one or two
 // points, those last layers are left to k_face (two small launches after this
 // pass: H then E), so that no CTA is spent on a nearly empty tile.
+//
+// PEC / PMC / periodic faces: the E layers whose curl reads an H ghost plane
+// (the ghost holds the mirror / periodic image of the new H) are left to the
+// E half of k_face too, which runs after the H ghost planes of the new level
+// are filled; the pass reads E ghost planes of step n as loaded (filled at
+// the end of the previous step), so the H update needs nothing else.
 //
 // The per-point arithmetic is the same as the separate H/E kernels
 // (stencil.cuh: pml_term, material_at, dft_point), so both passes give the
@@ -196,7 +202,7 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
 }
 
 // CPML instance: a warp covers 16 columns of two tile rows (see k_fused);
-// 2 (default): in fp64 only (1.4 % faster there, 2 % slower in fp32)
+// 1: in both precisions; 2 (default): in fp64 only
 #ifndef FFIP_FUSED_PML_SPLITWARP
 #define FFIP_FUSED_PML_SPLITWARP 2
 #endif
@@ -334,6 +340,11 @@ struct FusedLaunch
     int xlim, ylim;       // this pass updates 1 <= x < xlim, 1 <= y < ylim; k_face the rest
     int xend, yend;       // valid extents (max over components of vhi + 1)
     int kbeg, kend;       // valid z range
+    // E points of component c this pass owns along axis a: elo[c][a] ..
+    // ehi[c][a], the valid range less the layers whose curl reads a ghost H
+    // (PEC / PMC / periodic faces): k_face updates those after the H ghost
+    // planes are refreshed
+    int elo[3][3], ehi[3][3];
     const int4 *jobs;     // per CTA: x0, y0, k0, k1 (tile origin and owned z planes)
 };
 
@@ -830,16 +841,23 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     const int lane = threadIdx.x, wid = threadIdx.y, tid = wid * 32 + lane;
     // own points of a thread: column ol (NPT points from ol NPT) of tile row
     // r0 (RPT rows).  SPLITW (the CPML instance, one point and one row per
-    // thread): warp w covers 16 columns of two rows (columns 16 (w & 1) ..,
-    // rows 2 (w >> 1), + 1), so that in a tile whose first half lies in the x
-    // slab the CPML work falls to whole warps instead of half-masked ones;
+    // thread): warp w covers 16 columns of two rows (columns 16 (w & 1) ..),
+    // so that in a tile whose first half lies in the x slab the CPML work
+    // falls to whole warps instead of half-masked ones; in fp64 rows
+    // 2 (w >> 1) and 2 (w >> 1) + 1, in fp32 rows (w >> 1) and (w >> 1) + 4
+    // (shared-memory rows of 36 words: four rows apart, the two half-warps
+    // fall on disjoint banks; adjacent rows would overlap on 12 of them);
     // otherwise warp w covers row w, one column per lane
     constexpr bool SPLITW = (FFIP_FUSED_PML_SPLITWARP == 1 || (FFIP_FUSED_PML_SPLITWARP == 2 && sizeof(T) == 8)) && PML &&
                             NPT == 1 && RPT == 1 && SH::TX == 32;
     // warp-shuffle neighbours in this instance (lanes along x: not with SPLITW)
     constexpr bool SHFL = ((FFIP_FUSED_SHFL >> ((sizeof(T) == 8 ? 2 : 0) + (PML ? 1 : 0))) & 1) && !SPLITW;
     const int ol = SPLITW ? (lane & 15) + 16 * (wid & 1) : lane;
-    const int r0 = SPLITW ? 2 * (wid >> 1) + (lane >> 4) : wid * RPT;  // first tile row of this thread
+    constexpr int SPLIT_RS = sizeof(T) == 4 ? 4 : 1;  // SPLITW: rows of a warp this far apart
+    static_assert(!SPLITW || sizeof(T) == 8 || (SH::RW % 32 == 4 && SH::BX % 32 == 4 && SH::TY == 8),
+                  "fp32 split warps: the row pairing assumes rows of 36 words and 8-row tiles");
+    const int r0 = SPLITW ? (SPLIT_RS == 1 ? 2 * (wid >> 1) : (wid >> 1)) + SPLIT_RS * (lane >> 4)
+                          : wid * RPT;  // first tile row of this thread
     FusedCtx<T, PML> X;
     X.smem = smem;
     X.L = &L;
@@ -935,7 +953,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
         unsigned w = 0;
         for (int c = 0; c < 3; ++c)
         {
-            if (k >= PE.vlo[c][2] && k <= PE.vhi[c][2]) w |= 1u << (kInfoZValidShift + c);
+            if (k >= L.elo[c][2] && k <= L.ehi[c][2]) w |= 1u << (kInfoZValidShift + c);
             if (k >= PH.vlo[c][2] && k <= PH.vhi[c][2]) w |= 1u << (kInfoZValidShift + 3 + c);
         }
         if (pml_tables && k >= 0 && k < PE.Mz && (ld_keep(PE.pc[2][0] + k, keep) != T(0) || ld_keep(PE.pc[2][1] + k, keep) != T(0)))
@@ -982,7 +1000,8 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
         inside = inside && PE.vlo[c][0] <= X.x0 - (zcol ? 0 : 1) && X.x0 + TX - 1 <= PE.vhi[c][0] &&
                  PE.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PE.vhi[c][1] &&
                  PH.vlo[c][0] <= X.x0 - (zcol ? 0 : 1) && X.x0 + TX - 1 <= PH.vhi[c][0] &&
-                 PH.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PH.vhi[c][1];
+                 PH.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PH.vhi[c][1] && L.elo[c][0] <= X.x0 &&
+                 X.x0 + TX - 1 <= L.ehi[c][0] && L.elo[c][1] <= X.y0 && X.y0 + TY - 1 <= L.ehi[c][1];
     // per plane: may each side take the plain path; kInfoZPml becomes "CPML
     // at this tile plane" (the tile's x / y tables or the plane's z)
     for (int o = pt; o < LY::NZ; o += PT)
@@ -1014,7 +1033,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
             if (xp < L.xlim && y < L.ylim)
                 for (int c = 0; c < 3; ++c)
                 {
-                    if (xp >= PE.vlo[c][0] && xp <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1]) vxy[r][p] |= 1u << c;
+                    if (xp >= L.elo[c][0] && xp <= L.ehi[c][0] && y >= L.elo[c][1] && y <= L.ehi[c][1]) vxy[r][p] |= 1u << c;
                     if (xp >= PH.vlo[c][0] && xp <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1])
                         vxy[r][p] |= 1u << (3 + c);
                 }
@@ -1029,7 +1048,9 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     // (the pass is bound by the fp64 pipe there)
     const bool unit_dx = sizeof(T) == 8 && idh == T(1) && ide == T(1);
     // the rows of this thread's warp (the path choices stay warp-uniform)
-    const unsigned rowmask = SPLITW ? 3u << (2 * (wid >> 1)) : ((1u << RPT) - 1u) << r0;
+    const unsigned rowmask = !SPLITW ? ((1u << RPT) - 1u) << r0
+                             : SPLIT_RS == 1 ? 3u << (2 * (wid >> 1))
+                                             : (1u << (wid >> 1)) | (1u << ((wid >> 1) + 4));
     // fp64: axes x / y (bits 0 / 1) with CPML at the tile's own points, per side
     const unsigned axw = kAxisSpec<T> && PML ? info[LY::NZ] : 0u;
     const int ax_e = (int)(axw & 3u), ax_h = (int)((axw >> 2) & 3u);
@@ -1637,40 +1658,38 @@ __device__ __forceinline__ void face_point(const FusedParams<T> &F, int i, int j
     if (p.nunits) dft_point<T>(p.nunits, p.units, p.phase, GC, i, j, k, (double)v, (double)vd);
 }
 
-// The points with x >= xlim (all y) or y >= ylim (x < xlim), all z
-template <typename T, bool IS_E>
-__global__ void k_face(const __grid_constant__ FusedLaunch<T> L)
+// The points of one side that the pass does not own, as boxes of one
+// component each (built on the host): x >= xlim or y >= ylim, and for E the
+// layers whose curl reads a ghost H
+struct FaceBox
 {
-    const FusedParams<T> &F = L.fp;
-    const SideParams<T> &p = IS_E ? F.e : F.h;
+    int comp;       // component of the side, 0..2
+    int i0, ni;     // x range
+    int j0, nj;     // y range
+    int k0;         // first z plane (the box's count follows from the next start)
+    int64_t start;  // index of the box's first point in the list
+};
+constexpr int kMaxFaceBoxes = 18;  // 3 components x 6 sides of a box difference
+struct FaceList
+{
+    int n;
+    int64_t total;
+    FaceBox b[kMaxFaceBoxes];
+};
+
+template <typename T, bool IS_E>
+__global__ void k_face(const __grid_constant__ FusedLaunch<T> L, const __grid_constant__ FaceList B)
+{
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int wA = L.xend - L.xlim, hB = L.yend - L.ylim;
-    const int64_t nA = (int64_t)wA * L.yend * p.Mz, nB = (int64_t)L.xlim * hB * p.Mz;
-    int i, j, k;
-    if (t < nA)
-    {
-        i = L.xlim + (int)(t % wA);
-        j = (int)((t / wA) % L.yend);
-        k = (int)(t / ((int64_t)wA * L.yend));
-    }
-    else if (t < nA + nB)
-    {
-        const int64_t u = t - nA;
-        i = (int)(u % L.xlim);
-        j = L.ylim + (int)((u / L.xlim) % hB);
-        k = (int)(u / ((int64_t)L.xlim * hB));
-    }
-    else
-        return;
-    constexpr int B = IS_E ? 0 : 3;
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-    {
-        if (i < p.vlo[c][0] || i > p.vhi[c][0] || j < p.vlo[c][1] || j > p.vhi[c][1] || k < p.vlo[c][2] || k > p.vhi[c][2])
-            continue;
-        if (c == 0) face_point<T, B + 0>(F, i, j, k);
-        else if (c == 1) face_point<T, B + 1>(F, i, j, k);
-        else face_point<T, B + 2>(F, i, j, k);
-    }
+    if (t >= B.total) return;
+    int b = 0;
+    while (b + 1 < B.n && t >= B.b[b + 1].start) ++b;
+    const FaceBox &X = B.b[b];
+    const int64_t u = t - X.start, r = u / X.ni;
+    const int i = X.i0 + (int)(u - r * X.ni), j = X.j0 + (int)(r % X.nj), k = X.k0 + (int)(r / X.nj);
+    constexpr int C0 = IS_E ? 0 : 3;
+    if (X.comp == 0) face_point<T, C0 + 0>(L.fp, i, j, k);
+    else if (X.comp == 1) face_point<T, C0 + 1>(L.fp, i, j, k);
+    else face_point<T, C0 + 2>(L.fp, i, j, k);
 }
 } // namespace ffipg

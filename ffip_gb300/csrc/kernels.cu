@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 #include <map>
 #include <memory>
@@ -331,7 +332,7 @@ public:
     bool has_fused() const override { return true; }
 
     template <typename T>
-    int fused_t(const FusedParams<T> &p)
+    int fused_t(const FusedParams<T> &p, const GhostParams<T> *hg)
     {
         use();
         // interior instance (SH: its tiles define the column grid) and CPML
@@ -430,12 +431,43 @@ public:
         LC.yend = L.yend;
         LC.kbeg = L.kbeg;
         LC.kend = L.kend;
+        // E points the pass owns: the valid range less the layers whose curl
+        // reads an H ghost plane of hg (E component c reads H component
+        // (c + 2) % 3 along axis (c + 1) % 3 and (c + 1) % 3 along (c + 2) % 3,
+        // at its own index and the one below); ghost planes lie outside the
+        // valid H range, so those layers are the first / last of the range
+        const bool ghost = hg && hg->nfaces > 0;
+        for (int c = 0; c < 3; ++c)
+            for (int a = 0; a < 3; ++a)
+            {
+                L.elo[c][a] = LC.elo[c][a] = p.e.vlo[c][a];
+                L.ehi[c][a] = LC.ehi[c][a] = p.e.vhi[c][a];
+            }
+        for (int f = 0; ghost && f < hg->nfaces; ++f)
+        {
+            const GhostFace &G = hg->faces[f];
+            const int ch = G.comp - 3, a = G.axis;
+            for (int c = 0; c < 3; ++c)
+            {
+                if (!((ch == (c + 2) % 3 && a == (c + 1) % 3) || (ch == (c + 1) % 3 && a == (c + 2) % 3))) continue;
+                for (int i = G.dst; i <= G.dst + 1; ++i)
+                {
+                    int &lo = L.elo[c][a], &hi = L.ehi[c][a];
+                    if (i < lo || i > hi) continue;
+                    if (i == lo) ++lo;
+                    else if (i == hi) --hi;
+                    else throw std::runtime_error("fused pass: a ghost plane inside the grid");
+                }
+            }
+        }
+        std::memcpy(LC.elo, L.elo, sizeof L.elo);
+        std::memcpy(LC.ehi, L.ehi, sizeof L.ehi);
+        const FaceList fl_h = face_list(p.h, nullptr, nullptr, L.xlim, L.ylim);
+        const FaceList fl_e = face_list(p.e, L.elo, L.ehi, L.xlim, L.ylim);
         int n = 0;
-        const int64_t nface = ((int64_t)(L.xend - L.xlim) * L.yend + (int64_t)L.xlim * (L.yend - L.ylim)) * p.e.Mz;
-        const unsigned face_blocks = (unsigned)((nface + 255) / 256);
         // a second stream runs the interior instance beside the CPML one, and
         // the H half of k_face (it reads only step-n fields) beside both
-        const bool fork = (J.ni > 0 && J.nb > 0) || nface > 0;
+        const bool fork = (J.ni > 0 && J.nb > 0) || fl_h.total > 0;
         if (fork)
         {
             if (!side_)
@@ -470,9 +502,9 @@ public:
         }
         // the H half of k_face reads only step-n fields: first on the side
         // stream, ahead of the interior instance
-        if (nface > 0)
+        if (fl_h.total > 0)
         {
-            k_face<T, false><<<face_blocks, 256, 0, side_>>>(L);
+            k_face<T, false><<<(unsigned)((fl_h.total + 255) / 256), 256, 0, side_>>>(L, fl_h);
             check(cudaGetLastError(), "k_face launch");
             check(cudaEventRecord(face_h_, side_), "cudaEventRecord");
             ++n;
@@ -494,11 +526,14 @@ public:
         // E of the face layers reads the new H of the face layers and of the
         // tiles next to them; when those tiles are all CPML jobs it follows the
         // CPML instance on the main stream, beside the interior instance
-        const bool early_face = nface > 0 && J.nb > 0 && J.face_in_pml;
+        // (not with ghost faces: the E layers next to them wait for the
+        // ghost planes, which need every H of the step)
+        const unsigned e_blocks = (unsigned)((fl_e.total + 255) / 256);
+        const bool early_face = fl_e.total > 0 && J.nb > 0 && J.face_in_pml && !ghost;
         if (early_face)
         {
-            check(cudaStreamWaitEvent(stream_, face_h_, 0), "cudaStreamWaitEvent");
-            k_face<T, true><<<face_blocks, 256, 0, stream_>>>(L);
+            if (fl_h.total > 0) check(cudaStreamWaitEvent(stream_, face_h_, 0), "cudaStreamWaitEvent");
+            k_face<T, true><<<e_blocks, 256, 0, stream_>>>(L, fl_e);
             check(cudaGetLastError(), "k_face launch");
             ++n;
         }
@@ -508,16 +543,83 @@ public:
             check(cudaStreamWaitEvent(stream_, join_, 0), "cudaStreamWaitEvent");
         }
         if (pass_end) check(cudaEventRecord(pass_end, stream_), "cudaEventRecord");
-        if (nface > 0 && !early_face)
+        if (ghost)
         {
-            k_face<T, true><<<face_blocks, 256, 0, stream_>>>(L);
+            ghosts_t(*hg);
+            ++n;
+        }
+        if (fl_e.total > 0 && !early_face)
+        {
+            k_face<T, true><<<e_blocks, 256, 0, stream_>>>(L, fl_e);
             check(cudaGetLastError(), "k_face launch");
             ++n;
         }
         return n;
     }
-    int fused(const FusedParams<double> &p) override { return fused_t(p); }
-    int fused(const FusedParams<float> &p) override { return fused_t(p); }
+    int fused(const FusedParams<double> &p, const GhostParams<double> *hg) override { return fused_t(p, hg); }
+    int fused(const FusedParams<float> &p, const GhostParams<float> *hg) override { return fused_t(p, hg); }
+
+    // The points of one side's components that the fused pass does not own,
+    // as disjoint boxes: the valid range V less the owned box W (x < xlim,
+    // y < ylim and, for E, the range elo .. ehi), cut along x, then y, then z
+    template <typename T>
+    static FaceList face_list(const SideParams<T> &S, const int (*lo_own)[3], const int (*hi_own)[3], int xlim, int ylim)
+    {
+        FaceList B{};
+        for (int c = 0; c < 3; ++c)
+        {
+            int v0[3], v1[3], w0[3], w1[3];
+            bool vempty = false, wempty = false;
+            for (int a = 0; a < 3; ++a)
+            {
+                v0[a] = S.vlo[c][a];
+                v1[a] = S.vhi[c][a];
+                w0[a] = lo_own ? std::max(v0[a], lo_own[c][a]) : v0[a];
+                w1[a] = hi_own ? std::min(v1[a], hi_own[c][a]) : v1[a];
+                if (a == 0) w1[a] = std::min(w1[a], xlim - 1);
+                if (a == 1) w1[a] = std::min(w1[a], ylim - 1);
+                vempty = vempty || v1[a] < v0[a];
+                wempty = wempty || w1[a] < w0[a];
+            }
+            if (vempty) continue;
+            auto add = [&](const int (&b0)[3], const int (&b1)[3]) {
+                if (B.n == kMaxFaceBoxes) throw std::runtime_error("fused pass: too many face boxes");
+                FaceBox &X = B.b[B.n++];
+                X.comp = c;
+                X.i0 = b0[0];
+                X.ni = b1[0] - b0[0] + 1;
+                X.j0 = b0[1];
+                X.nj = b1[1] - b0[1] + 1;
+                X.k0 = b0[2];
+                X.start = B.total;
+                B.total += (int64_t)X.ni * X.nj * (b1[2] - b0[2] + 1);
+            };
+            if (wempty)
+            {
+                add(v0, v1);
+                continue;
+            }
+            int lo[3] = {v0[0], v0[1], v0[2]}, hi[3] = {v1[0], v1[1], v1[2]};
+            for (int a = 0; a < 3; ++a)
+            {
+                if (w0[a] > lo[a])
+                {
+                    int b0[3] = {lo[0], lo[1], lo[2]}, b1[3] = {hi[0], hi[1], hi[2]};
+                    b1[a] = w0[a] - 1;
+                    add(b0, b1);
+                }
+                if (w1[a] < hi[a])
+                {
+                    int b0[3] = {lo[0], lo[1], lo[2]}, b1[3] = {hi[0], hi[1], hi[2]};
+                    b0[a] = w1[a] + 1;
+                    add(b0, b1);
+                }
+                lo[a] = w0[a];
+                hi[a] = w1[a];
+            }
+        }
+        return B;
+    }
 
     // CTA jobs of the fused pass (x0, y0, k0, k1): the jobs whose tile, halo
     // and planes touch a CPML point first (nb of them), then the others (ni).

@@ -7,7 +7,7 @@
 // 907-1023).  Here every component gets its own dense array, all six with the
 // same shape (Mx_pad, My, Mz), x fastest.  Along an axis whose doubled range
 // is [lo, hi], let o = lo rounded down to even and f the axis's first index
-// (kXFirst = 4 along x, 1 along y and z); array index i holds the
+// (kXFirst along x, 1 along y and z); array index i holds the
 // coordinate o + 2(i-f) (even-parity components) or o + 2(i-f) + 1 (odd).
 // With that convention an even-parity point at index i has its odd neighbours
 // at i-1 and i, and an odd-parity point has its even neighbours at i and i+1,

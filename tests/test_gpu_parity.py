@@ -52,7 +52,7 @@ def test_fp32_within_tolerance(name):
     assert rel_err(gpu_run(cfg, ds, precision="fp32"), ref) <= FP32_TOL
 
 
-FUSED_ELIGIBLE = ["vacuum_pml", "dispersive", "debye_short", "density_boxes", "decay_stop", "dft_stop"]
+FUSED_ELIGIBLE = ["vacuum_pml", "dispersive", "debye_short", "density_boxes", "decay_stop", "dft_stop", "pmc_periodic_odd"]
 
 
 @pytest.mark.parametrize("name", FUSED_ELIGIBLE)
@@ -78,21 +78,110 @@ def test_fused_pass_is_bitwise_equal_to_separate_passes(name, precision):
 
 def test_auto_engine_picks_fused_when_eligible():
     from ffip_gb300 import native
-    cfg, ds, _ = load("vacuum_pml")
-    with native.NativeSim(cfg, ds) as s:
-        assert s.stats()["fused"] == 1
-    cfg, ds, _ = load("pmc_periodic_odd")
+    for name in ("vacuum_pml", "pmc_periodic_odd"):
+        cfg, ds, _ = load(name)
+        with native.NativeSim(cfg, ds) as s:
+            assert s.stats()["fused"] == 1, name
+    cfg, ds, _ = load("pec_periodic_magnetic")  # a magnetic Lorentz pole
     with native.NativeSim(cfg, ds) as s:
         assert s.stats()["fused"] == 0
 
 
-def test_fused_request_rejected_for_periodic():
+def test_fused_request_rejected_for_magnetic_poles():
     from ffip_gb300 import native
-    cfg, ds, _ = load("pmc_periodic_odd")
+    cfg, ds, _ = load("pec_periodic_magnetic")
     cfg = copy.deepcopy(cfg)
     cfg["engine"] = "fused"
     with pytest.raises(native.FfipError):
         native.NativeSim(cfg, ds)
+
+
+def _without_magnetic_poles(cfg):
+    """Magnetic susceptibilities and magnetic conductivity (a pole with
+    a0 = b1 = 1, as in the reference's json2medium) removed; mu kept."""
+    cfg = copy.deepcopy(cfg)
+    for g in cfg.get("geometry", []):
+        for key in ("medium", "medium1", "medium2"):
+            if key in g:
+                g[key]["magnetic susceptibility"] = []
+                g[key]["magnetic conductivity"] = 0.0
+    return cfg
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_fused_pec_periodic_magnetic_media_match_separate_passes(precision):
+    """PEC symmetry along z (both faces, with periodic z), periodic x, CPML of
+    different thickness on the two y faces, mu != 1 and an Hz source; the
+    magnetic pole and the magnetic conductivity of the golden case are
+    dropped (the fused pass does not take magnetic poles)."""
+    from ffip_gb300 import native
+    cfg, ds, _ = load("pec_periodic_magnetic")
+    cfg = _without_magnetic_poles(cfg)
+    cfg["precision"] = precision
+    cfg["periodic"] = [1, 0, 1]
+    outs = {}
+    for eng in ("unfused", "fused"):
+        c = copy.deepcopy(cfg)
+        c["engine"] = eng
+        with native.NativeSim(c, ds) as s:
+            assert s.stats()["fused"] == (1 if eng == "fused" else 0)
+            s.run(c["stop condition"])
+            outs[eng] = flatten(s.outputs())
+    for k in outs["unfused"]:
+        assert np.array_equal(outs["unfused"][k], outs["fused"][k]), k
+    assert max(np.abs(v).max() for k, v in outs["fused"].items() if k.endswith("/real")) > 0
+
+
+def _boundary_variant(kind, precision):
+    """The 96^3 dispersive-spheres workload (120 steps) with PEC / PMC /
+    periodic faces: CPML only along the axes without them, an Hz source, and
+    whole-grid DFT monitors of Ey and Hz so that the E and H layers next to
+    every face are compared."""
+    from ffip_gb300 import workloads
+    cfg = workloads.dispersive_spheres(96, steps=120, precision=precision)
+    pml = cfg["PML"][0]
+    if kind == "pmc_x_periodic_y":
+        cfg["symmetry"] = [{"direction": "x", "phase factor": 1}]
+        cfg["periodic"] = [0, 1, 0]
+        axes = ["z"]
+    elif kind == "odd_periodic_xz_pec_y":
+        # odd cell counts: the low faces start at odd doubled coordinates
+        cfg["size"] = [93.0, 90.0, 87.0]
+        cfg["symmetry"] = [{"direction": "y", "phase factor": -1}]
+        cfg["periodic"] = [1, 0, 1]
+        axes = []
+    else:  # pec_z_both_faces_pml_xy
+        cfg["symmetry"] = [{"direction": "z", "phase factor": -1}]
+        cfg["periodic"] = [0, 0, 1]
+        axes = ["x", "y"]
+    cfg["PML"] = [dict(pml, direction=a) for a in axes]
+    cfg["sources"].append({"type": "volume source", "center": [5.0, -7.0, 3.0], "size": [0.0, 0.0, 0.0], "amplitude": 1.0,
+                           "field component": "Hz",
+                           "function": {"type": "Gaussian1", "frequency": 0.12, "cutoff": 4.0, "start time": 0.0}})
+    for comp in ("Ey", "Hz"):
+        cfg["fields output"].append({"type": "volume fields dft", "center": [0.0, 0.0, 0.0], "size": list(cfg["size"]),
+                                     "frequency": [0.1], "field component": comp, "output group": "whole grid " + comp})
+    return cfg
+
+
+@pytest.mark.parametrize("kind", ["pmc_x_periodic_y", "odd_periodic_xz_pec_y", "pec_z_both_faces_pml_xy"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_fused_boundary_faces_large_grid_match_separate_passes(kind, precision):
+    """Several x units, y tiles and z chunks with ghost faces of each kind on
+    both lo parities: the fused pass (with the E layers next to H ghost
+    planes left to the face kernel) equals the separate passes bit for bit."""
+    from ffip_gb300 import native
+    outs = {}
+    for eng in ("unfused", "fused"):
+        cfg = _boundary_variant(kind, precision)
+        cfg["engine"] = eng
+        with native.NativeSim(cfg, {}) as s:
+            assert s.stats()["fused"] == (1 if eng == "fused" else 0)
+            s.run(cfg["stop condition"])
+            outs[eng] = flatten(s.outputs())
+    for k in outs["unfused"]:
+        assert np.array_equal(outs["unfused"][k], outs["fused"][k]), k
+    assert np.abs(outs["fused"]["whole grid Hz/real"]).max() > 0
 
 
 def test_fused_large_grid_matches_separate_passes():
