@@ -43,6 +43,23 @@ def test_transpose_matches_reference_restatement():
     np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-13)
 
 
+def test_transpose_is_the_adjoint_of_trilinear_interpolation():
+    """<interp(u) at the points, w> = <u, transpose(points, w)> for points
+    inside the grid (the adjointness the reference checks by differences in
+    scripts/transpose test.py)."""
+    from scipy.interpolate import RegularGridInterpolator
+    from ffip_gb300 import native
+    rng = np.random.default_rng(5)
+    gx = np.linspace(-1, 2, 13); gy = np.linspace(0, 1, 6); gz = np.linspace(0.5, 1.5, 4)
+    n = 700
+    xyz = np.stack([rng.uniform(-1, 2, n), rng.uniform(0, 1, n), rng.uniform(0.5, 1.5, n)], 1)
+    w = rng.normal(size=n)
+    u = rng.normal(size=(len(gz), len(gy), len(gx)))
+    lhs = np.sum(w * RegularGridInterpolator((gz, gy, gx), u)(xyz[:, ::-1]))
+    rhs = np.sum(u * native.transpose(gx, gy, gz, np.concatenate([xyz, w[:, None]], 1)))
+    assert abs(lhs - rhs) <= 1e-12 * np.abs(w).sum() * np.abs(u).max()
+
+
 def test_transpose_errors():
     from ffip_gb300 import native
     with pytest.raises(ValueError):
