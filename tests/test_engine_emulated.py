@@ -176,3 +176,20 @@ def test_divergence_check_interval_is_validated(lib):
     c["fused wait timeout"] = 0
     with pytest.raises(native.FfipError, match="fused wait timeout"):
         native.NativeSim(c, ds, lib=lib)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_emulated_random_boundaries_match_oracle(lib, seed):
+    """Seeded PEC / PMC / periodic / CPML faces on odd and even grids
+    (tests/test_gpu_parity.py random_boundary_config): the host logic of the
+    ghost faces against the oracle, whole-grid monitors of all six
+    components, 1e-10."""
+    from ffip_gb300 import native
+    from oracle import port
+    from test_gpu_parity import random_boundary_config
+    cfg = random_boundary_config(seed)
+    out = flatten(native.run_json(cfg, {}, lib=lib))
+    ref = flatten(port.run_json(cfg, {}, threads=4))
+    errs = rel_errors(out, ref)
+    assert all(np.abs(out[k]).max() > 0 for k in out if k.endswith("/real"))
+    assert max(errs.values()) <= 1e-10, errs

@@ -235,6 +235,61 @@ def random_config(seed, n=20, steps=150):
     }
 
 
+def random_boundary_config(seed, steps=120):
+    """random_config with seeded boundaries: per axis PEC or PMC symmetry,
+    periodic, both, or CPML (on one or both faces), odd and even cell counts,
+    resolution 1 or 2."""
+    rng = np.random.default_rng(1000 + seed)
+    cfg = random_config(seed, steps=steps)
+    cfg["resolution"] = float(rng.choice([1.0, 2.0]))
+    cfg["size"] = [float(rng.integers(9, 14) + rng.choice([0.0, 0.5])) for _ in range(3)]
+    sym, per, pml = [], [0, 0, 0], []
+    for a, d in enumerate("xyz"):
+        kind = rng.choice(["pec", "pmc", "periodic", "pec_periodic", "cpml", "cpml_one"])
+        if kind in ("pec", "pmc", "pec_periodic"):
+            sym.append({"direction": d, "phase factor": -1 if kind != "pmc" else 1})
+        if kind in ("periodic", "pec_periodic"):
+            per[a] = 1
+        if kind == "cpml":
+            pml.append({"thickness": 2.0, "k max": 1.0, "sigma max": 3.45, "order": 3, "direction": d})
+        if kind == "cpml_one":
+            pml.append({"thickness": 2.0, "k max": 1.0, "sigma max": 3.45, "order": 3, "direction": d,
+                        "side": str(rng.choice(["negative", "positive"]))})
+    cfg["symmetry"], cfg["periodic"], cfg["PML"] = sym, per, pml
+    for g in cfg["geometry"]:
+        g["center"] = [float(v) for v in rng.uniform(-3, 3, 3)]
+        g["radius"] = float(rng.uniform(1, 3))
+    # a symmetry face puts the grid on the positive side only (lo = 0)
+    symmetric = {d["direction"] for d in sym}
+    cfg["sources"][0]["center"] = [float(rng.uniform(0.6, 2.0) if d in symmetric else rng.uniform(-2, 2)) for d in "xyz"]
+    cfg["fields output"] = [dict(m, size=[float(v) for v in cfg["size"]]) for m in cfg["fields output"]]
+    return cfg
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_fused_random_boundaries_match_separate_passes_and_oracle(seed):
+    """Random PEC / PMC / periodic / CPML faces: the fused pass equals the
+    separate passes bit for bit and the oracle to 1e-10, with whole-grid
+    monitors of all six components."""
+    from ffip_gb300 import native
+    from oracle import port
+    cfg = random_boundary_config(seed)
+    outs = {}
+    for eng in ("unfused", "fused"):
+        c = copy.deepcopy(cfg)
+        c["engine"] = eng
+        c["precision"] = "fp64"
+        with native.NativeSim(c) as s:
+            assert s.stats()["fused"] == (1 if eng == "fused" else 0)
+            s.run(c["stop condition"])
+            outs[eng] = flatten(s.outputs())
+    for k in outs["unfused"]:
+        assert np.array_equal(outs["unfused"][k], outs["fused"][k]), k
+    assert all(np.abs(v).max() > 0 for k, v in outs["fused"].items() if k.endswith("/real"))
+    ref = flatten(port.run_json(cfg, {}, threads=4))
+    assert rel_err(outs["fused"], ref) <= FP64_TOL
+
+
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_fp64_matches_oracle_on_random_configs(seed):
     from oracle import port
