@@ -111,6 +111,12 @@ namespace ffipg
 #ifndef FFIP_FUSED_F32_STAGE_PSI
 #define FFIP_FUSED_F32_STAGE_PSI 1
 #endif
+// with STAGE_PSI: the H-side psi of the own points is staged too, copied by
+// cp.async right after the H update of the iteration before the one that
+// uses it (a tuning switch)
+#ifndef FFIP_FUSED_F32_STAGE_PSIH
+#define FFIP_FUSED_F32_STAGE_PSIH 0
+#endif
 #ifndef FFIP_FUSED_F64_RPT
 #define FFIP_FUSED_F64_RPT 1
 #endif
@@ -152,14 +158,14 @@ struct FusedShape<float, P>
                          RW = (XOFF + TX + 3) / 4 * 4,
                          SE = NPT == 1 ? FFIP_FUSED_F32_SE : FFIP_FUSED_F32_SE_X2, SH = FFIP_FUSED_F32_SH, KCH = FFIP_FUSED_KCH,
                          KCH_SHORT = FFIP_FUSED_F32_KCH_SHORT, MINB = NPT == 1 ? FFIP_FUSED_F32_MINB : FFIP_FUSED_F32_MINB_X2,
-                         STAGE_PSI = FFIP_FUSED_F32_STAGE_PSI;
+                         STAGE_PSI = FFIP_FUSED_F32_STAGE_PSI, STAGE_PSIH = STAGE_PSI && FFIP_FUSED_F32_STAGE_PSIH;
 };
 template <bool P>
 struct FusedShape<double, P>
 {
     static constexpr int NPT = 1, TX = 32, RPT = FFIP_FUSED_F64_RPT, TY = 8 * RPT, XOFF = 2, BX = fused_box_width(XOFF, TX, 2),
                          RW = XOFF + TX, SE = FFIP_FUSED_F64_SE, SH = FFIP_FUSED_F64_SH, KCH = FFIP_FUSED_KCH,
-                         KCH_SHORT = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB, STAGE_PSI = 0;
+                         KCH_SHORT = FFIP_FUSED_KCH, MINB = FFIP_FUSED_F64_MINB, STAGE_PSI = 0, STAGE_PSIH = 0;
 };
 
 // NPT consecutive values of one row: an aligned vector load / store (float2
@@ -302,8 +308,8 @@ struct FusedLayout
     // cp.async, one slot of 256 elements (one per thread) per
     // [row][point][component][axis]
     static constexpr int PSI_OFF = (INFO_OFF + (NZ + 1) * 4 + 15) / 16 * 16;  // NZ plane words + the tile's axis word
-    static constexpr int PSI_E = 0;
-    static constexpr int PSI_SLOTS = SH::STAGE_PSI ? 6 * SH::RPT * SH::NPT : 0;
+    static constexpr int PSI_E = 0, PSI_H = 6 * SH::RPT * SH::NPT;  // E slots, then (STAGE_PSIH) H slots
+    static constexpr int PSI_SLOTS = (SH::STAGE_PSI ? 6 * SH::RPT * SH::NPT : 0) + (SH::STAGE_PSIH ? 6 * SH::RPT * SH::NPT : 0);
     static constexpr int SMEM = PSI_OFF;  // the instance without CPML code
     static constexpr int SMEM_PML = PSI_OFF + PSI_SLOTS * 256 * (int)sizeof(T);
     static_assert((SH::SE + SH::SH + 5) * 8 <= 120, "mbarriers do not fit");
@@ -517,6 +523,8 @@ __device__ __forceinline__ bool bar_warps_1_7_or(bool v)
 }
 
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// all but the most recent group complete
+__device__ __forceinline__ void cp_async_wait_but_last() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
 // Per-CTA context of the fused pass
 template <typename T, bool P>
@@ -1070,8 +1078,14 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     // points of iteration q is copied by cp.async at the top of the
     // iteration, during the waits and the H update
     constexpr bool STG = PML && SH::STAGE_PSI;
+    // STGH: the H-side psi of iteration q + 1 is copied after the H update of
+    // iteration q (its own group, after the E group of iteration q, so that
+    // "all but the last group" waits for the E psi before the E update and
+    // for the H psi at the next H update)
+    constexpr bool STGH = PML && SH::STAGE_PSIH;
     T *pstage = reinterpret_cast<T *>(smem + LY::PSI_OFF) + tid;
     auto stage_slot = [&](int r, int p, int c, int a) { return pstage + (LY::PSI_E + ((r * NPT + p) * 3 + c) * 2 + a) * NTH; };
+    auto stage_slot_h = [&](int r, int p, int c, int a) { return pstage + (LY::PSI_H + ((r * NPT + p) * 3 + c) * 2 + a) * NTH; };
     // iteration q: H at plane k = k0 - 1 + q (q <= NP - 2), E at plane k - 1 (q >= 2)
     for (int q = 0; q < NP; ++q, idx += sz)
     {
@@ -1103,7 +1117,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
 #pragma unroll
             for (int p = 0; p < NPT; ++p)
                 for (int c = 0; c < 3; ++c) ph[r][p][c][0] = ph[r][p][c][1] = T(0);
-        if (do_h && pml_h)
+        if (do_h && pml_h && !(STGH && q >= 1))
         {
             const bool cz = X.tab(2, 1)[q].nz();  // H side (parity 1): c != 0
 #pragma unroll
@@ -1202,6 +1216,29 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 for (int p = 0; p < h_issued; ++p) mbar_wait_bounded(&hbar[p % SHS], (p / SHS) & 1, kFusedDrainWaitNs);
             }
             return;
+        }
+        // STGH: this iteration's H-side psi from its staging slots (the last
+        // group, this iteration's E psi, may still be in flight)
+        if (STGH && do_h && pml_h && q >= 1)
+        {
+            cp_async_wait_but_last();
+            const bool cz = X.tab(2, 1)[q].nz();
+#pragma unroll
+            for (int r = 0; r < RPT; ++r)
+#pragma unroll
+                for (int p = 0; p < NPT; ++p)
+                {
+                    const bool ch[3] = {X.tab(0, 1)[ol * NPT + p + 1].nz(), X.tab(1, 1)[r0 + r + 1].nz(), cz};
+                    const unsigned vb = vxy[r][p] & (wh >> kInfoZValidShift);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                    {
+                        const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+                        const bool vh = (vb >> (3 + c)) & 1u;
+                        if (vh && ch[a1]) ph[r][p][c][0] = *stage_slot_h(r, p, c, 0);
+                        if (vh && ch[a2]) ph[r][p][c][1] = *stage_slot_h(r, p, c, 1);
+                    }
+                }
         }
         // 1. H(k) at the tile's own points, and the halo the E update of the
         //    next iteration reads: Hz, Hx on the low-y row (warps 7, 6), Hz,
@@ -1416,6 +1453,34 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
             }
         }
         mbar_arrive(&hd[q & 3]);
+        // STGH: copy the H-side psi of the next iteration's own points (read
+        // above once this copy's group has completed)
+        if (STGH)
+        {
+            const int q1 = q + 1;
+            const unsigned wh1 = q1 <= NP - 2 ? info[q1] : 0u;
+            if (q1 <= NP - 2 && !(wh1 & kInfoFastH) && pml_tables && (wh1 & kInfoZPml))
+            {
+                const bool cz = X.tab(2, 1)[q1].nz();
+#pragma unroll
+                for (int r = 0; r < RPT; ++r)
+#pragma unroll
+                    for (int p = 0; p < NPT; ++p)
+                    {
+                        const bool ch[3] = {X.tab(0, 1)[ol * NPT + p + 1].nz(), X.tab(1, 1)[r0 + r + 1].nz(), cz};
+                        const unsigned vb = vxy[r][p] & (wh1 >> kInfoZValidShift);
+#pragma unroll
+                        for (int c = 0; c < 3; ++c)
+                        {
+                            const int a1 = (c + 1) % 3, a2 = (c + 2) % 3;
+                            const bool vh = (vb >> (3 + c)) & 1u;
+                            if (vh && ch[a1]) cp_async_elem(stage_slot_h(r, p, c, 0), F.psih_in[c][0] + idx + sz + r * sy + p);
+                            if (vh && ch[a2]) cp_async_elem(stage_slot_h(r, p, c, 1), F.psih_in[c][1] + idx + sz + r * sy + p);
+                        }
+                    }
+            }
+            cp_async_commit();
+        }
         // 2. E(k-1) on the tile from H(k-1) and H(k-2)
         if (do_e)
         {
@@ -1531,7 +1596,13 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
             }
             else
             {
-                if (STG && pml_e) cp_async_wait_all();
+                if (STG && pml_e)
+                {
+                    // this iteration's E psi (STGH: the next iteration's H
+                    // psi, committed after it, may stay in flight)
+                    if (STGH) cp_async_wait_but_last();
+                    else cp_async_wait_all();
+                }
                 // the interior instance adds the DFT sums of a row's points
                 // together, with their loads batched (dft_points)
                 constexpr bool DEFER = FFIP_FUSED_DFT_DEFER && !PML && sizeof(T) == 4 && NPT > 1;
