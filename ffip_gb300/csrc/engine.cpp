@@ -20,6 +20,7 @@ struct DevSlots
     uint8_t *group{nullptr};
     SlotRec<T> *rec{nullptr};
     T *A{nullptr}, *amp{nullptr}, *P{nullptr}, *P1{nullptr};
+    T *Pb{nullptr}, *P1b{nullptr};  // fused pass, H side: the other P / J buffers (ping-pong between steps)
     int64_t n{0};
     int stride{0};
     bool poles{false};
@@ -136,6 +137,7 @@ private:
     void init_sources();
     void init_dft();
     void init_ghosts();
+    void alloc_fused_pole_state();
     void bind_params();
     void compute_bytes();
     void set_phases(int side, double t, double (*phase)[2]);
@@ -174,15 +176,13 @@ void Engine<T>::init()
     // the media: slot tables on the device (rasterised there, or uploaded
     // from the host's rasterisation)
     media();
-    // fused pass eligibility (no magnetic poles)
-    bool mag_poles = false;
-    for (int c = 3; c < 6; ++c) mag_poles = mag_poles || comp_poles_[c];
-    const bool eligible = !mag_poles && be_->has_fused();
-    if (P_.engine == "fused" && !eligible)
-        throw std::runtime_error("engine \"fused\" requested but the fused pass needs a grid without magnetic poles and a CUDA backend");
+    // fused pass eligibility (a CUDA backend)
+    const bool eligible = be_->has_fused();
+    if (P_.engine == "fused" && !eligible) throw std::runtime_error("engine \"fused\" requested but the backend has no fused pass");
     if (P_.engine != "auto" && P_.engine != "fused" && P_.engine != "unfused")
         throw std::runtime_error("engine must be \"auto\", \"fused\" or \"unfused\"");
     fused_ = eligible && P_.engine != "unfused";
+    alloc_fused_pole_state();
     for (int c = 0; c < 6; ++c)
     {
         buf_[0][c] = dalloc<T>(cells);
@@ -591,6 +591,22 @@ void Engine<T>::init_sources()
     }
 }
 
+// The fused pass keeps the H side's pole state in two buffers (neighbouring
+// tiles recompute halo H from the old state while the owner writes the new),
+// allocated with the media
+template <typename T>
+void Engine<T>::alloc_fused_pole_state()
+{
+    if (!fused_) return;
+    for (int c = 3; c < 6; ++c)
+    {
+        DevSlots<T> &D = slots_[c];
+        if (!D.P) continue;
+        D.Pb = dalloc<T>((size_t)D.stride * D.n, kMedia);
+        D.P1b = dalloc<T>((size_t)D.stride * D.n, kMedia);
+    }
+}
+
 template <typename T>
 void Engine<T>::init_ghosts()
 {
@@ -807,6 +823,7 @@ void Engine<T>::one_step()
     const double dt = P_.dt;
     // ---- H half step: sources at t = n dt, DFT at (n + 1/2) dt
     set_phases(1, (ts_ + 0.5) * dt, sp_[1].phase);
+    bool h_src_active = false;
     {
         double t = ts_ * dt;
         if (src_[1].npts && !(t > src_[1].max_end))
@@ -814,6 +831,7 @@ void Engine<T>::one_step()
             srcp_[1].time = t;
             be_->sources(srcp_[1]);
             ++nlaunch_;
+            h_src_active = true;
         }
     }
     set_phases(0, (ts_ + 1) * dt, sp_[0].phase);
@@ -841,8 +859,28 @@ void Engine<T>::one_step()
         }
         fp.wait_ns = P_.fused_wait_ns;
         fp.stall_test = P_.fused_stall_test ? 1 : 0;
+        // H pole state: read the buffers of this step's parity, write the others
+        bool h_pending = false;
+        for (int c = 0; c < 3; ++c)
+        {
+            DevSlots<T> &D = slots_[3 + c];
+            if (!D.Pb) continue;
+            SlotView<T> &v = fp.h.slot[c];
+            const bool even = (ts_ % 2) == 0;
+            v.P = even ? D.P : D.Pb;
+            v.P1 = even ? D.P1 : D.P1b;
+            v.Po = even ? D.Pb : D.P;
+            v.P1o = even ? D.P1b : D.P1;
+            h_pending = h_pending || D.A;
+        }
         for (int c = 0; c < 6; ++c) gph_.f[c] = buf_[nx][c];
         nlaunch_ += be_->fused(fp, gph_.nfaces ? &gph_ : nullptr);
+        // the pass reads the H sources waiting at slots with poles without
+        // clearing them: clear them once every reader has finished, in the
+        // steps whose H sources were active
+        if (h_pending && h_src_active)
+            for (int c = 3; c < 6; ++c)
+                if (slots_[c].A) be_->zero(slots_[c].A, slots_[c].n * sizeof(T));
         cur_ = nx;
         for (int c = 0; c < 3; ++c)
         {
@@ -1115,6 +1153,8 @@ void Engine<T>::reset()
         if (D.A) be_->zero(D.A, D.n * sizeof(T));
         if (D.P) be_->zero(D.P, D.n * D.stride * sizeof(T));
         if (D.P1) be_->zero(D.P1, D.n * D.stride * sizeof(T));
+        if (D.Pb) be_->zero(D.Pb, D.n * D.stride * sizeof(T));
+        if (D.P1b) be_->zero(D.P1b, D.n * D.stride * sizeof(T));
     }
     for (size_t u = 0; u < P_.units.size(); ++u)
     {
@@ -1151,9 +1191,7 @@ void Engine<T>::set_density(const std::string &dataset, const double *rho, uint6
         rasterize_media(P_);
         init_media();
     }
-    bool mag_poles = false;
-    for (int c = 3; c < 6; ++c) mag_poles = mag_poles || comp_poles_[c];
-    if (fused_ && mag_poles) throw std::runtime_error("the new density adds magnetic poles, which the fused pass does not support");
+    alloc_fused_pole_state();
     reset();
     compute_bytes();
 }

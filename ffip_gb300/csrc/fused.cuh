@@ -22,11 +22,11 @@
 //   can run ahead by an E update.
 // Every field value is read from HBM once and written once per time step.
 // Because neighbouring CTAs read the previous level while this CTA writes the
-// new one, field buffers (and the H-side CPML psi) ping-pong between steps;
-// E-side CPML psi and polarisation state are only touched by their owner and
-// are updated in place.  Each chunk starts by recomputing H of the plane
-// below it (no writes).  Used on grids without magnetic poles (the engine
-// checks this).
+// new one, field buffers (and the H-side CPML psi and pole state) ping-pong
+// between steps; E-side CPML psi and polarisation state are only touched by
+// their owner and are updated in place.  Each chunk starts by recomputing H
+// of the plane below it (no field writes).  H sources waiting at slots with
+// poles are read, not cleared (the engine clears them after the pass).
 //
 // Two code paths per side and plane.  The common one (a tile plane with no
 // CPML, no material slot, no DFT unit, every point valid) is the plain curl
@@ -643,7 +643,8 @@ __device__ __forceinline__ T fused_h_halo(const FusedCtx<T, P> &X, int x, int y,
     const T old = X.h_tile(hA, c)[o];
     T vd;
     if (!slots) return old + PH.coef_def * term;
-    return material_at(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
+    // not owned: the value only (the owner updates the slot's pole state)
+    return material_at<T, false>(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
 }
 
 // Halo H point p (0 .. NPT-1) of this thread, if any: Hz / Hx of the low-y
@@ -725,6 +726,9 @@ __device__ __forceinline__ void h_own_general(const FusedCtx<T, P> &X, int q, in
             vd = PH.g_def * v;
         }
         else
+            // (on the recomputed plane below the chunk, owned = false, the
+            // owner of that plane writes the same new pole state: both read
+            // the old state and the same inputs)
             v = material_at(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
         const bool val = (vb >> (3 + c)) & 1u;
         X.hn_at(slot_new, c, row + 1, SH::XOFF + xi) = val ? v : T(0);

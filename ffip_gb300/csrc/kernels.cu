@@ -686,8 +686,8 @@ public:
         split(L.kbeg, za);
         split(za, zb);
         split(zb, L.kend);
-        // E material slot row ranges (the fused pass updates no H slots
-        // with poles), for the job weights below
+        // E material slot row ranges, for the job weights below (H slots
+        // put their tile planes on the general path instead)
         std::vector<RowRange> rows[3];
         for (int c = 0; c < 3; ++c)
             if (P.slot[c].map)

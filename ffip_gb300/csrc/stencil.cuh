@@ -61,6 +61,10 @@ struct SlotView
     T *A;                    // pending source sum per slot (H side, slots with poles; else null)
     const T *amp;            // [stride][n]
     T *P, *P1;               // [stride][n] polarisation P and its last increment J = P - P_prev
+    // fused pass, H side: the new P / J go to Po / P1o, so that the old ones
+    // stay readable for the halo points that neighbouring tiles recompute,
+    // and A is left for the engine to clear after the pass; null: in place
+    T *Po, *P1o;
     int64_t n;
     int stride;              // poles per slot in amp / P / P1
 };
@@ -300,8 +304,9 @@ FFIP_HD T pole_field(T old, T term, T pend, T dt, T dsum, T inv)
 
 // Constitutive update of one point given its accdb increment `term`; `old`
 // is the point's field before this half step.  Returns the new field; *vd
-// receives the D/B value for D/B monitors.
-template <typename T>
+// receives the D/B value for D/B monitors.  WRITE = false: the same value
+// without touching the slot state (a halo point the fused pass recomputes).
+template <typename T, bool WRITE = true>
 FFIP_HD T material_at(const SideParams<T> &p, const SlotView<T> &S, int slot, T old, T term, T *vd)
 {
     T v;
@@ -330,7 +335,7 @@ FFIP_HD T material_at(const SideParams<T> &p, const SlotView<T> &S, int slot, T 
     if (S.A)
     {
         pend = S.A[slot];
-        if (pend != T(0)) S.A[slot] = T(0);
+        if (WRITE && !S.Po && pend != T(0)) S.A[slot] = T(0);
     }
     // Each pole keeps P and its last increment J = P - P_prev.  The
     // reference's P_new = c1 P + c2 P_prev + amp c3 E_old is the same as
@@ -347,8 +352,11 @@ FFIP_HD T material_at(const SideParams<T> &p, const SlotView<T> &S, int slot, T 
         const T Pq = S.P[s], Jq = S.P1[s];
         const T Jn = pole_increment(d1, d2, c3, Pq, Jq, S.amp[s], old);
         const T Pn = Pq + Jn;
-        S.P1[s] = Jn;
-        S.P[s] = Pn;
+        if (WRITE)
+        {
+            (S.P1o ? S.P1o : S.P1)[s] = Jn;
+            (S.Po ? S.Po : S.P)[s] = Pn;
+        }
         dsum = dsum + Jn;
         psum = psum + Pn;
     }

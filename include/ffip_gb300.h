@@ -66,17 +66,17 @@ typedef struct ffip_stats {
 /* Simulation::init(config) (src/simulation.cpp:127-188): parses the config
  * JSON, builds the grid, CPML, media, sources and DFT monitors, and uploads
  * them to a CUDA device.  Rebuild-only keys: "precision" ("fp64" default,
- * "fp32" = fp32 field state with fp64 DFT sums), "engine" ("auto": the fused
- * pass unless a medium has magnetic poles; "fused", which fails on magnetic
- * poles; "unfused": separate H and E passes), "device" (CUDA device index;
- * default: the device current in the calling thread), "divergence check
- * interval" (every that many steps the fields are checked for NaN /
- * infinite values and stepping stops with FFIP_ERR_DIVERGED; default 4096,
- * 0 = never; the reference has no such check), "fused wait timeout" (seconds after which a wait inside the fused
- * pass gives up; the next synchronising call then returns FFIP_ERR_CUDA and
- * the fields stay invalid until ffip_reset; default 2) and "fused wait test"
- * (true: every CTA of the fused pass first waits on a barrier that nothing
- * completes, so that the timeout path can be tested). */
+ * "fp32" = fp32 field state with fp64 DFT sums), "engine" ("auto" and
+ * "fused": the fused pass; "unfused": separate H and E passes), "device"
+ * (CUDA device index; default: the device current in the calling thread),
+ * "divergence check interval" (every that many steps the fields are checked
+ * for NaN / infinite values and stepping stops with FFIP_ERR_DIVERGED;
+ * default 4096, 0 = never; the reference has no such check), "fused wait
+ * timeout" (seconds after which a wait inside the fused pass gives up; the
+ * next synchronising call then returns FFIP_ERR_CUDA and the fields stay
+ * invalid until ffip_reset; default 2) and "fused wait test" (true: every CTA
+ * of the fused pass first waits on a barrier that nothing completes, so that
+ * the timeout path can be tested). */
 int ffip_create(const char *config_json, const ffip_dataset *datasets, uint64_t n_datasets, ffip_sim **out);
 
 /* n iterations of the time loop body of Simulation::run_until_time

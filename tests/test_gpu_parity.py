@@ -52,7 +52,8 @@ def test_fp32_within_tolerance(name):
     assert rel_err(gpu_run(cfg, ds, precision="fp32"), ref) <= FP32_TOL
 
 
-FUSED_ELIGIBLE = ["vacuum_pml", "dispersive", "debye_short", "density_boxes", "decay_stop", "dft_stop", "pmc_periodic_odd"]
+FUSED_ELIGIBLE = ["vacuum_pml", "dispersive", "debye_short", "density_boxes", "decay_stop", "dft_stop", "pmc_periodic_odd",
+                  "pec_periodic_magnetic"]
 
 
 @pytest.mark.parametrize("name", FUSED_ELIGIBLE)
@@ -76,24 +77,18 @@ def test_fused_pass_is_bitwise_equal_to_separate_passes(name, precision):
         assert np.array_equal(outs["unfused"][k], outs["fused"][k]), k
 
 
-def test_auto_engine_picks_fused_when_eligible():
+def test_auto_engine_picks_the_fused_pass():
+    """Every boundary kind and medium, magnetic poles included."""
     from ffip_gb300 import native
-    for name in ("vacuum_pml", "pmc_periodic_odd"):
+    for name in ("vacuum_pml", "pmc_periodic_odd", "pec_periodic_magnetic"):
         cfg, ds, _ = load(name)
         with native.NativeSim(cfg, ds) as s:
             assert s.stats()["fused"] == 1, name
-    cfg, ds, _ = load("pec_periodic_magnetic")  # a magnetic Lorentz pole
+    cfg, ds, _ = load("vacuum_pml")
+    cfg = copy.deepcopy(cfg)
+    cfg["engine"] = "unfused"
     with native.NativeSim(cfg, ds) as s:
         assert s.stats()["fused"] == 0
-
-
-def test_fused_request_rejected_for_magnetic_poles():
-    from ffip_gb300 import native
-    cfg, ds, _ = load("pec_periodic_magnetic")
-    cfg = copy.deepcopy(cfg)
-    cfg["engine"] = "fused"
-    with pytest.raises(native.FfipError):
-        native.NativeSim(cfg, ds)
 
 
 def _without_magnetic_poles(cfg):
@@ -111,9 +106,9 @@ def _without_magnetic_poles(cfg):
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_fused_pec_periodic_magnetic_media_match_separate_passes(precision):
     """PEC symmetry along z (both faces, with periodic z), periodic x, CPML of
-    different thickness on the two y faces, mu != 1 and an Hz source; the
-    magnetic pole and the magnetic conductivity of the golden case are
-    dropped (the fused pass does not take magnetic poles)."""
+    different thickness on the two y faces, mu != 1 and an Hz source, with H
+    slots that hold no pole (the golden case's magnetic pole and magnetic
+    conductivity dropped; the case itself runs in FUSED_ELIGIBLE)."""
     from ffip_gb300 import native
     cfg, ds, _ = load("pec_periodic_magnetic")
     cfg = _without_magnetic_poles(cfg)
@@ -150,6 +145,21 @@ def _boundary_variant(kind, precision):
         cfg["symmetry"] = [{"direction": "y", "phase factor": -1}]
         cfg["periodic"] = [1, 0, 1]
         axes = []
+    elif kind == "magnetic_pmc_x_periodic_y":
+        # magnetic Lorentz poles and magnetic conductivity in every third
+        # sphere, and a magnetic sphere around the Hz source (its current
+        # waits at a slot with poles until the H update)
+        cfg["symmetry"] = [{"direction": "x", "phase factor": 1}]
+        cfg["periodic"] = [0, 1, 0]
+        axes = ["z"]
+        msus = [{"type": "Lorentz", "frequency": 0.11, "gamma": 0.02, "amplitude": 0.6}]
+        for i, g in enumerate(cfg["geometry"]):
+            if i % 3 == 0:
+                g["medium"] = dict(g["medium"], mu=1.4, **{"magnetic susceptibility": msus, "magnetic conductivity": 0.01})
+        cfg["geometry"].insert(0, {"type": "sphere", "center": [5.0, -7.0, 3.0], "radius": 4.0,
+                                   "medium": dict(cfg["geometry"][0]["medium"], **{"magnetic susceptibility": msus})})
+        cfg["fields output"].append({"type": "volume fields dft", "center": [0.0, 0.0, 0.0], "size": list(cfg["size"]),
+                                     "frequency": [0.1], "field component": "By", "output group": "whole grid By"})
     else:  # pec_z_both_faces_pml_xy
         cfg["symmetry"] = [{"direction": "z", "phase factor": -1}]
         cfg["periodic"] = [0, 0, 1]
@@ -164,7 +174,8 @@ def _boundary_variant(kind, precision):
     return cfg
 
 
-@pytest.mark.parametrize("kind", ["pmc_x_periodic_y", "odd_periodic_xz_pec_y", "pec_z_both_faces_pml_xy"])
+@pytest.mark.parametrize("kind", ["pmc_x_periodic_y", "odd_periodic_xz_pec_y", "pec_z_both_faces_pml_xy",
+                                  "magnetic_pmc_x_periodic_y"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_fused_boundary_faces_large_grid_match_separate_passes(kind, precision):
     """Several x units, y tiles and z chunks with ghost faces of each kind on
