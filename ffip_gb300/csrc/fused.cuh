@@ -212,6 +212,13 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
 #ifndef FFIP_FUSED_PML_SPLITWARP
 #define FFIP_FUSED_PML_SPLITWARP 2
 #endif
+// with split warps: on a CPML tile plane whose points are all valid and hold
+// no slot and no DFT unit (the lean paths), a warp whose own columns and
+// rows have no CPML, on a plane without z CPML, takes the plain path (in an
+// x-slab tile half the warps lie outside the slab)
+#ifndef FFIP_FUSED_PML_WARP_FAST
+#define FFIP_FUSED_PML_WARP_FAST 1
+#endif
 
 // plain paths: x +- 1 neighbours from the adjacent lane by warp shuffle
 // instead of shared memory, per instance: bit 0 the fp32 interior instance,
@@ -1059,6 +1066,16 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
     // fp64: the plain path without the 1/dx multiplications when 1/dx is 1
     // (the pass is bound by the fp64 pipe there)
     const bool unit_dx = sizeof(T) == 8 && idh == T(1) && ide == T(1);
+    // split warps, CPML instance: no CPML along x at the warp's columns and
+    // along y at its rows (either parity), the same for all its lanes
+    constexpr bool WFAST = PML && SPLITW && FFIP_FUSED_PML_WARP_FAST;
+    bool warp_plain = false;
+    if constexpr (WFAST)
+    {
+        const bool mine = pml_tables && !X.tab(0, 0)[ol + 1].nz() && !X.tab(0, 1)[ol + 1].nz() && !X.tab(1, 0)[r0 + 1].nz() &&
+                          !X.tab(1, 1)[r0 + 1].nz();
+        warp_plain = __all_sync(0xffffffffu, mine);
+    }
     // the rows of this thread's warp (the path choices stay warp-uniform)
     const unsigned rowmask = !SPLITW ? ((1u << RPT) - 1u) << r0
                              : SPLIT_RS == 1 ? 3u << (2 * (wid >> 1))
@@ -1247,9 +1264,34 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
         // 1. H(k) at the tile's own points, and the halo the E update of the
         //    next iteration reads: Hz, Hx on the low-y row (warps 7, 6), Hz,
         //    Hy on the low-x column (warp 5) (recomputed, not written)
+        // the lean planes' halo H (general code, also after a warp's plain
+        // own points)
+        auto general_halo = [&]() {
+#pragma unroll
+            for (int p = 0; p < NPT; ++p)
+            {
+                int hx, hy, comp, row, col;
+                if (halo_point(X, wid, lane, p, hx, hy, comp, row, col))
+                {
+                    auto halo = [&](auto unit) {
+                        constexpr bool U = decltype(unit)::value;
+                        if (comp == 0) return fused_h_halo<T, PML, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        if (comp == 1) return fused_h_halo<T, PML, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        return fused_h_halo<T, PML, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                    };
+                    T v;
+                    if constexpr (sizeof(T) == 8)
+                        v = unit_dx ? halo(std::true_type{}) : halo(std::false_type{});
+                    else
+                        v = halo(std::false_type{});
+                    X.hn_at(rn, comp, row, col) = v;
+                }
+            }
+        };
+        const bool warp_fast_h = WFAST && lean_h && warp_plain && !X.tab(2, 1)[q].nz();
         if (do_h)
         {
-            if (fast_h)
+            if (fast_h || warp_fast_h)
             {
                 auto fast_h_own = [&](auto unit) {
                     constexpr bool U = decltype(unit)::value;
@@ -1345,6 +1387,10 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 }
                 else
                     fast_h_own(std::false_type{});
+                if (WFAST && !fast_h)
+                    general_halo();
+                else
+                {
                 const T *gA0 = X.e_tile(eA, 0), *gA1 = X.e_tile(eA, 1), *gA2 = X.e_tile(eA, 2), *gB0 = X.e_tile(eB, 0),
                         *gB1 = X.e_tile(eB, 1);
                 auto fast_h_halo = [&](auto unit) {
@@ -1382,6 +1428,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 }
                 else
                     fast_h_halo(std::false_type{});
+                }
             }
             else
             {
@@ -1434,26 +1481,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 }
                 else
                     general_h_own(std::false_type{});
-#pragma unroll
-                for (int p = 0; p < NPT; ++p)
-                {
-                    int hx, hy, comp, row, col;
-                    if (halo_point(X, wid, lane, p, hx, hy, comp, row, col))
-                    {
-                        auto halo = [&](auto unit) {
-                            constexpr bool U = decltype(unit)::value;
-                            if (comp == 0) return fused_h_halo<T, PML, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                            if (comp == 1) return fused_h_halo<T, PML, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                            return fused_h_halo<T, PML, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                        };
-                        T v;
-                        if constexpr (sizeof(T) == 8)
-                            v = unit_dx ? halo(std::true_type{}) : halo(std::false_type{});
-                        else
-                            v = halo(std::false_type{});
-                        X.hn_at(rn, comp, row, col) = v;
-                    }
-                }
+                general_halo();
             }
         }
         mbar_arrive(&hd[q & 3]);
@@ -1488,7 +1516,10 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
         // 2. E(k-1) on the tile from H(k-1) and H(k-2)
         if (do_e)
         {
-            if (fast_e)
+            // split warps: a warp without CPML on a lean CPML plane takes
+            // the plain path (no slots on lean planes)
+            const bool warp_fast_e = WFAST && lean_e && warp_plain && !X.tab(2, 0)[q - 1].nz();
+            if (fast_e || warp_fast_e)
             {
                 auto fast_e_own = [&](auto unit, auto slotted) {
                     constexpr bool U = decltype(unit)::value;
