@@ -871,7 +871,7 @@ void Engine<T>::one_step()
             v.P1 = even ? D.P1 : D.P1b;
             v.Po = even ? D.Pb : D.P;
             v.P1o = even ? D.P1b : D.P1;
-            h_pending = h_pending || D.A;
+            h_pending = h_pending || D.A != nullptr;
         }
         for (int c = 0; c < 6; ++c) gph_.f[c] = buf_[nx][c];
         nlaunch_ += be_->fused(fp, gph_.nfaces ? &gph_ : nullptr);
