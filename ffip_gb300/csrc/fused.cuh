@@ -358,6 +358,11 @@ struct FusedLaunch
     // (PEC / PMC / periodic faces): k_face updates those after the H ghost
     // planes are refreshed
     int elo[3][3], ehi[3][3];
+    // PEC / PMC face at the low x (a = 0) / y (a = 1) end: its H ghost
+    // column / row hghost[a] holds hmirror[a] (+1 / -1) times the new H of the
+    // first column / row, which the tiles there put into their halo (so the
+    // E layer next to it stays in the pass); hmirror[a] = 0: no such face
+    int hmirror[2], hghost[2];
     const int4 *jobs;     // per CTA: x0, y0, k0, k1 (tile origin and owned z planes)
 };
 
@@ -612,8 +617,8 @@ __device__ __forceinline__ T plane_term(const PmlCoef<T> &A1, const PmlCoef<T> &
 // component GC (3..5), point (x, y) of plane k; E stages eA/eB hold planes
 // k/k+1, H stage hA plane k.  Returns 0 where the component has no grid point.
 template <typename T, bool P, int GC, bool UNIT = false>
-__device__ __forceinline__ T fused_h_halo(const FusedCtx<T, P> &X, int x, int y, int k, int eA, int eB, int hA, bool pml_plane,
-                                          bool slots)
+__device__ __forceinline__ T fused_h_point(const FusedCtx<T, P> &X, int x, int y, int k, int eA, int eB, int hA, bool pml_plane,
+                                           bool slots)
 {
     using SH = FusedShape<T, P>;
     constexpr int BX = SH::BX, XOFF = SH::XOFF, c = GC - 3;
@@ -652,6 +657,21 @@ __device__ __forceinline__ T fused_h_halo(const FusedCtx<T, P> &X, int x, int y,
     if (!slots) return old + PH.coef_def * term;
     // not owned: the value only (the owner updates the slot's pole state)
     return material_at<T, false>(PH, PH.slot[c], slot_of(PH.slot[c], PH.My, x, y, k, idx), old, term, &vd);
+}
+
+// fused_h_point, or on the H ghost column / row of a PEC / PMC low x / y
+// face the mirrored value of the first column / row (the value the ghost
+// planes receive after the step)
+template <typename T, bool P, int GC, bool UNIT = false>
+__device__ __forceinline__ T fused_h_halo(const FusedCtx<T, P> &X, int x, int y, int k, int eA, int eB, int hA, bool pml_plane,
+                                          bool slots)
+{
+    const FusedLaunch<T> &L = *X.L;
+    if (L.hmirror[0] && x == L.hghost[0] && x == X.x0 - 1)
+        return T(L.hmirror[0]) * fused_h_point<T, P, GC, UNIT>(X, x + 1, y, k, eA, eB, hA, pml_plane, slots);
+    if (L.hmirror[1] && y == L.hghost[1] && y == X.y0 - 1)
+        return T(L.hmirror[1]) * fused_h_point<T, P, GC, UNIT>(X, x, y + 1, k, eA, eB, hA, pml_plane, slots);
+    return fused_h_point<T, P, GC, UNIT>(X, x, y, k, eA, eB, hA, pml_plane, slots);
 }
 
 // Halo H point p (0 .. NPT-1) of this thread, if any: Hz / Hx of the low-y
@@ -1395,30 +1415,35 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                         *gB1 = X.e_tile(eB, 1);
                 auto fast_h_halo = [&](auto unit) {
                     constexpr bool U = decltype(unit)::value;
+                    // Hz / Hx / Hy at box offset o (fast-path arithmetic)
+                    auto hz = [&](int o) { return X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh); };
+                    auto hx = [&](int o) { return X.h_tile(hA, 0)[o] + coefH * curl_diff<U>(gA2[o], gA2[o + BX], gA1[o], gB1[o], idh); };
+                    auto hy = [&](int o) { return X.h_tile(hA, 1)[o] + coefH * curl_diff<U>(gA0[o], gB0[o], gA2[o], gA2[o + 1], idh); };
                     if (wid >= 6)
                     {
+                        // a PEC / PMC low y face: the row holds the mirrored first row
+                        const bool mir = L.hmirror[1] && X.y0 - 1 == L.hghost[1];
+                        const T ms = T(L.hmirror[1]);
 #pragma unroll
                         for (int p = 0; p < NPT; ++p)
                         {
                             const int o = XOFF + lane * NPT + p;  // row y0 - 1 of the boxes
                             if (wid == 7)
-                                X.hn_at(rn, 2, 0, o) =
-                                    (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh);
+                                X.hn_at(rn, 2, 0, o) = mir ? ms * hz(o + BX) : (wh & kInfoZeroRow) ? T(0) : hz(o);
                             else
-                                X.hn_at(rn, 0, 0, o) =
-                                    (wh & kInfoZeroRow) ? T(0) : X.h_tile(hA, 0)[o] + coefH * curl_diff<U>(gA2[o], gA2[o + BX], gA1[o], gB1[o], idh);
+                                X.hn_at(rn, 0, 0, o) = mir ? ms * hx(o + BX) : (wh & kInfoZeroRow) ? T(0) : hx(o);
                         }
                     }
                     else if (wid == 5 && lane < 2 * TY)
                     {
+                        const bool mir = L.hmirror[0] && X.x0 - 1 == L.hghost[0];
+                        const T ms = T(L.hmirror[0]);
                         const int v = lane < TY ? lane : lane - TY;
                         const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
                         if (lane < TY)
-                            X.hn_at(rn, 2, v + 1, XOFF - 1) =
-                                (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 2)[o] + coefH * curl_diff<U>(gA1[o], gA1[o + 1], gA0[o], gA0[o + BX], idh);
+                            X.hn_at(rn, 2, v + 1, XOFF - 1) = mir ? ms * hz(o + 1) : (wh & kInfoZeroCol) ? T(0) : hz(o);
                         else
-                            X.hn_at(rn, 1, v + 1, XOFF - 1) =
-                                (wh & kInfoZeroCol) ? T(0) : X.h_tile(hA, 1)[o] + coefH * curl_diff<U>(gA0[o], gB0[o], gA2[o], gA2[o + 1], idh);
+                            X.hn_at(rn, 1, v + 1, XOFF - 1) = mir ? ms * hy(o + 1) : (wh & kInfoZeroCol) ? T(0) : hy(o);
                     }
                 };
                 if constexpr (sizeof(T) == 8)

@@ -443,9 +443,32 @@ public:
                 L.elo[c][a] = LC.elo[c][a] = p.e.vlo[c][a];
                 L.ehi[c][a] = LC.ehi[c][a] = p.e.vhi[c][a];
             }
+        // a PEC / PMC face at the low x / y end whose ghost is the column /
+        // row just before the first tile (the ghost mirrors the index after
+        // it): the tiles there mirror their first column / row into the halo
+        // instead, and the E layer next to it stays in the pass
+        const int first[2] = {kXFirst, 1};
+        for (int a = 0; a < 2; ++a)
+        {
+            L.hmirror[a] = LC.hmirror[a] = 0;
+            L.hghost[a] = LC.hghost[a] = -1;
+        }
+        auto mirrored = [&](const GhostFace &G) {
+            return G.axis < 2 && G.dst == first[G.axis] - 1 && G.src == G.dst + 1 && L.hmirror[G.axis] == G.mult;
+        };
         for (int f = 0; ghost && f < hg->nfaces; ++f)
         {
             const GhostFace &G = hg->faces[f];
+            if (G.axis < 2 && G.dst == first[G.axis] - 1 && G.src == G.dst + 1)
+            {
+                L.hmirror[G.axis] = LC.hmirror[G.axis] = G.mult;
+                L.hghost[G.axis] = LC.hghost[G.axis] = G.dst;
+            }
+        }
+        for (int f = 0; ghost && f < hg->nfaces; ++f)
+        {
+            const GhostFace &G = hg->faces[f];
+            if (mirrored(G)) continue;
             const int ch = G.comp - 3, a = G.axis;
             for (int c = 0; c < 3; ++c)
             {
