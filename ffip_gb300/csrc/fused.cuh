@@ -219,6 +219,11 @@ __device__ __forceinline__ void stv(T *p, const Vals<T, N> &v)
 #ifndef FFIP_FUSED_PML_WARP_FAST
 #define FFIP_FUSED_PML_WARP_FAST 1
 #endif
+// PEC / PMC faces at the low x / y end mirrored into the halo of the first
+// tiles (FusedLaunch::hmirror); 0: their E layers deferred like the others'
+#ifndef FFIP_FUSED_HALO_MIRROR
+#define FFIP_FUSED_HALO_MIRROR 1
+#endif
 
 // plain paths: x +- 1 neighbours from the adjacent lane by warp shuffle
 // instead of shared memory, per instance: bit 0 the fp32 interior instance,
@@ -662,16 +667,29 @@ __device__ __forceinline__ T fused_h_point(const FusedCtx<T, P> &X, int x, int y
 // fused_h_point, or on the H ghost column / row of a PEC / PMC low x / y
 // face the mirrored value of the first column / row (the value the ghost
 // planes receive after the step)
-template <typename T, bool P, int GC, bool UNIT = false>
+template <typename T, bool P, int GC, bool UNIT = false, bool MIR = false>
 __device__ __forceinline__ T fused_h_halo(const FusedCtx<T, P> &X, int x, int y, int k, int eA, int eB, int hA, bool pml_plane,
                                           bool slots)
 {
+    if constexpr (!MIR) return fused_h_point<T, P, GC, UNIT>(X, x, y, k, eA, eB, hA, pml_plane, slots);
+    else
+    {
+    // one evaluation at the mirrored point, scaled by +-1 (exact)
     const FusedLaunch<T> &L = *X.L;
+    int xe = x, ye = y, sc = 1;
     if (L.hmirror[0] && x == L.hghost[0] && x == X.x0 - 1)
-        return T(L.hmirror[0]) * fused_h_point<T, P, GC, UNIT>(X, x + 1, y, k, eA, eB, hA, pml_plane, slots);
-    if (L.hmirror[1] && y == L.hghost[1] && y == X.y0 - 1)
-        return T(L.hmirror[1]) * fused_h_point<T, P, GC, UNIT>(X, x, y + 1, k, eA, eB, hA, pml_plane, slots);
-    return fused_h_point<T, P, GC, UNIT>(X, x, y, k, eA, eB, hA, pml_plane, slots);
+    {
+        xe = x + 1;
+        sc = L.hmirror[0];
+    }
+    else if (L.hmirror[1] && y == L.hghost[1] && y == X.y0 - 1)
+    {
+        ye = y + 1;
+        sc = L.hmirror[1];
+    }
+    const T v = fused_h_point<T, P, GC, UNIT>(X, xe, ye, k, eA, eB, hA, pml_plane, slots);
+    return sc == 1 ? v : -v;
+    }
 }
 
 // Halo H point p (0 .. NPT-1) of this thread, if any: Hz / Hx of the low-y
@@ -864,8 +882,11 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T, P> &X, int qe, i
 }
 
 // PML = false: the instance for jobs whose tiles, halos and planes hold no
-// CPML point (the host sorts the jobs); it carries no CPML code.
-template <typename T, bool PML>
+// CPML point (the host sorts the jobs); it carries no CPML code.  MIR: the
+// copy launched on grids with a PEC / PMC face at the low x or y end (its
+// first tiles mirror that face's H ghost into their halo); without it the
+// halo code of the other grids stays as small as before.
+template <typename T, bool PML, bool MIR = false>
 __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const __grid_constant__ FusedLaunch<T> L)
 {
     using SH = FusedShape<T, PML>;
@@ -1295,9 +1316,9 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 {
                     auto halo = [&](auto unit) {
                         constexpr bool U = decltype(unit)::value;
-                        if (comp == 0) return fused_h_halo<T, PML, 3, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                        if (comp == 1) return fused_h_halo<T, PML, 4, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                        return fused_h_halo<T, PML, 5, U>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        if (comp == 0) return fused_h_halo<T, PML, 3, U, MIR>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        if (comp == 1) return fused_h_halo<T, PML, 4, U, MIR>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        return fused_h_halo<T, PML, 5, U, MIR>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
                     };
                     T v;
                     if constexpr (sizeof(T) == 8)
@@ -1421,29 +1442,27 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                     auto hy = [&](int o) { return X.h_tile(hA, 1)[o] + coefH * curl_diff<U>(gA0[o], gB0[o], gA2[o], gA2[o + 1], idh); };
                     if (wid >= 6)
                     {
-                        // a PEC / PMC low y face: the row holds the mirrored first row
-                        const bool mir = L.hmirror[1] && X.y0 - 1 == L.hghost[1];
-                        const T ms = T(L.hmirror[1]);
+                        // a PEC / PMC low y face: the row holds the mirrored first
+                        // row (one evaluation, at row y0, negated for -1)
+                        const bool mir = MIR && L.hmirror[1] && X.y0 - 1 == L.hghost[1];
+                        const bool neg = mir && L.hmirror[1] < 0, zero = !mir && (wh & kInfoZeroRow);
+                        const int sh = mir ? BX : 0;
 #pragma unroll
                         for (int p = 0; p < NPT; ++p)
                         {
-                            const int o = XOFF + lane * NPT + p;  // row y0 - 1 of the boxes
-                            if (wid == 7)
-                                X.hn_at(rn, 2, 0, o) = mir ? ms * hz(o + BX) : (wh & kInfoZeroRow) ? T(0) : hz(o);
-                            else
-                                X.hn_at(rn, 0, 0, o) = mir ? ms * hx(o + BX) : (wh & kInfoZeroRow) ? T(0) : hx(o);
+                            const int o = XOFF + lane * NPT + p + sh;  // row y0 - 1 of the boxes (y0: mirrored)
+                            const T v = zero ? T(0) : wid == 7 ? hz(o) : hx(o);
+                            X.hn_at(rn, wid == 7 ? 2 : 0, 0, o - sh) = neg ? -v : v;
                         }
                     }
                     else if (wid == 5 && lane < 2 * TY)
                     {
-                        const bool mir = L.hmirror[0] && X.x0 - 1 == L.hghost[0];
-                        const T ms = T(L.hmirror[0]);
+                        const bool mir = MIR && L.hmirror[0] && X.x0 - 1 == L.hghost[0];
+                        const bool neg = mir && L.hmirror[0] < 0, zero = !mir && (wh & kInfoZeroCol);
                         const int v = lane < TY ? lane : lane - TY;
-                        const int o = (v + 1) * BX + XOFF - 1;  // column x0 - 1
-                        if (lane < TY)
-                            X.hn_at(rn, 2, v + 1, XOFF - 1) = mir ? ms * hz(o + 1) : (wh & kInfoZeroCol) ? T(0) : hz(o);
-                        else
-                            X.hn_at(rn, 1, v + 1, XOFF - 1) = mir ? ms * hy(o + 1) : (wh & kInfoZeroCol) ? T(0) : hy(o);
+                        const int o = (v + 1) * BX + XOFF - (mir ? 0 : 1);  // column x0 - 1 (x0: mirrored)
+                        const T h = zero ? T(0) : lane < TY ? hz(o) : hy(o);
+                        X.hn_at(rn, lane < TY ? 2 : 1, v + 1, XOFF - 1) = neg ? -h : h;
                     }
                 };
                 if constexpr (sizeof(T) == 8)

@@ -362,9 +362,11 @@ public:
             const int64_t need = std::max<int64_t>((int64_t)SP::MINB * (LP::SMEM_PML + 1024), (int64_t)SH::MINB * (LY::SMEM + 1024));
             const int carve = FFIP_FUSED_CARVEOUT >= 0 ? FFIP_FUSED_CARVEOUT
                                                        : (int)std::min<int64_t>(100, (need * 100 + maxsm - 1) / std::max(maxsm, 1));
-            for (int pml = 0; pml < 2; ++pml)
+            for (int v = 0; v < 4; ++v)
             {
-                const auto fn = pml ? k_fused<T, true> : k_fused<T, false>;
+                const int pml = v & 1;
+                const auto fn = v == 0 ? k_fused<T, false, false> : v == 1 ? k_fused<T, true, false> : v == 2 ? k_fused<T, false, true>
+                                                                                                           : k_fused<T, true, true>;
                 check(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pml ? LP::SMEM_PML : LY::SMEM),
                       "cudaFuncSetAttribute");
                 check(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, carve), "cudaFuncSetAttribute");
@@ -459,7 +461,7 @@ public:
         for (int f = 0; ghost && f < hg->nfaces; ++f)
         {
             const GhostFace &G = hg->faces[f];
-            if (G.axis < 2 && G.dst == first[G.axis] - 1 && G.src == G.dst + 1)
+            if (FFIP_FUSED_HALO_MIRROR && G.axis < 2 && G.dst == first[G.axis] - 1 && G.src == G.dst + 1)
             {
                 L.hmirror[G.axis] = LC.hmirror[G.axis] = G.mult;
                 L.hghost[G.axis] = LC.hghost[G.axis] = G.dst;
@@ -484,6 +486,7 @@ public:
             }
         }
         std::memcpy(LC.elo, L.elo, sizeof L.elo);
+        const bool mirror = L.hmirror[0] != 0 || L.hmirror[1] != 0;
         std::memcpy(LC.ehi, L.ehi, sizeof L.ehi);
         const FaceList fl_h = face_list(p.h, nullptr, nullptr, L.xlim, L.ylim);
         const FaceList fl_e = face_list(p.e, L.elo, L.ehi, L.xlim, L.ylim);
@@ -535,14 +538,16 @@ public:
         if (J.nb > 0)
         {
             LC.jobs = J.dev;
-            k_fused<T, true><<<J.nb, block, LP::SMEM_PML, stream_>>>(LC);
+            if (mirror) k_fused<T, true, true><<<J.nb, block, LP::SMEM_PML, stream_>>>(LC);
+            else k_fused<T, true, false><<<J.nb, block, LP::SMEM_PML, stream_>>>(LC);
             check(cudaGetLastError(), "k_fused launch");
             ++n;
         }
         if (J.ni > 0)
         {
             L.jobs = J.dev + J.nb;
-            k_fused<T, false><<<J.ni, block, LY::SMEM, J.nb > 0 ? side_ : stream_>>>(L);
+            if (mirror) k_fused<T, false, true><<<J.ni, block, LY::SMEM, J.nb > 0 ? side_ : stream_>>>(L);
+            else k_fused<T, false, false><<<J.ni, block, LY::SMEM, J.nb > 0 ? side_ : stream_>>>(L);
             check(cudaGetLastError(), "k_fused launch");
             ++n;
         }
