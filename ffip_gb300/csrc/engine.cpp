@@ -607,47 +607,57 @@ void Engine<T>::alloc_fused_pole_state()
     }
 }
 
-template <typename T>
-void Engine<T>::init_ghosts()
+} // namespace
+
+int build_ghost_faces(const Plan &P, GhostFace *faces, int max_faces)
 {
     // Faces filled after every half step, src/fields.cpp:327-482:
     //   PEC/PMC: ghost(lo-1) = mult * value(lo+1), mult = (lo odd ? phase : -phase)
     //   periodic: ghost(lo-1) = value(hi-1), ghost(hi+1) = value(lo+1)
-    gp_ = GhostParams<T>();
     int nf = 0;
     for (int a = 0; a < 3; ++a)
         for (int side = 0; side < 2; ++side)
         {
-            int bc = P_.bc[a][side];
+            int bc = P.bc[a][side];
             if (bc == BC_NONE || bc == BC_SYNC) continue;
-            int edge = side == 0 ? P_.lo[a] : P_.hi[a];
-            int ghost = side == 0 ? P_.lo[a] - 1 : P_.hi[a] + 1;
+            int edge = side == 0 ? P.lo[a] : P.hi[a];
+            int ghost = side == 0 ? P.lo[a] - 1 : P.hi[a] + 1;
             int src;
             int mult = 1;
-            if (bc == BC_PERIOD) src = side == 0 ? P_.hi[a] - 1 : P_.lo[a] + 1;
+            if (bc == BC_PERIOD) src = side == 0 ? P.hi[a] - 1 : P.lo[a] + 1;
             else
             {
-                src = side == 0 ? P_.lo[a] + 1 : P_.hi[a] - 1;
+                src = side == 0 ? P.lo[a] + 1 : P.hi[a] - 1;
                 int phase = bc == BC_PEC ? -1 : 1;
                 mult = (edge & 1) ? phase : -phase;
             }
             for (int c = 0; c < 6; ++c)
             {
                 if (comp_parity(c, a) != (ghost & 1)) continue;
-                if (nf >= kMaxFaces) throw std::runtime_error("too many ghost faces");
-                GhostFace &F = gp_.faces[nf++];
+                if (nf >= max_faces) throw std::runtime_error("too many ghost faces");
+                GhostFace &F = faces[nf++];
                 F.comp = c;
                 F.axis = a;
-                F.src = P_.index_of(a, src);
-                F.dst = P_.index_of(a, ghost);
+                F.src = P.index_of(a, src);
+                F.dst = P.index_of(a, ghost);
                 F.mult = mult;
                 int au = (a + 1) % 3, av = (a + 2) % 3;
-                F.u0 = P_.vlo[c][au];
-                F.u1 = std::max(0, P_.vhi[c][au] - P_.vlo[c][au] + 1);
-                F.v0 = P_.vlo[c][av];
-                F.v1 = std::max(0, P_.vhi[c][av] - P_.vlo[c][av] + 1);
+                F.u0 = P.vlo[c][au];
+                F.u1 = std::max(0, P.vhi[c][au] - P.vlo[c][au] + 1);
+                F.v0 = P.vlo[c][av];
+                F.v1 = std::max(0, P.vhi[c][av] - P.vlo[c][av] + 1);
             }
         }
+    return nf;
+}
+
+namespace
+{
+template <typename T>
+void Engine<T>::init_ghosts()
+{
+    gp_ = GhostParams<T>();
+    const int nf = build_ghost_faces(P_, gp_.faces, kMaxFaces);
     gp_.nfaces = nf;
     gp_.sy = P_.Mx_pad;
     gp_.sz = P_.plane();

@@ -36,6 +36,10 @@ struct FusedParams
     int stall_test;
 };
 
+// The PEC / PMC / periodic ghost faces of a plan (Fields::sync_boundary,
+// src/fields.cpp:327-482); returns their number
+int build_ghost_faces(const Plan &P, GhostFace *faces, int max_faces);
+
 // A bounded wait inside a kernel gave up: the results of the steps since
 // the last check are invalid.
 struct DeviceTimeout : std::runtime_error

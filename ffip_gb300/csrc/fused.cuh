@@ -65,6 +65,7 @@
 #include <type_traits>
 
 #include "engine.hpp"
+#include "fused_plan.hpp"
 
 namespace ffipg
 {
@@ -1807,25 +1808,6 @@ __device__ __forceinline__ void face_point(const FusedParams<T> &F, int i, int j
     (IS_E ? F.eout : F.hout)[c][idx] = v;
     if (p.nunits) dft_point<T>(p.nunits, p.units, p.phase, GC, i, j, k, (double)v, (double)vd);
 }
-
-// The points of one side that the pass does not own, as boxes of one
-// component each (built on the host): x >= xlim or y >= ylim, and for E the
-// layers whose curl reads a ghost H
-struct FaceBox
-{
-    int comp;       // component of the side, 0..2
-    int i0, ni;     // x range
-    int j0, nj;     // y range
-    int k0;         // first z plane (the box's count follows from the next start)
-    int64_t start;  // index of the box's first point in the list
-};
-constexpr int kMaxFaceBoxes = 18;  // 3 components x 6 sides of a box difference
-struct FaceList
-{
-    int n;
-    int64_t total;
-    FaceBox b[kMaxFaceBoxes];
-};
 
 template <typename T, bool IS_E>
 __global__ void k_face(const __grid_constant__ FusedLaunch<T> L, const __grid_constant__ FaceList B)

@@ -400,15 +400,11 @@ public:
         // tiles start at the first index holding grid points (kXFirst along
         // x, 1 along y); one or two layers beyond a whole number of tiles go
         // to k_face
-        const int nxp = xend - kXFirst, nyp = yend - 1;
         // x is cut into units of the CPML instance's tile width: a unit
         // that touches CPML runs as a CPML job, two (or TX / TX_P) adjacent
         // units without CPML as one interior job
-        const int rx = nxp % SP::TX, ry = nyp % SH::TY;
-        const int nbx = (nxp >= SP::TX && rx <= 2) ? nxp / SP::TX : (nxp + SP::TX - 1) / SP::TX;
-        const int nby = (nyp >= SH::TY && ry <= 2) ? nyp / SH::TY : (nyp + SH::TY - 1) / SH::TY;
-        L.xlim = std::min(xend, kXFirst + nbx * SP::TX);
-        L.ylim = std::min(yend, 1 + nby * SH::TY);
+        int nbx, nby;
+        fused_limits(xend, yend, kXFirst, SP::TX, SH::TY, nbx, nby, L.xlim, L.ylim);
         L.xend = xend;
         L.yend = yend;
         L.kbeg = kbeg;
@@ -433,63 +429,22 @@ public:
         LC.yend = L.yend;
         LC.kbeg = L.kbeg;
         LC.kend = L.kend;
-        // E points the pass owns: the valid range less the layers whose curl
-        // reads an H ghost plane of hg (E component c reads H component
-        // (c + 2) % 3 along axis (c + 1) % 3 and (c + 1) % 3 along (c + 2) % 3,
-        // at its own index and the one below); ghost planes lie outside the
-        // valid H range, so those layers are the first / last of the range
+        // E points the pass owns and the PEC / PMC faces it mirrors into
+        // the halo of its first tiles (fused_plan.hpp)
         const bool ghost = hg && hg->nfaces > 0;
-        for (int c = 0; c < 3; ++c)
-            for (int a = 0; a < 3; ++a)
-            {
-                L.elo[c][a] = LC.elo[c][a] = p.e.vlo[c][a];
-                L.ehi[c][a] = LC.ehi[c][a] = p.e.vhi[c][a];
-            }
-        // a PEC / PMC face at the low x / y end whose ghost is the column /
-        // row just before the first tile (the ghost mirrors the index after
-        // it): the tiles there mirror their first column / row into the halo
-        // instead, and the E layer next to it stays in the pass
-        const int first[2] = {kXFirst, 1};
-        for (int a = 0; a < 2; ++a)
-        {
-            L.hmirror[a] = LC.hmirror[a] = 0;
-            L.hghost[a] = LC.hghost[a] = -1;
-        }
-        auto mirrored = [&](const GhostFace &G) {
-            return G.axis < 2 && G.dst == first[G.axis] - 1 && G.src == G.dst + 1 && L.hmirror[G.axis] == G.mult;
-        };
-        for (int f = 0; ghost && f < hg->nfaces; ++f)
-        {
-            const GhostFace &G = hg->faces[f];
-            if (FFIP_FUSED_HALO_MIRROR && G.axis < 2 && G.dst == first[G.axis] - 1 && G.src == G.dst + 1)
-            {
-                L.hmirror[G.axis] = LC.hmirror[G.axis] = G.mult;
-                L.hghost[G.axis] = LC.hghost[G.axis] = G.dst;
-            }
-        }
-        for (int f = 0; ghost && f < hg->nfaces; ++f)
-        {
-            const GhostFace &G = hg->faces[f];
-            if (mirrored(G)) continue;
-            const int ch = G.comp - 3, a = G.axis;
-            for (int c = 0; c < 3; ++c)
-            {
-                if (!((ch == (c + 2) % 3 && a == (c + 1) % 3) || (ch == (c + 1) % 3 && a == (c + 2) % 3))) continue;
-                for (int i = G.dst; i <= G.dst + 1; ++i)
-                {
-                    int &lo = L.elo[c][a], &hi = L.ehi[c][a];
-                    if (i < lo || i > hi) continue;
-                    if (i == lo) ++lo;
-                    else if (i == hi) --hi;
-                    else throw std::runtime_error("fused pass: a ghost plane inside the grid");
-                }
-            }
-        }
-        std::memcpy(LC.elo, L.elo, sizeof L.elo);
+        const FusedOwnership own = fused_ownership(p.e.vlo, p.e.vhi, ghost ? hg->faces : nullptr, ghost ? hg->nfaces : 0, kXFirst,
+                                                   FFIP_FUSED_HALO_MIRROR != 0);
+        std::memcpy(L.elo, own.elo, sizeof L.elo);
+        std::memcpy(L.ehi, own.ehi, sizeof L.ehi);
+        std::memcpy(L.hmirror, own.hmirror, sizeof L.hmirror);
+        std::memcpy(L.hghost, own.hghost, sizeof L.hghost);
+        std::memcpy(LC.elo, own.elo, sizeof LC.elo);
+        std::memcpy(LC.ehi, own.ehi, sizeof LC.ehi);
+        std::memcpy(LC.hmirror, own.hmirror, sizeof LC.hmirror);
+        std::memcpy(LC.hghost, own.hghost, sizeof LC.hghost);
         const bool mirror = L.hmirror[0] != 0 || L.hmirror[1] != 0;
-        std::memcpy(LC.ehi, L.ehi, sizeof L.ehi);
-        const FaceList fl_h = face_list(p.h, nullptr, nullptr, L.xlim, L.ylim);
-        const FaceList fl_e = face_list(p.e, L.elo, L.ehi, L.xlim, L.ylim);
+        const FaceList fl_h = fused_face_list(p.h.vlo, p.h.vhi, nullptr, nullptr, L.xlim, L.ylim);
+        const FaceList fl_e = fused_face_list(p.e.vlo, p.e.vhi, L.elo, L.ehi, L.xlim, L.ylim);
         int n = 0;
         // a second stream runs the interior instance beside the CPML one, and
         // the H half of k_face (it reads only step-n fields) beside both
@@ -586,68 +541,6 @@ public:
     }
     int fused(const FusedParams<double> &p, const GhostParams<double> *hg) override { return fused_t(p, hg); }
     int fused(const FusedParams<float> &p, const GhostParams<float> *hg) override { return fused_t(p, hg); }
-
-    // The points of one side's components that the fused pass does not own,
-    // as disjoint boxes: the valid range V less the owned box W (x < xlim,
-    // y < ylim and, for E, the range elo .. ehi), cut along x, then y, then z
-    template <typename T>
-    static FaceList face_list(const SideParams<T> &S, const int (*lo_own)[3], const int (*hi_own)[3], int xlim, int ylim)
-    {
-        FaceList B{};
-        for (int c = 0; c < 3; ++c)
-        {
-            int v0[3], v1[3], w0[3], w1[3];
-            bool vempty = false, wempty = false;
-            for (int a = 0; a < 3; ++a)
-            {
-                v0[a] = S.vlo[c][a];
-                v1[a] = S.vhi[c][a];
-                w0[a] = lo_own ? std::max(v0[a], lo_own[c][a]) : v0[a];
-                w1[a] = hi_own ? std::min(v1[a], hi_own[c][a]) : v1[a];
-                if (a == 0) w1[a] = std::min(w1[a], xlim - 1);
-                if (a == 1) w1[a] = std::min(w1[a], ylim - 1);
-                vempty = vempty || v1[a] < v0[a];
-                wempty = wempty || w1[a] < w0[a];
-            }
-            if (vempty) continue;
-            auto add = [&](const int (&b0)[3], const int (&b1)[3]) {
-                if (B.n == kMaxFaceBoxes) throw std::runtime_error("fused pass: too many face boxes");
-                FaceBox &X = B.b[B.n++];
-                X.comp = c;
-                X.i0 = b0[0];
-                X.ni = b1[0] - b0[0] + 1;
-                X.j0 = b0[1];
-                X.nj = b1[1] - b0[1] + 1;
-                X.k0 = b0[2];
-                X.start = B.total;
-                B.total += (int64_t)X.ni * X.nj * (b1[2] - b0[2] + 1);
-            };
-            if (wempty)
-            {
-                add(v0, v1);
-                continue;
-            }
-            int lo[3] = {v0[0], v0[1], v0[2]}, hi[3] = {v1[0], v1[1], v1[2]};
-            for (int a = 0; a < 3; ++a)
-            {
-                if (w0[a] > lo[a])
-                {
-                    int b0[3] = {lo[0], lo[1], lo[2]}, b1[3] = {hi[0], hi[1], hi[2]};
-                    b1[a] = w0[a] - 1;
-                    add(b0, b1);
-                }
-                if (w1[a] < hi[a])
-                {
-                    int b0[3] = {lo[0], lo[1], lo[2]}, b1[3] = {hi[0], hi[1], hi[2]};
-                    b0[a] = w1[a] + 1;
-                    add(b0, b1);
-                }
-                lo[a] = w0[a];
-                hi[a] = w1[a];
-            }
-        }
-        return B;
-    }
 
     // CTA jobs of the fused pass (x0, y0, k0, k1): the jobs whose tile, halo
     // and planes touch a CPML point first (nb of them), then the others (ni).

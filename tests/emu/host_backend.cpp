@@ -9,6 +9,7 @@
 // emulated (it is a CUDA-only tiling of the same rules).
 #include <cmath>
 #include <cstdlib>
+#include <cstdio>
 #include <cstring>
 #include <stdexcept>
 
@@ -175,3 +176,113 @@ int sg_col2im(const float *, const int *, const int *, const int *, const int *,
     throw std::runtime_error("not emulated");
 }
 } // namespace ffipg
+
+// ---------------------------------------------------------------------------
+// Test hook: the host half of the fused pass's split of a step's points
+// (ffip_gb300/csrc/fused_plan.hpp, the code the CUDA backend runs before each
+// pass) checked on a config's plan without a GPU.  Tile shape of the CPML
+// instance (which sets xlim / ylim): 32 x 8.
+#include <string>
+#include <vector>
+
+#include "fused_plan.hpp"
+
+extern "C" int ffip_emu_fused_partition_check(const char *config_json, char *msg, uint64_t msg_len)
+{
+    using namespace ffipg;
+    auto fail = [&](const std::string &m) {
+        if (msg && msg_len) std::snprintf(msg, msg_len, "%s", m.c_str());
+        return 1;
+    };
+    try
+    {
+        Json cfg = Json::parse(config_json);
+        Plan P;
+        build_plan(cfg, {}, P);
+        GhostFace all[kMaxFaces];
+        const int nf = build_ghost_faces(P, all, kMaxFaces);
+        std::vector<GhostFace> hf;
+        for (int f = 0; f < nf; ++f)
+            if (all[f].comp >= 3) hf.push_back(all[f]);
+        int vlo[2][3][3], vhi[2][3][3];
+        int xend = 0, yend = 0;
+        for (int c = 0; c < 6; ++c)
+            for (int a = 0; a < 3; ++a)
+            {
+                vlo[c / 3][c % 3][a] = P.vlo[c][a];
+                vhi[c / 3][c % 3][a] = P.vhi[c][a];
+                if (a == 0) xend = std::max(xend, P.vhi[c][0] + 1);
+                if (a == 1) yend = std::max(yend, P.vhi[c][1] + 1);
+            }
+        int nbx, nby, xlim, ylim;
+        fused_limits(xend, yend, kXFirst, 32, 8, nbx, nby, xlim, ylim);
+        const FusedOwnership own = fused_ownership(vlo[0], vhi[0], hf.data(), (int)hf.size(), kXFirst, true);
+        const FaceList fl[2] = {fused_face_list(vlo[0], vhi[0], own.elo, own.ehi, xlim, ylim),
+                                fused_face_list(vlo[1], vhi[1], nullptr, nullptr, xlim, ylim)};
+        auto owned = [&](int side, int c, int i, int j, int k) {
+            if (i >= xlim || j >= ylim) return false;
+            const int(*lo)[3] = side == 0 ? own.elo : vlo[1];
+            const int(*hi)[3] = side == 0 ? own.ehi : vhi[1];
+            return i >= lo[c][0] && i <= hi[c][0] && j >= lo[c][1] && j <= hi[c][1] && k >= lo[c][2] && k <= hi[c][2];
+        };
+        auto in_box = [&](const FaceList &B, int c, int i, int j, int k) {
+            int hits = 0;
+            for (int b = 0; b < B.n; ++b)
+            {
+                const FaceBox &X = B.b[b];
+                const int64_t end = b + 1 < B.n ? B.b[b + 1].start : B.total;
+                const int nk = (int)((end - X.start) / ((int64_t)X.ni * X.nj));
+                hits += X.comp == c && i >= X.i0 && i < X.i0 + X.ni && j >= X.j0 && j < X.j0 + X.nj && k >= X.k0 && k < X.k0 + nk;
+            }
+            return hits;
+        };
+        // a ghost position of H component h: on a face's ghost plane, inside its in-plane range
+        auto ghost_of = [&](int h, const int q[3]) -> const GhostFace * {
+            for (const GhostFace &G : hf)
+            {
+                if (G.comp != 3 + h || q[G.axis] != G.dst) continue;
+                const int au = (G.axis + 1) % 3, av = (G.axis + 2) % 3;
+                if (q[au] >= G.u0 && q[au] < G.u0 + G.u1 && q[av] >= G.v0 && q[av] < G.v0 + G.v1) return &G;
+            }
+            return nullptr;
+        };
+        for (int side = 0; side < 2; ++side)
+            for (int c = 0; c < 3; ++c)
+                for (int k = vlo[side][c][2]; k <= vhi[side][c][2]; ++k)
+                    for (int j = vlo[side][c][1]; j <= vhi[side][c][1]; ++j)
+                        for (int i = vlo[side][c][0]; i <= vhi[side][c][0]; ++i)
+                        {
+                            const bool o = owned(side, c, i, j, k);
+                            const int f = in_box(fl[side], c, i, j, k);
+                            if ((o ? 1 : 0) + f != 1)
+                                return fail("point " + std::to_string(side * 3 + c) + " (" + std::to_string(i) + "," +
+                                            std::to_string(j) + "," + std::to_string(k) + "): owned " + std::to_string(o) +
+                                            ", face boxes " + std::to_string(f));
+                            if (side != 0 || !o) continue;
+                            // the H values the pass's E update reads
+                            const int pairs[2][2] = {{(c + 2) % 3, (c + 1) % 3}, {(c + 1) % 3, (c + 2) % 3}};
+                            for (const auto &hp : pairs)
+                                for (int d = 0; d <= 1; ++d)
+                                {
+                                    int q[3] = {i, j, k};
+                                    q[hp[1]] -= d;
+                                    const GhostFace *G = ghost_of(hp[0], q);
+                                    if (!G) continue;
+                                    const int first[2] = {kXFirst, 1};
+                                    const bool mirrored = G->axis < 2 && own.hmirror[G->axis] == G->mult && own.hghost[G->axis] == G->dst &&
+                                                          q[G->axis] == first[G->axis] - 1 && G->src == G->dst + 1;
+                                    if (!mirrored)
+                                        return fail("owned E point " + std::to_string(c) + " (" + std::to_string(i) + "," +
+                                                    std::to_string(j) + "," + std::to_string(k) + ") reads the H ghost of face axis " +
+                                                    std::to_string(G->axis));
+                                }
+                        }
+        if (msg && msg_len) std::snprintf(msg, msg_len, "ok %d H faces, %d + %d face boxes, mirror %d %d", (int)hf.size(), fl[0].n,
+                                          fl[1].n, own.hmirror[0], own.hmirror[1]);
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        return fail(std::string("error: ") + e.what());
+    }
+}

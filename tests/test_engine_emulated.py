@@ -193,3 +193,47 @@ def test_emulated_random_boundaries_match_oracle(lib, seed):
     errs = rel_errors(out, ref)
     assert all(np.abs(out[k]).max() > 0 for k in out if k.endswith("/real"))
     assert max(errs.values()) <= 1e-10, errs
+
+
+def partition_check(lib, cfg):
+    """The host half of the fused pass's split of a step (fused_plan.hpp) on
+    a config's plan: every valid point owned by the pass or in exactly one
+    face box, and no E point of the pass reading an H ghost unless its face
+    is mirrored into the halo of the first tiles (tests/emu/host_backend.cpp)."""
+    import ctypes
+    import json
+    fn = lib.ffip_emu_fused_partition_check
+    fn.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint64]
+    fn.restype = ctypes.c_int
+    msg = ctypes.create_string_buffer(512)
+    rc = fn(json.dumps(cfg).encode(), msg, 512)
+    return rc, msg.value.decode()
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_fused_partition_on_random_boundaries(lib, seed):
+    from test_gpu_parity import random_boundary_config
+    rc, msg = partition_check(lib, random_boundary_config(seed))
+    assert rc == 0, msg
+
+
+def test_fused_partition_on_golden_cases_and_workloads(lib):
+    """Golden cases (PMC / PEC symmetry with periodic faces, odd grids) and
+    the spheres workload at 33 and 40 cells with every kind of face."""
+    from ffip_gb300 import workloads
+    from test_gpu_parity import _boundary_variant
+    cfgs = [cfg for cfg, ds, _ in (load(n) for n in CASES) if not ds]  # (the hook takes no datasets)
+    for n in (33, 40):
+        cfg = workloads.dispersive_spheres(n, steps=10)
+        cfgs.append(cfg)
+        for sym, per in (([{"direction": "x", "phase factor": 1}], [0, 1, 0]), ([{"direction": "y", "phase factor": -1}], [1, 0, 1]),
+                         ([{"direction": "x", "phase factor": -1}, {"direction": "y", "phase factor": 1}], [1, 1, 1])):
+            c = copy.deepcopy(cfg)
+            c["symmetry"], c["periodic"] = sym, per
+            cfgs.append(c)
+    mirrored = 0
+    for cfg in cfgs:
+        rc, msg = partition_check(lib, cfg)
+        assert rc == 0, msg
+        mirrored += "mirror 0 0" not in msg
+    assert mirrored >= 6  # the symmetry faces along x / y are mirrored, not deferred
