@@ -802,7 +802,7 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T, P> &X, int qe, i
     constexpr int BX = SH::BX, RW = SH::RW;
     if (!FULL)
     {
-        vb = 63u;
+        vb &= 63u;  // every point valid (less the caller's masked ones)
         slots = dft = false;
     }
     const FusedParams<T> &F = X.L->fp;
@@ -883,11 +883,14 @@ __device__ __forceinline__ void e_own_general(const FusedCtx<T, P> &X, int qe, i
 }
 
 // PML = false: the instance for jobs whose tiles, halos and planes hold no
-// CPML point (the host sorts the jobs); it carries no CPML code.  MIR: the
-// copy launched on grids with a PEC / PMC face at the low x or y end (its
-// first tiles mirror that face's H ghost into their halo); without it the
-// halo code of the other grids stays as small as before.
-template <typename T, bool PML, bool MIR = false>
+// CPML point (the host sorts the jobs); it carries no CPML code.  GH: the
+// copy launched on grids with PEC / PMC / periodic faces: the first tiles
+// next to a PEC / PMC low x / y face mirror its H ghost into their halo, and
+// tiles whose first column or row of an E component is deferred to the face
+// kernel keep the plain and lean paths with those points' stores and DFT
+// sums masked; without it the code of the other grids stays as small as
+// before.
+template <typename T, bool PML, bool GH = false>
 __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const __grid_constant__ FusedLaunch<T> L)
 {
     using SH = FusedShape<T, PML>;
@@ -1061,8 +1064,10 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
         inside = inside && PE.vlo[c][0] <= X.x0 - (zcol ? 0 : 1) && X.x0 + TX - 1 <= PE.vhi[c][0] &&
                  PE.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PE.vhi[c][1] &&
                  PH.vlo[c][0] <= X.x0 - (zcol ? 0 : 1) && X.x0 + TX - 1 <= PH.vhi[c][0] &&
-                 PH.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PH.vhi[c][1] && L.elo[c][0] <= X.x0 &&
-                 X.x0 + TX - 1 <= L.ehi[c][0] && L.elo[c][1] <= X.y0 && X.y0 + TY - 1 <= L.ehi[c][1];
+                 PH.vlo[c][1] <= X.y0 - (zrow ? 0 : 1) && X.y0 + TY - 1 <= PH.vhi[c][1];
+    // (E points left to the face kernel, the first column / row of a
+    // component next to a deferred ghost, are masked on the plain and lean
+    // paths: GH; without ghost faces every valid E point is owned)
     // per plane: may each side take the plain path; kInfoZPml becomes "CPML
     // at this tile plane" (the tile's x / y tables or the plane's z)
     for (int o = pt; o < LY::NZ; o += PT)
@@ -1098,6 +1103,25 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                     if (xp >= PH.vlo[c][0] && xp <= PH.vhi[c][0] && y >= PH.vlo[c][1] && y <= PH.vhi[c][1])
                         vxy[r][p] |= 1u << (3 + c);
                 }
+        }
+    // GH: per own row and point, the E components whose point is valid but
+    // left to the face kernel (the plain and lean paths skip its store and
+    // DFT sums)
+    unsigned dm[RPT][NPT];
+#pragma unroll
+    for (int r = 0; r < RPT; ++r)
+#pragma unroll
+        for (int p = 0; p < NPT; ++p)
+        {
+            dm[r][p] = 0;
+            if constexpr (GH)
+            {
+                const int y = X.y0 + r0 + r, xp = x + p;
+                if (xp < L.xlim && y < L.ylim)
+                    for (int c = 0; c < 3; ++c)
+                        if (xp >= PE.vlo[c][0] && xp <= PE.vhi[c][0] && y >= PE.vlo[c][1] && y <= PE.vhi[c][1] && !((vxy[r][p] >> c) & 1u))
+                            dm[r][p] |= 1u << c;
+            }
         }
     __syncthreads();
     const int sz = (int)PE.sz, sy = (int)PE.sy;
@@ -1317,9 +1341,9 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                 {
                     auto halo = [&](auto unit) {
                         constexpr bool U = decltype(unit)::value;
-                        if (comp == 0) return fused_h_halo<T, PML, 3, U, MIR>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                        if (comp == 1) return fused_h_halo<T, PML, 4, U, MIR>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
-                        return fused_h_halo<T, PML, 5, U, MIR>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        if (comp == 0) return fused_h_halo<T, PML, 3, U, GH>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        if (comp == 1) return fused_h_halo<T, PML, 4, U, GH>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
+                        return fused_h_halo<T, PML, 5, U, GH>(X, hx, hy, k, eA, eB, hA, pml_h, h_slots);
                     };
                     T v;
                     if constexpr (sizeof(T) == 8)
@@ -1445,7 +1469,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                     {
                         // a PEC / PMC low y face: the row holds the mirrored first
                         // row (one evaluation, at row y0, negated for -1)
-                        const bool mir = MIR && L.hmirror[1] && X.y0 - 1 == L.hghost[1];
+                        const bool mir = GH && L.hmirror[1] && X.y0 - 1 == L.hghost[1];
                         const bool neg = mir && L.hmirror[1] < 0, zero = !mir && (wh & kInfoZeroRow);
                         const int sh = mir ? BX : 0;
 #pragma unroll
@@ -1458,7 +1482,7 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                     }
                     else if (wid == 5 && lane < 2 * TY)
                     {
-                        const bool mir = MIR && L.hmirror[0] && X.x0 - 1 == L.hghost[0];
+                        const bool mir = GH && L.hmirror[0] && X.x0 - 1 == L.hghost[0];
                         const bool neg = mir && L.hmirror[0] < 0, zero = !mir && (wh & kInfoZeroCol);
                         const int v = lane < TY ? lane : lane - TY;
                         const int o = (v + 1) * BX + XOFF - (mir ? 0 : 1);  // column x0 - 1 (x0: mirrored)
@@ -1639,9 +1663,27 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                                          curl_diff<U>(hyr[p], hyx, hx[r + 1][p], hx[r][p], ide), &vds[2][p]);
                             }
                         }
-                        st_outv(&F.eout[0][idx_e + r * sy], ex);
-                        st_outv(&F.eout[1][idx_e + r * sy], ey);
-                        st_outv(&F.eout[2][idx_e + r * sy], ez);
+                        // GH: points left to the face kernel are neither stored
+                        // nor summed (they add zero to the DFT sums)
+                        unsigned dmr = 0;
+#pragma unroll
+                        for (int p = 0; p < NPT; ++p) dmr |= dm[r][p];
+                        if (!GH || dmr == 0)
+                        {
+                            st_outv(&F.eout[0][idx_e + r * sy], ex);
+                            st_outv(&F.eout[1][idx_e + r * sy], ey);
+                            st_outv(&F.eout[2][idx_e + r * sy], ez);
+                        }
+                        else
+                        {
+#pragma unroll
+                            for (int p = 0; p < NPT; ++p)
+                            {
+                                if (!(dm[r][p] & 1u)) st_out(&F.eout[0][idx_e + r * sy + p], ex[p]);
+                                if (!(dm[r][p] & 2u)) st_out(&F.eout[1][idx_e + r * sy + p], ey[p]);
+                                if (!(dm[r][p] & 4u)) st_out(&F.eout[2][idx_e + r * sy + p], ez[p]);
+                            }
+                        }
                         if (dft_e)
                             for (int c = 0; c < 3; ++c)
                             {
@@ -1655,10 +1697,14 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                                         vd[p] = (double)vds[c][p];
                                     else
                                         vd[p] = (double)(PE.g_def * ev[p]);
+                                    if (GH && ((dm[r][p] >> c) & 1u)) v[p] = vd[p] = 0.0;
                                 }
                                 if constexpr (PML || NPT == 1)
+                                {
                                     for (int p = 0; p < NPT; ++p)
-                                        dft_point<T>(PE.nunits, PE.units, PE.phase, c, x + p, X.y0 + r0 + r, k - 1, v[p], vd[p]);
+                                        if (!GH || !((dm[r][p] >> c) & 1u))
+                                            dft_point<T>(PE.nunits, PE.units, PE.phase, c, x + p, X.y0 + r0 + r, k - 1, v[p], vd[p]);
+                                }
                                 else
                                     dft_points<NPT>(PE.nunits, PE.units, PE.phase, c, x, X.y0 + r0 + r, k - 1, v, vd);
                             }
@@ -1712,8 +1758,8 @@ __global__ void __launch_bounds__(256, FusedShape<T, PML>::MINB) k_fused(const _
                             {
                                 auto lean = [&](auto ax) {
                                     constexpr int A = decltype(ax)::value;
-                                    e_own_general<T, PML, false, STG, U, A>(X, q - 1, r0 + r, xi, eS, rp, rpp, 63u, true, false,
-                                                                       false, idx_e + r * sy + p, sl_e[r][p], pe);
+                                    e_own_general<T, PML, false, STG, U, A>(X, q - 1, r0 + r, xi, eS, rp, rpp, 63u & ~dm[r][p], true,
+                                                                       false, false, idx_e + r * sy + p, sl_e[r][p], pe);
                                 };
                                 if constexpr (kAxisSpec<T>)
                                 {

@@ -442,7 +442,9 @@ public:
         std::memcpy(LC.ehi, own.ehi, sizeof LC.ehi);
         std::memcpy(LC.hmirror, own.hmirror, sizeof LC.hmirror);
         std::memcpy(LC.hghost, own.hghost, sizeof LC.hghost);
-        const bool mirror = L.hmirror[0] != 0 || L.hmirror[1] != 0;
+        // grids with ghost faces take the pass's GH copy (mirrored halo,
+        // masked stores of the deferred E points)
+        const bool gh = ghost;
         const FaceList fl_h = fused_face_list(p.h.vlo, p.h.vhi, nullptr, nullptr, L.xlim, L.ylim);
         const FaceList fl_e = fused_face_list(p.e.vlo, p.e.vhi, L.elo, L.ehi, L.xlim, L.ylim);
         int n = 0;
@@ -493,7 +495,7 @@ public:
         if (J.nb > 0)
         {
             LC.jobs = J.dev;
-            if (mirror) k_fused<T, true, true><<<J.nb, block, LP::SMEM_PML, stream_>>>(LC);
+            if (gh) k_fused<T, true, true><<<J.nb, block, LP::SMEM_PML, stream_>>>(LC);
             else k_fused<T, true, false><<<J.nb, block, LP::SMEM_PML, stream_>>>(LC);
             check(cudaGetLastError(), "k_fused launch");
             ++n;
@@ -501,7 +503,7 @@ public:
         if (J.ni > 0)
         {
             L.jobs = J.dev + J.nb;
-            if (mirror) k_fused<T, false, true><<<J.ni, block, LY::SMEM, J.nb > 0 ? side_ : stream_>>>(L);
+            if (gh) k_fused<T, false, true><<<J.ni, block, LY::SMEM, J.nb > 0 ? side_ : stream_>>>(L);
             else k_fused<T, false, false><<<J.ni, block, LY::SMEM, J.nb > 0 ? side_ : stream_>>>(L);
             check(cudaGetLastError(), "k_fused launch");
             ++n;
