@@ -49,7 +49,11 @@
 // (the ghost holds the mirror / periodic image of the new H) are left to the
 // E half of k_face too, which runs after the H ghost planes of the new level
 // are filled; the pass reads E ghost planes of step n as loaded (filled at
-// the end of the previous step), so the H update needs nothing else.
+// the end of the previous step), so the H update needs nothing else.  A
+// PEC / PMC face at the low x / y end is not deferred: its ghost is +-1
+// times the first column / row, which the tiles there compute and mirror
+// into their halo.  On such grids the GH copy of the pass runs: the mirror,
+// and the plain / lean E paths with the deferred points' stores masked.
 //
 // The per-point arithmetic is the same as the separate H/E kernels
 // (stencil.cuh: pml_term, material_at, dft_point), so both passes give the
