@@ -6,8 +6,8 @@
 //
 // Datasets.  The reference reads its input datasets from the HDF5 file named
 // by "input file" and writes one HDF5 group per output to "fields output
-// file" (src/simulation.cpp:151-157, src/dft.cpp:273-320).  HDF5 is not part
-// of this build; the same content is exchanged as a directory of .npy files:
+// file" (src/simulation.cpp:151-157, src/dft.cpp:273-320).  This driver links
+// no HDF5 library; the same content is exchanged as a directory of .npy files:
 // the input datasets are <input file>.d/<dataset name>.npy (float64), and
 // every output group is <fields output file>.d/<group name>/ with real.npy,
 // imag.npy ([nf][nz][ny][nx]), x.npy, y.npy, z.npy and f.npy, or x/y/z.npy
