@@ -21,7 +21,7 @@ import ctypes
 import json
 import math
 import time
-from typing import Dict, List, Optional, Tuple
+from typing import List, Optional
 
 import numpy as np
 

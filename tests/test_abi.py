@@ -6,7 +6,6 @@ import json
 import os
 import re
 
-import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 

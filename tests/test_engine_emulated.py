@@ -221,7 +221,6 @@ def test_fused_partition_on_golden_cases_and_workloads(lib):
     """Golden cases (PMC / PEC symmetry with periodic faces, odd grids) and
     the spheres workload at 33 and 40 cells with every kind of face."""
     from ffip_gb300 import workloads
-    from test_gpu_parity import _boundary_variant
     cfgs = [cfg for cfg, ds, _ in (load(n) for n in CASES) if not ds]  # (the hook takes no datasets)
     for n in (33, 40):
         cfg = workloads.dispersive_spheres(n, steps=10)

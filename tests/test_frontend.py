@@ -6,7 +6,6 @@ import json
 import os
 
 import numpy as np
-import pytest
 
 import ffip_gb300 as ffip
 

@@ -1,7 +1,6 @@
 """The run_sim_json driver (config.json + .npy input directory in, .npy
 output groups out) against the in-process C ABI, on the emulation library
 (CPU) and, marked gpu, on the CUDA library."""
-import os
 
 import numpy as np
 import pytest
