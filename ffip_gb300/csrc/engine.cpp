@@ -641,7 +641,8 @@ int build_ghost_faces(const Plan &P, GhostFace *faces, int max_faces)
                 F.src = P.index_of(a, src);
                 F.dst = P.index_of(a, ghost);
                 F.mult = mult;
-                int au = (a + 1) % 3, av = (a + 2) % 3;
+                int au, av;
+                ghost_axes(a, au, av);
                 F.u0 = P.vlo[c][au];
                 F.u1 = std::max(0, P.vhi[c][au] - P.vlo[c][au] + 1);
                 F.v0 = P.vlo[c][av];

@@ -647,9 +647,17 @@ struct GhostFace
     int axis;     // normal axis
     int src, dst; // array index along the axis
     int mult;     // +1 / -1
-    int u0, u1;   // first index and count along the first in-plane axis
+    int u0, u1;   // first index and count along the first in-plane axis (ghost_axes)
     int v0, v1;   // ... second in-plane axis
 };
+
+// In-plane axes of a ghost face: x first where it lies in the plane, so that
+// the threads of a warp (along u) write consecutive addresses
+FFIP_HD void ghost_axes(int axis, int &au, int &av)
+{
+    au = axis == 0 ? 1 : 0;
+    av = axis == 2 ? 1 : 2;
+}
 template <typename T>
 struct GhostParams
 {
@@ -665,7 +673,8 @@ FFIP_HD void ghost_point(const GhostParams<T> &p, int face, int u, int v)
     const GhostFace &F = p.faces[face];
     if (u >= F.u1 || v >= F.v1) return;
     const int64_t st[3] = {1, p.sy, p.sz};
-    const int au = (F.axis + 1) % 3, av = (F.axis + 2) % 3;
+    int au, av;
+    ghost_axes(F.axis, au, av);
     const int64_t base = (int64_t)(F.u0 + u) * st[au] + (int64_t)(F.v0 + v) * st[av];
     T *A = p.f[F.comp];
     A[base + (int64_t)F.dst * st[F.axis]] = A[base + (int64_t)F.src * st[F.axis]] * (T)F.mult;

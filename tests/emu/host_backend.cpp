@@ -241,7 +241,8 @@ extern "C" int ffip_emu_fused_partition_check(const char *config_json, char *msg
             for (const GhostFace &G : hf)
             {
                 if (G.comp != 3 + h || q[G.axis] != G.dst) continue;
-                const int au = (G.axis + 1) % 3, av = (G.axis + 2) % 3;
+                int au, av;
+                ghost_axes(G.axis, au, av);
                 if (q[au] >= G.u0 && q[au] < G.u0 + G.u1 && q[av] >= G.v0 && q[av] < G.v0 + G.v1) return &G;
             }
             return nullptr;
