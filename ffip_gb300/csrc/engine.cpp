@@ -90,6 +90,7 @@ private:
     SourceParams<T> srcp_[2];
     GhostParams<T> gp_{};
     GhostParams<T> gph_{};  // the H faces of gp_ (the fused pass fills them between its halves)
+    GhostParams<T> gpe_{};  // the E faces of gp_ (all that is left to fill after a fused step)
     bool fused_{false};
     int64_t ts_{0};
     int64_t nlaunch_{0};
@@ -665,8 +666,11 @@ void Engine<T>::init_ghosts()
     gph_ = GhostParams<T>();
     gph_.sy = gp_.sy;
     gph_.sz = gp_.sz;
+    gpe_ = gph_;
+    gpe_.nfaces = 0;
     for (int f = 0; f < nf; ++f)
         if (gp_.faces[f].comp >= 3) gph_.faces[gph_.nfaces++] = gp_.faces[f];
+        else gpe_.faces[gpe_.nfaces++] = gp_.faces[f];
 }
 
 template <typename T>
@@ -777,7 +781,7 @@ void Engine<T>::bind_params()
         s.nunits = p.nunits;
         for (int su = 0; su < p.nunits; ++su) s.units[su] = p.units[su];
     }
-    for (int c = 0; c < 6; ++c) gp_.f[c] = buf_[cur_][c];
+    for (int c = 0; c < 6; ++c) gp_.f[c] = gpe_.f[c] = buf_[cur_][c];
 }
 
 template <typename T>
@@ -900,7 +904,7 @@ void Engine<T>::one_step()
             sp_[0].o[c] = buf_[cur_][3 + c];
             sp_[1].o[c] = buf_[cur_][c];
         }
-        for (int c = 0; c < 6; ++c) gp_.f[c] = buf_[cur_][c];
+        for (int c = 0; c < 6; ++c) gp_.f[c] = gpe_.f[c] = buf_[cur_][c];
     }
     else
     {
@@ -922,7 +926,10 @@ void Engine<T>::one_step()
             ++nlaunch_;
         }
     }
-    if (gp_.nfaces) { be_->ghosts(gp_); ++nlaunch_; }
+    // the fused pass filled the H ghost planes of the new level already (no
+    // later update touches H): only the E faces are left
+    const GhostParams<T> &gend = fused_ ? gpe_ : gp_;
+    if (gend.nfaces) { be_->ghosts(gend); ++nlaunch_; }
     ++ts_;
     if (P_.divergence_check > 0 && ts_ % P_.divergence_check == 0) check_finite();
 }
