@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <cstdint>
 #include <stdexcept>
+#include <utility>
+#include <vector>
 
 #include "stencil.cuh"
 
@@ -165,5 +167,178 @@ inline FaceList fused_face_list(const int vlo[3][3], const int vhi[3][3], const 
         }
     }
     return B;
+}
+
+// CTA jobs of the pass: tile origin (x, y) and owned z planes [z, w)
+struct JobBox
+{
+    int x, y, z, w;
+};
+// a DFT monitor unit's local box (array indices) and its frequencies
+struct DftBox
+{
+    int i0[3], ld[3], nf;
+};
+struct JobInputs
+{
+    std::vector<char> pml[3];         // CPML (c != 0 at either parity) per position along each axis
+    std::vector<RowRange> rows[3];    // E material slot row ranges per (j, k), empty: no slots
+    std::vector<DftBox> dft;          // E and H monitor units
+    int My = 0, Mz = 0;
+    int xlim = 0, ylim = 0, kbeg = 0, kend = 0;
+    int nbx = 0, nby = 0;             // x units of TXP columns, y tiles of TY rows
+    int TX = 0, TXP = 0, TY = 0, KCH = 0;
+};
+struct JobLists
+{
+    std::vector<JobBox> b, in;  // CPML instance jobs, then interior instance jobs
+    // no interior job holds the last x tile or the last y tile: the tiles
+    // whose new H the E half of the face kernel reads all belong to the
+    // CPML instance
+    bool face_in_pml = true;
+};
+
+// The jobs of the pass (the CUDA backend builds them once per grid, CPML
+// tables and media): x is cut into units of TXP columns from first_x; a
+// unit, row of tiles and z chunk without any CPML point in the unit with its
+// low-x halo (nor in the row or the chunk) may go to the instance without
+// CPML code, TX / TXP adjacent such units per job; z chunks of at most KCH
+// planes, the longest CPML-free run of planes chunked apart from the rest.
+// slots_to_p: units whose rows hold E material slots go to the CPML
+// instance; dft_split > 0: a job whose planes meet DFT monitors is split
+// along z into 1 + (frequencies summed over the monitors it meets) /
+// dft_split pieces; heavy_first: within each instance the jobs with DFT sums
+// (then those with slots) go first; cpml_order: then by the number of axes
+// along which the job meets CPML.
+inline JobLists fused_jobs(const JobInputs &I, int first_x, bool slots_to_p, int dft_split, bool heavy_first, bool cpml_order)
+{
+    const int TX = I.TX, TXP = I.TXP, TY = I.TY, KCH = I.KCH;
+    auto any = [&](int a, int lo, int hi) {  // CPML anywhere in [lo, hi]
+        const int len = (int)I.pml[a].size();
+        for (int i = std::max(lo, 0); i <= std::min(hi, len - 1); ++i)
+            if (I.pml[a][i]) return true;
+        return false;
+    };
+    // z: chunks [a, b) whose planes a-1 .. b-1 hold no CPML point come from
+    // the longest run f0 .. f1 of such planes (a = f0 + 1, b = f1 + 1),
+    // chunked apart from the rest
+    int za = I.kbeg, zb = I.kbeg;
+    for (int f = I.kbeg - 1; f < I.kend;)
+    {
+        int e = f;
+        while (e < I.kend && !any(2, e, e)) ++e;  // planes f .. e-1 are free
+        const int a = std::max(f + 1, I.kbeg), bnd = std::min(e, I.kend);
+        if (bnd - a > zb - za)
+        {
+            za = a;
+            zb = bnd;
+        }
+        f = e + 1;
+    }
+    std::vector<std::pair<int, int>> chunks;
+    auto split = [&](int lo, int hi) {
+        if (hi <= lo) return;
+        const int nch = (hi - lo + KCH - 1) / KCH;
+        for (int i = 0; i < nch; ++i)
+            chunks.emplace_back(lo + (int)((int64_t)(hi - lo) * i / nch), lo + (int)((int64_t)(hi - lo) * (i + 1) / nch));
+    };
+    split(I.kbeg, za);
+    split(za, zb);
+    split(zb, I.kend);
+    auto meets = [&](const DftBox &U, const JobBox &j, int tx) {
+        return U.i0[0] < j.x + tx && U.i0[0] + U.ld[0] > j.x && U.i0[1] < j.y + TY && U.i0[1] + U.ld[1] > j.y && U.i0[2] < j.w &&
+               U.i0[2] + U.ld[2] > j.z - 1;
+    };
+    // 2: a DFT unit meets the job's box, 1: material slots in its rows
+    auto heavy = [&](const JobBox &j, int tx) {
+        int w = 0;
+        for (const DftBox &U : I.dft)
+            if (meets(U, j, tx)) w = 2;
+        for (int c = 0; c < 3 && w < 1; ++c)
+            for (int k = std::max(j.z - 1, 0); k < std::min(j.w, I.Mz) && w < 1 && !I.rows[c].empty(); ++k)
+                for (int y = j.y; y < std::min(j.y + TY, I.My); ++y)
+                {
+                    const RowRange &rr = I.rows[c][(size_t)k * I.My + y];
+                    if (rr.lo <= rr.hi && rr.lo < j.x + tx && rr.hi >= j.x)
+                    {
+                        w = 1;
+                        break;
+                    }
+                }
+        return w;
+    };
+    JobLists J;
+    for (auto &ch : chunks)
+    {
+        const bool zin = !any(2, ch.first - 1, ch.second - 1);
+        for (int by = 0; by < std::max(I.nby, 1); ++by)
+        {
+            const int y0 = 1 + by * TY;
+            const bool yin = !any(1, y0 - 1, y0 + TY - 1);
+            const int nu = std::max(I.nbx, 1), per = TX / TXP;
+            std::vector<char> plain(nu);
+            for (int u = 0; u < nu; ++u)
+            {
+                const int x0 = first_x + u * TXP;
+                plain[u] = zin && yin && !any(0, x0 - 1, x0 + TXP - 1) &&
+                           !(slots_to_p && heavy(JobBox{x0, y0, ch.first, ch.second}, TXP) == 1);
+            }
+            for (int u = 0; u < nu;)
+            {
+                const int x0 = first_x + u * TXP;
+                bool all = u + per <= nu;
+                for (int t = 0; t < per && all; ++t) all = plain[u + t] != 0;
+                if (all)
+                {
+                    J.in.push_back(JobBox{x0, y0, ch.first, ch.second});
+                    u += per;
+                }
+                else
+                {
+                    if (x0 < I.xlim) J.b.push_back(JobBox{x0, y0, ch.first, ch.second});
+                    ++u;
+                }
+            }
+        }
+    }
+    if (dft_split > 0)
+    {
+        auto split_dft = [&](std::vector<JobBox> &v, int tx) {
+            std::vector<JobBox> o;
+            o.reserve(v.size());
+            for (const JobBox &j : v)
+            {
+                int nf = 0;
+                for (const DftBox &U : I.dft)
+                    if (meets(U, j, tx)) nf += U.nf;
+                const int planes = j.w - j.z;
+                const int m = nf ? std::max(1, std::min(planes, 1 + nf / dft_split)) : 1;
+                for (int i = 0; i < m; ++i)
+                    o.push_back(JobBox{j.x, j.y, j.z + (int)((int64_t)planes * i / m), j.z + (int)((int64_t)planes * (i + 1) / m)});
+            }
+            v.swap(o);
+        };
+        split_dft(J.b, TXP);
+        split_dft(J.in, TX);
+    }
+    if (heavy_first)
+    {
+        auto cpml_axes = [&](const JobBox &j, int tx) {
+            return (int)any(0, j.x - 1, j.x + tx - 1) + (int)any(1, j.y - 1, j.y + TY - 1) + (int)any(2, j.z - 1, j.w - 1);
+        };
+        auto order = [&](std::vector<JobBox> &v, int tx) {
+            std::vector<std::pair<int, size_t>> key(v.size());
+            for (size_t i = 0; i < v.size(); ++i) key[i] = {-(4 * heavy(v[i], tx) + (cpml_order ? cpml_axes(v[i], tx) : 0)), i};
+            std::stable_sort(key.begin(), key.end());
+            std::vector<JobBox> o(v.size());
+            for (size_t i = 0; i < v.size(); ++i) o[i] = v[key[i].second];
+            v.swap(o);
+        };
+        order(J.b, TXP);
+        order(J.in, TX);
+    }
+    for (const JobBox &j : J.in)
+        if (j.x + TX >= I.xlim || j.y + TY >= I.ylim) J.face_in_pml = false;
+    return J;
 }
 } // namespace ffipg

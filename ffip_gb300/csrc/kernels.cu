@@ -568,187 +568,66 @@ public:
                       (const void *)P.slot[1].rows, (const void *)P.slot[2].rows);
         auto it = jobs_.find(key);
         if (it != jobs_.end()) return it->second;
-        // CPML flags per position along each axis (either parity)
-        std::vector<char> pml[3];
+        // the job lists' inputs copied back from the device: CPML flags per
+        // position along each axis (either parity), E slot row ranges, DFT
+        // unit boxes (fused_plan.hpp builds the lists)
+        JobInputs I;
         const int len[3] = {L.xend, P.My, P.Mz};  // table lengths (x: the valid extent, not the padded row)
         for (int a = 0; a < 3; ++a)
         {
-            pml[a].assign(len[a], 0);
+            I.pml[a].assign(len[a], 0);
             if (!P.pc[0][0]) continue;
             for (int q = 0; q < 2; ++q)
             {
                 std::vector<T> c(len[a]);
                 check(cudaMemcpy(c.data(), P.pc[a][q], len[a] * sizeof(T), cudaMemcpyDeviceToHost), "cudaMemcpy D2H");
-                for (int i = 0; i < len[a]; ++i) pml[a][i] |= c[i] != T(0);
+                for (int i = 0; i < len[a]; ++i) I.pml[a][i] |= c[i] != T(0);
             }
         }
-        auto any = [&](int a, int lo, int hi) {  // CPML anywhere in [lo, hi]
-            for (int i = std::max(lo, 0); i <= std::min(hi, len[a] - 1); ++i)
-                if (pml[a][i]) return true;
-            return false;
-        };
-        // z: chunks [a, b) whose planes a-1 .. b-1 hold no CPML point come
-        // from the longest run f0 .. f1 of such planes (a = f0 + 1,
-        // b = f1 + 1), chunked apart from the rest
-        int za = L.kbeg, zb = L.kbeg;
-        for (int f = L.kbeg - 1; f < L.kend;)
-        {
-            int e = f;
-            while (e < L.kend && !any(2, e, e)) ++e;  // planes f .. e-1 are free
-            const int a = std::max(f + 1, L.kbeg), bnd = std::min(e, L.kend);
-            if (bnd - a > zb - za) { za = a; zb = bnd; }
-            f = e + 1;
-        }
-        std::vector<std::pair<int, int>> chunks;
-        auto split = [&](int lo, int hi) {
-            if (hi <= lo) return;
-            const int nch = (hi - lo + KCH - 1) / KCH;
-            for (int i = 0; i < nch; ++i)
-                chunks.emplace_back(lo + (int)((int64_t)(hi - lo) * i / nch), lo + (int)((int64_t)(hi - lo) * (i + 1) / nch));
-        };
-        split(L.kbeg, za);
-        split(za, zb);
-        split(zb, L.kend);
-        // E material slot row ranges, for the job weights below (H slots
-        // put their tile planes on the general path instead)
-        std::vector<RowRange> rows[3];
         for (int c = 0; c < 3; ++c)
             if (P.slot[c].map)
             {
-                rows[c].resize((size_t)P.My * P.Mz);
-                check(cudaMemcpy(rows[c].data(), P.slot[c].rows, rows[c].size() * sizeof(RowRange), cudaMemcpyDeviceToHost),
+                I.rows[c].resize((size_t)P.My * P.Mz);
+                check(cudaMemcpy(I.rows[c].data(), P.slot[c].rows, I.rows[c].size() * sizeof(RowRange), cudaMemcpyDeviceToHost),
                       "cudaMemcpy D2H");
             }
-        // 2: a DFT unit meets the job's box, 1: material slots in its rows
-        auto heavy = [&](const int4 &j, int tx) {
-            int w = 0;
-            for (int sd = 0; sd < 2; ++sd)
-            {
-                const SideParams<T> &S = sd ? p.h : p.e;
-                for (int u = 0; u < S.nunits; ++u)
-                {
-                    const DftView &U = S.units[u];
-                    if (U.i0[0] < j.x + tx && U.i0[0] + U.ld[0] > j.x && U.i0[1] < j.y + TY && U.i0[1] + U.ld[1] > j.y &&
-                        U.i0[2] < j.w && U.i0[2] + U.ld[2] > j.z - 1)
-                        w = 2;
-                }
-            }
-            for (int c = 0; c < 3 && w < 1; ++c)
-                for (int k = std::max(j.z - 1, 0); k < std::min(j.w, P.Mz) && w < 1 && !rows[c].empty(); ++k)
-                    for (int y = j.y; y < std::min(j.y + TY, P.My); ++y)
-                    {
-                        const RowRange &rr = rows[c][(size_t)k * P.My + y];
-                        if (rr.lo <= rr.hi && rr.lo < j.x + tx && rr.hi >= j.x)
-                        {
-                            w = 1;
-                            break;
-                        }
-                    }
-            return w;
-        };
-        std::vector<int4> b, in;
-        for (auto &ch : chunks)
+        for (int sd = 0; sd < 2; ++sd)
         {
-            const bool zin = !any(2, ch.first - 1, ch.second - 1);
-            for (int by = 0; by < std::max(nby, 1); ++by)
+            const SideParams<T> &S = sd ? p.h : p.e;
+            for (int u = 0; u < S.nunits; ++u)
             {
-                const int y0 = 1 + by * TY;
-                const bool yin = !any(1, y0 - 1, y0 + TY - 1);
-                // units that the interior instance may take: no CPML point in
-                // the unit with its low-x halo (nor in the row or the chunk);
-                // FFIP_FUSED_SLOTS_TO_P: nor material slots (without a DFT
-                // unit): the CPML instance's one point per thread and more
-                // CTAs per SM hide the latency of the slot loads better
-                const int nu = std::max(nbx, 1), per = TX / TXP;
-                std::vector<char> plain(nu);
-                for (int u = 0; u < nu; ++u)
+                DftBox d;
+                for (int a = 0; a < 3; ++a)
                 {
-                    const int x0 = kXFirst + u * TXP;
-                    plain[u] = zin && yin && !any(0, x0 - 1, x0 + TXP - 1) &&
-                               !(FFIP_FUSED_SLOTS_TO_P && heavy(make_int4(x0, y0, ch.first, ch.second), TXP) == 1);
+                    d.i0[a] = S.units[u].i0[a];
+                    d.ld[a] = S.units[u].ld[a];
                 }
-                for (int u = 0; u < nu;)
-                {
-                    const int x0 = kXFirst + u * TXP;
-                    bool all = u + per <= nu;
-                    for (int t = 0; t < per && all; ++t) all = plain[u + t] != 0;
-                    if (all)
-                    {
-                        in.push_back(make_int4(x0, y0, ch.first, ch.second));
-                        u += per;
-                    }
-                    else
-                    {
-                        if (x0 < L.xlim) b.push_back(make_int4(x0, y0, ch.first, ch.second));
-                        ++u;
-                    }
-                }
+                d.nf = S.units[u].nf;
+                I.dft.push_back(d);
             }
         }
-#if FFIP_FUSED_DFT_SPLIT > 0
-        // a job whose planes meet DFT monitors carries the monitors' running
-        // sums beside its field traffic (fp64 re + im per frequency, read and
-        // written): it is split along z into about 1 + (frequencies summed
-        // over the monitors it meets) / FFIP_FUSED_DFT_SPLIT shorter jobs, so
-        // that the pass does not wait on a few long ones
-        auto dft_freqs = [&](const int4 &j, int tx) {
-            int nf = 0;
-            for (int sd = 0; sd < 2; ++sd)
-            {
-                const SideParams<T> &S = sd ? p.h : p.e;
-                for (int u = 0; u < S.nunits; ++u)
-                {
-                    const DftView &U = S.units[u];
-                    if (U.i0[0] < j.x + tx && U.i0[0] + U.ld[0] > j.x && U.i0[1] < j.y + TY && U.i0[1] + U.ld[1] > j.y &&
-                        U.i0[2] < j.w && U.i0[2] + U.ld[2] > j.z - 1)
-                        nf += U.nf;
-                }
-            }
-            return nf;
-        };
-        auto split_dft = [&](std::vector<int4> &v, int tx) {
-            std::vector<int4> o;
-            o.reserve(v.size());
-            for (const int4 &j : v)
-            {
-                const int nf = dft_freqs(j, tx), planes = j.w - j.z;
-                const int m = nf ? std::max(1, std::min(planes, 1 + nf / FFIP_FUSED_DFT_SPLIT)) : 1;
-                for (int i = 0; i < m; ++i)
-                    o.push_back(make_int4(j.x, j.y, j.z + (int)((int64_t)planes * i / m), j.z + (int)((int64_t)planes * (i + 1) / m)));
-            }
-            v.swap(o);
-        };
-        split_dft(b, TXP);
-        split_dft(in, TX);
-#endif
-#if FFIP_FUSED_HEAVY_FIRST
-        // within each instance, the jobs that add DFT sums or update material
-        // slots (several times the work of a plain job) go first, so that the
-        // launch does not end on a few long jobs
-        // CPML jobs: the more axes along which the job's box meets CPML, the
-        // more psi it updates (FFIP_FUSED_CPML_ORDER)
-        auto cpml_axes = [&](const int4 &j, int tx) {
-            return (int)any(0, j.x - 1, j.x + tx - 1) + (int)any(1, j.y - 1, j.y + TY - 1) + (int)any(2, j.z - 1, j.w - 1);
-        };
-        auto order = [&](std::vector<int4> &v, int tx) {
-            std::vector<std::pair<int, size_t>> key(v.size());
-            for (size_t i = 0; i < v.size(); ++i)
-                key[i] = {-(4 * heavy(v[i], tx) + (FFIP_FUSED_CPML_ORDER ? cpml_axes(v[i], tx) : 0)), i};
-            std::stable_sort(key.begin(), key.end());
-            std::vector<int4> o(v.size());
-            for (size_t i = 0; i < v.size(); ++i) o[i] = v[key[i].second];
-            v.swap(o);
-        };
-        order(b, TXP);
-        order(in, TX);
-#endif
+        I.My = P.My;
+        I.Mz = P.Mz;
+        I.xlim = L.xlim;
+        I.ylim = L.ylim;
+        I.kbeg = L.kbeg;
+        I.kend = L.kend;
+        I.nbx = nbx;
+        I.nby = nby;
+        I.TX = TX;
+        I.TXP = TXP;
+        I.TY = TY;
+        I.KCH = KCH;
+        const JobLists JL = fused_jobs(I, kXFirst, FFIP_FUSED_SLOTS_TO_P != 0, FFIP_FUSED_DFT_SPLIT, FFIP_FUSED_HEAVY_FIRST != 0,
+                                       FFIP_FUSED_CPML_ORDER != 0);
         Jobs J;
-        J.nb = (int)b.size();
-        J.ni = (int)in.size();
-        J.face_in_pml = true;
-        for (const int4 &j : in)
-            if (j.x + TX >= L.xlim || j.y + TY >= L.ylim) J.face_in_pml = false;
-        b.insert(b.end(), in.begin(), in.end());
+        J.nb = (int)JL.b.size();
+        J.ni = (int)JL.in.size();
+        J.face_in_pml = JL.face_in_pml;
+        std::vector<int4> b;
+        b.reserve(JL.b.size() + JL.in.size());
+        for (const JobBox &jb : JL.b) b.push_back(make_int4(jb.x, jb.y, jb.z, jb.w));
+        for (const JobBox &jb : JL.in) b.push_back(make_int4(jb.x, jb.y, jb.z, jb.w));
         check(cudaMalloc(&J.dev, b.size() * sizeof(int4)), "cudaMalloc");
         check(cudaMemcpy(J.dev, b.data(), b.size() * sizeof(int4), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
         return jobs_[key] = J;

@@ -287,3 +287,134 @@ extern "C" int ffip_emu_fused_partition_check(const char *config_json, char *msg
         return fail(std::string("error: ") + e.what());
     }
 }
+
+// Test hook: the fused pass's CTA job lists (fused_plan.hpp fused_jobs, which
+// the CUDA backend runs once per grid) built from a config's plan, with the
+// interior instance's tile width tx (64: fp32, 32: fp64) and z chunks of at
+// most kch planes, checked: every 32-column unit below xlim, 8-row tile and
+// valid z plane belongs to exactly one job; no job of the instance without
+// CPML code meets CPML in its tile, low-x / low-y halo or planes (or the plane
+// below its first); jobs start on unit and tile boundaries inside the valid
+// z range.
+extern "C" int ffip_emu_fused_jobs_check(const char *config_json, int tx, int kch, char *msg, uint64_t msg_len)
+{
+    using namespace ffipg;
+    auto fail = [&](const std::string &m) {
+        if (msg && msg_len) std::snprintf(msg, msg_len, "%s", m.c_str());
+        return 1;
+    };
+    try
+    {
+        Json cfg = Json::parse(config_json);
+        Plan P;
+        build_plan(cfg, {}, P);
+        if (P.rasterize != "host") rasterize_media(P);
+        const int TXP = 32, TY = 8;
+        int xend = 0, yend = 0, kbeg = P.M[2], kend = 0;
+        for (int c = 0; c < 6; ++c)
+        {
+            xend = std::max(xend, P.vhi[c][0] + 1);
+            yend = std::max(yend, P.vhi[c][1] + 1);
+            kbeg = std::min(kbeg, P.vlo[c][2]);
+            kend = std::max(kend, P.vhi[c][2] + 1);
+        }
+        kend = std::max(kend, kbeg + 1);
+        JobInputs I;
+        fused_limits(xend, yend, kXFirst, TXP, TY, I.nbx, I.nby, I.xlim, I.ylim);
+        const int len[3] = {xend, P.M[1], P.M[2]};
+        for (int a = 0; a < 3; ++a)
+        {
+            I.pml[a].assign(len[a], 0);
+            for (int q = 0; q < 2; ++q)
+                for (int i = 0; i < len[a] && i < (int)P.pml_c[a][q].size(); ++i) I.pml[a][i] |= P.pml_c[a][q][i] != 0;
+        }
+        I.My = P.M[1];
+        I.Mz = P.M[2];
+        for (int c = 0; c < 3; ++c)
+        {
+            const SlotList &S = P.slots[c];
+            if (S.lin.empty()) continue;
+            I.rows[c].assign((size_t)I.My * I.Mz, RowRange{1, 0});
+            for (int64_t l : S.lin)
+            {
+                const int i = (int)(l % P.Mx_pad), j = (int)((l / P.Mx_pad) % P.M[1]), k = (int)(l / P.plane());
+                RowRange &r = I.rows[c][(size_t)k * I.My + j];
+                if (r.lo > r.hi) r.lo = r.hi = i;
+                else
+                {
+                    r.lo = std::min(r.lo, i);
+                    r.hi = std::max(r.hi, i);
+                }
+            }
+        }
+        for (const DftUnit &U : P.units)
+            if (U.has_local)
+            {
+                DftBox d;
+                for (int a = 0; a < 3; ++a)
+                {
+                    d.i0[a] = U.i0[a];
+                    d.ld[a] = U.ldim[a];
+                }
+                d.nf = (int)U.freqs.size();
+                I.dft.push_back(d);
+            }
+        I.kbeg = kbeg;
+        I.kend = kend;
+        I.TX = tx;
+        I.TXP = TXP;
+        I.TY = TY;
+        I.KCH = kch;
+        const JobLists J = fused_jobs(I, kXFirst, false, 4, true, false);
+        auto anyp = [&](int a, int lo, int hi) {
+            for (int i = std::max(lo, 0); i <= std::min(hi, len[a] - 1); ++i)
+                if (I.pml[a][i]) return true;
+            return false;
+        };
+        const int nu = std::max(I.nbx, 1), nby = std::max(I.nby, 1), nz = kend - kbeg;
+        std::vector<int> cover((size_t)nu * nby * nz, 0);
+        auto mark = [&](const JobBox &j, int width) -> std::string {
+            if ((j.x - kXFirst) % TXP != 0 || (j.y - 1) % TY != 0 || j.z < kbeg || j.w > kend || j.z >= j.w)
+                return "a job off the unit / tile grid or the z range";
+            for (int x0 = j.x; x0 < j.x + width; x0 += TXP)
+            {
+                const int u = (x0 - kXFirst) / TXP, by = (j.y - 1) / TY;
+                if (u >= nu || by >= nby) return "a job beyond the units / tiles";
+                for (int z = j.z; z < j.w; ++z) ++cover[((size_t)by * nu + u) * nz + (z - kbeg)];
+            }
+            return "";
+        };
+        for (const JobBox &j : J.b)
+        {
+            const std::string e = mark(j, TXP);
+            if (!e.empty()) return fail(e);
+            if (j.x >= I.xlim) return fail("a CPML job at or beyond xlim");
+        }
+        for (const JobBox &j : J.in)
+        {
+            const std::string e = mark(j, tx);
+            if (!e.empty()) return fail(e);
+            if (anyp(0, j.x - 1, j.x + tx - 1) || anyp(1, j.y - 1, j.y + TY - 1) || anyp(2, j.z - 1, j.w - 1))
+                return fail("an interior job at (" + std::to_string(j.x) + "," + std::to_string(j.y) + "," + std::to_string(j.z) +
+                            ") meets CPML");
+        }
+        for (int by = 0; by < nby; ++by)
+            for (int u = 0; u < nu; ++u)
+                for (int z = 0; z < nz; ++z)
+                {
+                    const int n = cover[((size_t)by * nu + u) * nz + z];
+                    const bool below = kXFirst + u * TXP < I.xlim;
+                    if ((below && n != 1) || n > 1)
+                        return fail("unit " + std::to_string(u) + ", tile " + std::to_string(by) + ", plane " +
+                                    std::to_string(z + kbeg) + " covered " + std::to_string(n) + " times");
+                }
+        if (msg && msg_len)
+            std::snprintf(msg, msg_len, "ok %d CPML jobs, %d interior jobs, %d units x %d tiles x %d planes", (int)J.b.size(),
+                          (int)J.in.size(), nu, nby, nz);
+        return 0;
+    }
+    catch (const std::exception &e)
+    {
+        return fail(std::string("error: ") + e.what());
+    }
+}

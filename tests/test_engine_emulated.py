@@ -236,3 +236,36 @@ def test_fused_partition_on_golden_cases_and_workloads(lib):
         assert rc == 0, msg
         mirrored += "mirror 0 0" not in msg
     assert mirrored >= 6  # the symmetry faces along x / y are mirrored, not deferred
+
+
+def jobs_check(lib, cfg, tx, kch):
+    """The fused pass's CTA job lists (fused_plan.hpp fused_jobs) on a
+    config's plan: every unit / tile / plane in exactly one job, no
+    CPML-free job meeting CPML (tests/emu/host_backend.cpp)."""
+    import ctypes
+    import json
+    fn = lib.ffip_emu_fused_jobs_check
+    fn.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_uint64]
+    fn.restype = ctypes.c_int
+    msg = ctypes.create_string_buffer(512)
+    rc = fn(json.dumps(cfg).encode(), tx, kch, msg, 512)
+    return rc, msg.value.decode()
+
+
+@pytest.mark.parametrize("tx", [32, 64])
+@pytest.mark.parametrize("kch", [4, 12, 16])
+def test_fused_jobs_cover_the_grid(lib, tx, kch):
+    """The spheres workload at 64, 128 and 256 cells (CPML on every face,
+    spheres with slots, the DFT volume), the plain vacuum box and seeded
+    random boundary configurations; the interior instance's tile is 64
+    columns wide in fp32, 32 in fp64."""
+    from ffip_gb300 import workloads
+    from test_gpu_parity import random_boundary_config
+    cfgs = [workloads.dispersive_spheres(n, steps=10) for n in (64, 128, 256)] + [workloads.vacuum_point(64)]
+    cfgs += [random_boundary_config(s) for s in range(8)]
+    interior = 0
+    for cfg in cfgs:
+        rc, msg = jobs_check(lib, cfg, tx, kch)
+        assert rc == 0, msg
+        interior += int(msg.split(" CPML jobs, ")[1].split()[0])
+    assert interior > 0  # the larger grids put jobs on the instance without CPML code
