@@ -1,7 +1,8 @@
-// Host side of the fused pass's split of a time step's points: which points
-// the pass owns, which the face kernel updates (as a list of boxes), and
-// which PEC / PMC faces the pass mirrors into the halo of its first tiles.
-// Plain C++ (no CUDA), shared by the CUDA backend and the host tests.
+// Host side of the fused pass: the split of a time step's points (which
+// points the pass owns, which the face kernel updates as a list of boxes,
+// which PEC / PMC faces the pass mirrors into the halo of its first tiles)
+// and the pass's CTA job lists.  Plain C++ (no CUDA), shared by the CUDA
+// backend and the host tests.
 #pragma once
 #include <algorithm>
 #include <cstdint>
