@@ -15,4 +15,4 @@ from .native import to_convolve_transpose as TO_convolve_transpose  # noqa: F401
 from .simulation import (PML, Adjoint_Flux, Adjoint_Source, Adjoint_Volume, Fields_DFT, Flux_Box,  # noqa: F401
                          Flux_Region, Geom_Info, Simulation, Symmetry, field_match_objective, run_until_dft,
                          run_until_fields_decay, run_until_time, sensitivity_scatter)
-from .source import Gaussian1, Gaussian2, Inhom_Source, Source  # noqa: F401
+from .source import Gaussian1, Gaussian2, Inhom_Source, Source, Source_Function  # noqa: F401
