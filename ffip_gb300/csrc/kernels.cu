@@ -628,8 +628,22 @@ public:
         b.reserve(JL.b.size() + JL.in.size());
         for (const JobBox &jb : JL.b) b.push_back(make_int4(jb.x, jb.y, jb.z, jb.w));
         for (const JobBox &jb : JL.in) b.push_back(make_int4(jb.x, jb.y, jb.z, jb.w));
+        // a new media or grid makes a new key (the slot row arrays are new):
+        // keep the lists of the last few only (a design loop re-rasterises
+        // every iteration); cudaFree waits for the launches that read them
+        if (jobs_.size() >= kJobCache)
+        {
+            auto old = jobs_.find(jobs_order_.front());
+            if (old != jobs_.end())
+            {
+                check(cudaFree(old->second.dev), "cudaFree");
+                jobs_.erase(old);
+            }
+            jobs_order_.erase(jobs_order_.begin());
+        }
         check(cudaMalloc(&J.dev, b.size() * sizeof(int4)), "cudaMalloc");
         check(cudaMemcpy(J.dev, b.data(), b.size() * sizeof(int4), cudaMemcpyHostToDevice), "cudaMemcpy H2D");
+        jobs_order_.push_back(key);
         return jobs_[key] = J;
     }
 
@@ -839,6 +853,8 @@ private:
     int *flag_{nullptr};  // result word of the divergence check
     std::map<std::tuple<const void *, int, int>, CUtensorMap> maps_;
     std::map<std::string, Jobs> jobs_;
+    std::vector<std::string> jobs_order_;  // keys of jobs_, oldest first
+    static constexpr size_t kJobCache = 8;
     cudaStream_t side_{nullptr};
     int nsm_{0};
     cudaEvent_t fork_{nullptr}, join_{nullptr}, face_h_{nullptr};
